@@ -1,0 +1,424 @@
+// api.cu -- the extern "C" entry points of libgenfire.so (declared in
+// include/genfire.h).  Each call validates its arguments the way the
+// reference's error() guards do (GENFIRE_Reconstructor.m:87-221), moves host
+// data to the device when needed, runs the kernels on the context stream and
+// returns a status; exceptions never cross the C boundary.
+#include "internal.h"
+
+#include <cstring>
+#include <functional>
+
+using gf::DevBuf;
+using gf::Error;
+
+namespace {
+
+thread_local std::string g_noctx_error;
+
+genfire_status guarded(genfire_ctx *ctx, const std::function<void()> &fn)
+{
+    try {
+        if (ctx) {
+            GF_CUDA(cudaSetDevice(ctx->device));
+            ctx->last_error.clear();
+        }
+        fn();
+        return GENFIRE_OK;
+    } catch (const Error &e) {
+        if (ctx) ctx->last_error = e.msg;
+        else g_noctx_error = e.msg;
+        return e.st;
+    } catch (const std::bad_alloc &) {
+        if (ctx) ctx->last_error = "GENFIRE: host memory exhausted";
+        return GENFIRE_ERR_OOM;
+    } catch (...) {
+        if (ctx) ctx->last_error = "GENFIRE: unexpected internal error";
+        return GENFIRE_ERR_STATE;
+    }
+}
+
+void need(const void *ptr, const char *what)
+{
+    if (!ptr) gf::fail(GENFIRE_ERR_ARG, std::string(what) + " is NULL.");
+}
+
+size_t real_size(int precision) { return precision == GENFIRE_PREC_FP64 ? sizeof(double) : sizeof(float); }
+
+}  // namespace
+
+extern "C" {
+
+int32_t genfire_abi_version(void) { return GENFIRE_ABI_VERSION; }
+
+const char *genfire_status_string(genfire_status s)
+{
+    switch (s) {
+    case GENFIRE_OK: return "ok";
+    case GENFIRE_ERR_ARG: return "invalid argument";
+    case GENFIRE_ERR_OOM: return "out of memory";
+    case GENFIRE_ERR_CUDA: return "CUDA error";
+    case GENFIRE_ERR_TIMEOUT: return "device wait timed out";
+    case GENFIRE_ERR_UNSUPPORTED: return "unsupported size";
+    case GENFIRE_ERR_STATE: return "invalid state";
+    }
+    return "unknown status";
+}
+
+genfire_status genfire_params_init(genfire_params *p)
+{
+    if (!p) return GENFIRE_ERR_ARG;
+    std::memset(p, 0, sizeof(*p));
+    // GENFIRE_Reconstructor.m:30-70
+    p->DFT_CentroSymmetricity = 1;
+    p->oversamplingRatio = 3;
+    p->interpolationCutoffDistance = 0.7;
+    p->vector1[2] = 1;  // [0 0 1]
+    p->vector2[1] = 1;  // [0 1 0]
+    p->vector3[0] = 1;  // [1 0 0]
+    p->numIterations = 50;
+    p->constraintEnforcementMode = 1;
+    p->constraintPositivity = 1;
+    p->constraintSupport = 1;
+    p->monitor_R = 0;
+    p->monitorR_loopLength = 10;
+    p->precision = GENFIRE_PREC_FP64;
+    return GENFIRE_OK;
+}
+
+genfire_status genfire_grid_size(const genfire_params *p, int32_t *n1, int32_t *n2)
+{
+    if (!p || !n1 || !n2) return GENFIRE_ERR_ARG;
+    *n1 = gf::oversampled(p->Dim1, p->oversamplingRatio);
+    *n2 = gf::oversampled(p->Dim2, p->oversamplingRatio);
+    return GENFIRE_OK;
+}
+
+genfire_status genfire_create(int32_t device, genfire_ctx **out)
+{
+    if (!out) return GENFIRE_ERR_ARG;
+    *out = nullptr;
+    genfire_ctx *c = new genfire_ctx();
+    c->device = device;
+    genfire_status st = guarded(nullptr, [&] {
+        int n = 0;
+        GF_CUDA(cudaGetDeviceCount(&n));
+        if (device < 0 || device >= n) gf::fail(GENFIRE_ERR_ARG, "device index out of range.");
+        GF_CUDA(cudaSetDevice(device));
+        GF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        GF_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+    });
+    if (st != GENFIRE_OK) {
+        delete c;
+        return st;
+    }
+    *out = c;
+    return GENFIRE_OK;
+}
+
+genfire_status genfire_destroy(genfire_ctx *ctx)
+{
+    if (!ctx) return GENFIRE_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return GENFIRE_OK;
+}
+
+const char *genfire_last_error(const genfire_ctx *ctx) { return ctx ? ctx->last_error.c_str() : g_noctx_error.c_str(); }
+
+void *genfire_stream(genfire_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+// ---------------------------------------------------------------- gridding
+genfire_status genfire_grid_dft_device(genfire_ctx *ctx, const genfire_params *p, const double *d_projections,
+                                       const double *angles, void *d_measuredK, void *d_recIFFT, int64_t *nk)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        need(d_projections, "projections");
+        need(angles, "angles");
+        need(d_measuredK, "measuredK");
+        gf::check_params(*p, true);
+        gf::grid_dft(ctx, *p, d_projections, angles, d_measuredK, d_recIFFT, nk);
+    });
+}
+
+genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p, const double *projections,
+                                const double *angles, void *measuredK, void *recIFFT, int64_t *nk)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        need(projections, "projections");
+        need(angles, "angles");
+        need(measuredK, "measuredK");
+        gf::check_params(*p, true);
+        cudaStream_t st = ctx->stream;
+        const int n1 = gf::oversampled(p->Dim1, p->oversamplingRatio);
+        const int n2 = gf::oversampled(p->Dim2, p->oversamplingRatio);
+        const size_t npj = (size_t)p->Dim1 * p->Dim2 * p->NumProjs;
+        const size_t nM = (size_t)n1 * n2 * n1 * 2 * real_size(p->precision);
+        const size_t nR = (size_t)p->Dim1 * p->Dim2 * p->Dim1 * real_size(p->precision);
+        DevBuf dp(sizeof(double) * npj, st), dM(nM, st), dR;
+        if (recIFFT) dR.alloc(nR, st);
+        GF_CUDA(cudaMemcpyAsync(dp.p, projections, sizeof(double) * npj, cudaMemcpyHostToDevice, st));
+        gf::grid_dft(ctx, *p, dp.as<double>(), angles, dM.p, recIFFT ? dR.p : nullptr, nk);
+        GF_CUDA(cudaMemcpyAsync(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st));
+        if (recIFFT) GF_CUDA(cudaMemcpyAsync(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+// ---------------------------------------------------------------- iteration
+genfire_status genfire_recon_create(genfire_ctx *ctx, const genfire_params *p, const void *measuredK,
+                                    const uint8_t *measuredK_mask, const uint8_t *support, const void *initialObject,
+                                    const double *projections, const double *angles, int32_t on_device,
+                                    genfire_recon **out)
+{
+    if (!ctx || !out) return GENFIRE_ERR_ARG;
+    *out = nullptr;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        *out = gf::recon_create(ctx, *p, measuredK, measuredK_mask, support, initialObject, projections, angles,
+                                on_device != 0);
+    });
+}
+
+genfire_status genfire_recon_iterate(genfire_recon *r, int32_t count)
+{
+    if (!r) return GENFIRE_ERR_ARG;
+    genfire_ctx *ctx = r->ctx;
+    return guarded(ctx, [&] { gf::recon_iterate(r, count); });
+}
+
+genfire_status genfire_recon_result(genfire_recon *r, void *reconstruction, double *errK, double *errR, double *Rarr,
+                                    double *Rarr2, int32_t on_device)
+{
+    if (!r) return GENFIRE_ERR_ARG;
+    genfire_ctx *ctx = r->ctx;
+    return guarded(ctx, [&] { gf::recon_result(r, reconstruction, errK, errR, Rarr, Rarr2, on_device != 0); });
+}
+
+genfire_status genfire_recon_destroy(genfire_recon *r)
+{
+    if (!r) return GENFIRE_OK;
+    genfire_ctx *ctx = r->ctx;
+    return guarded(ctx, [&] { gf::recon_destroy(r); });
+}
+
+genfire_status genfire_reconstruct(genfire_ctx *ctx, const genfire_params *p, const void *measuredK,
+                                   const uint8_t *measuredK_mask, const uint8_t *support, const void *initialObject,
+                                   const double *projections, const double *angles, void *reconstruction,
+                                   double *errK, double *errR, double *Rarr, double *Rarr2)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    genfire_recon *r = nullptr;
+    genfire_status st = genfire_recon_create(ctx, p, measuredK, measuredK_mask, support, initialObject, projections,
+                                             angles, 0, &r);
+    if (st != GENFIRE_OK) return st;
+    st = genfire_recon_iterate(r, p->numIterations);
+    if (st == GENFIRE_OK) st = genfire_recon_result(r, reconstruction, errK, errR, Rarr, Rarr2, 0);
+    std::string keep = ctx->last_error;
+    genfire_recon_destroy(r);
+    if (st != GENFIRE_OK) ctx->last_error = keep;
+    return st;
+}
+
+// ---------------------------------------------------------------- projector
+static void host_rotations(int P, const double *angles, const double *vectors, std::vector<double> &Rs)
+{
+    Rs.resize(9 * (size_t)P);
+    for (int i = 0; i < P; ++i) {
+        double *R = &Rs[9 * (size_t)i];
+        if (vectors) gf::euler_rot(vectors, vectors + 3, vectors + 6, angles[i], angles[i + P], angles[i + 2 * P], R);
+        else gf::rot_zyz(angles[i], angles[i + P], angles[i + 2 * P], R);
+    }
+}
+
+genfire_status genfire_project(genfire_ctx *ctx, int32_t precision, const void *vol, int32_t n1, int32_t n2,
+                               int32_t n3, int32_t num_proj, const double *angles, const double *vectors, void *projs)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(vol, "vol");
+        need(angles, "angles");
+        need(projs, "projs");
+        if (precision != GENFIRE_PREC_FP64 && precision != GENFIRE_PREC_MIXED) gf::fail(GENFIRE_ERR_ARG, "bad precision.");
+        if (num_proj < 1) gf::fail(GENFIRE_ERR_ARG, "num_proj must be positive.");
+        cudaStream_t st = ctx->stream;
+        const size_t es = real_size(precision);
+        std::vector<double> Rs;
+        host_rotations(num_proj, angles, vectors, Rs);
+        const size_t nv = (size_t)n1 * n2 * n3, np = (size_t)n1 * n2 * num_proj;
+        DevBuf dv(es * nv, st), dp(es * np, st), dR(sizeof(double) * Rs.size(), st);
+        GF_CUDA(cudaMemcpyAsync(dv.p, vol, es * nv, cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemcpyAsync(dR.p, Rs.data(), sizeof(double) * Rs.size(), cudaMemcpyHostToDevice, st));
+        gf::project_batch(ctx, precision, dv.p, n1, n2, n3, n1, (long long)n1 * n2, num_proj, dR.as<double>(), dp.p,
+                          nullptr, nullptr, st);
+        GF_CUDA(cudaMemcpyAsync(projs, dp.p, es * np, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+genfire_status genfire_rfactor(genfire_ctx *ctx, int32_t precision, const void *vol, int32_t n1, int32_t n2,
+                               int32_t n3, int32_t num_proj, const double *angles, const double *vectors,
+                               const double *measured, double *Rarr, double *Rarr2, double *errR)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(vol, "vol");
+        need(angles, "angles");
+        need(measured, "measured");
+        if (precision != GENFIRE_PREC_FP64 && precision != GENFIRE_PREC_MIXED) gf::fail(GENFIRE_ERR_ARG, "bad precision.");
+        if (num_proj < 1) gf::fail(GENFIRE_ERR_ARG, "num_proj must be positive.");
+        cudaStream_t st = ctx->stream;
+        const size_t es = real_size(precision);
+        std::vector<double> Rs;
+        host_rotations(num_proj, angles, vectors, Rs);
+        const size_t nv = (size_t)n1 * n2 * n3, np = (size_t)n1 * n2 * num_proj;
+        DevBuf dv(es * nv, st), dm(sizeof(double) * np, st), dR(sizeof(double) * Rs.size(), st),
+            ds(sizeof(double) * 4 * num_proj, st);
+        GF_CUDA(cudaMemcpyAsync(dv.p, vol, es * nv, cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemcpyAsync(dm.p, measured, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemcpyAsync(dR.p, Rs.data(), sizeof(double) * Rs.size(), cudaMemcpyHostToDevice, st));
+        gf::project_batch(ctx, precision, dv.p, n1, n2, n3, n1, (long long)n1 * n2, num_proj, dR.as<double>(), nullptr,
+                          dm.as<double>(), ds.as<double>(), st);
+        std::vector<double> sums(4 * (size_t)num_proj);
+        GF_CUDA(cudaMemcpyAsync(sums.data(), ds.p, sizeof(double) * sums.size(), cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+        double tot = 0;
+        for (int i = 0; i < num_proj; ++i) {
+            const double r1 = sums[4 * i] / sums[4 * i + 1];
+            const double r2 = std::sqrt(sums[4 * i + 2]) / std::sqrt(sums[4 * i + 3]);
+            if (Rarr) Rarr[i] = r1;
+            if (Rarr2) Rarr2[i] = r2;
+            tot += r1;
+        }
+        if (errR) *errR = tot / num_proj;
+    });
+}
+
+// ---------------------------------------------------------------- index and symmetry kernels
+genfire_status genfire_centro_symmetricity(genfire_ctx *ctx, const double *FS, int32_t n1, int32_t n_k1, int32_t n2,
+                                           double *measuredK)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(FS, "FS");
+        need(measuredK, "measuredK");
+        if (n1 < 1 || n2 < 1 || n_k1 != n1 / 2) gf::fail(GENFIRE_ERR_ARG, "CentroSymmetricity: n_k1 must be floor(n1/2).");
+        cudaStream_t st = ctx->stream;
+        const size_t nfs = (size_t)(n_k1 + 1) * (2 * (n2 / 2) + 1) * (2 * (n1 / 2) + 1);
+        const size_t nm = (size_t)n1 * n2 * n1;
+        DevBuf a(sizeof(double2) * nfs, st), b(sizeof(double2) * nm, st);
+        GF_CUDA(cudaMemcpyAsync(a.p, FS, sizeof(double2) * nfs, cudaMemcpyHostToDevice, st));
+        gf::centro_device(ctx, a.as<double2>(), n1, n_k1, n2, b.as<double2>());
+        GF_CUDA(cudaMemcpyAsync(measuredK, b.p, sizeof(double2) * nm, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+genfire_status genfire_hermitian_symmetrize(genfire_ctx *ctx, const double *in, int32_t d1, int32_t d2, int32_t d3,
+                                            double *out)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(in, "in");
+        need(out, "out");
+        if (d1 < 1 || d2 < 1 || d3 < 1) gf::fail(GENFIRE_ERR_ARG, "hermitianSymmetrize: bad size.");
+        cudaStream_t st = ctx->stream;
+        const size_t n = (size_t)d1 * d2 * d3;
+        DevBuf a(sizeof(double2) * n, st), b(sizeof(double2) * n, st);
+        GF_CUDA(cudaMemcpyAsync(a.p, in, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+        gf::hermitian_device(ctx, a.as<double2>(), d1, d2, d3, b.as<double2>());
+        GF_CUDA(cudaMemcpyAsync(out, b.p, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+genfire_status genfire_make_kspace_indices(genfire_ctx *ctx, int32_t d1, int32_t d2, int32_t d3, double *Q)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(Q, "Q");
+        if (d1 < 1 || d2 < 1 || d3 < 1) gf::fail(GENFIRE_ERR_ARG, "make_Kspace_indices: bad size.");
+        cudaStream_t st = ctx->stream;
+        const size_t n = (size_t)d1 * d2 * d3;
+        DevBuf a(sizeof(double) * n, st);
+        gf::kspace_device(ctx, d1, d2, d3, a.as<double>());
+        GF_CUDA(cudaMemcpyAsync(Q, a.p, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+genfire_status genfire_volumn_index(const int32_t big[3], const int32_t ori[3], int32_t out[6])
+{
+    if (!big || !ori || !out) return GENFIRE_ERR_ARG;
+    for (int i = 0; i < 3; ++i) {
+        if (ori[i] > big[i] || ori[i] < 0) {
+            g_noctx_error = "GENFIRE: paddedsize should be equal to or smaller than original volume in all dimensions!";
+            return GENFIRE_ERR_ARG;
+        }
+        // the four parity cases of My_volumn_index.m:12-28 all equal floor(big/2) - floor(ori/2)
+        const int s = big[i] / 2 - ori[i] / 2;
+        out[i] = s + 1;
+        out[i + 3] = s + ori[i];
+    }
+    return GENFIRE_OK;
+}
+
+genfire_status genfire_iffshift3_ind(genfire_ctx *ctx, const int32_t size[3], int64_t count, const int64_t *inds,
+                                     int64_t *out)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(size, "size");
+        if (count < 0) gf::fail(GENFIRE_ERR_ARG, "count must be non-negative.");
+        if (count == 0) return;
+        need(inds, "inds");
+        need(out, "out");
+        cudaStream_t st = ctx->stream;
+        DevBuf a(sizeof(long long) * count, st), b(sizeof(long long) * count, st);
+        GF_CUDA(cudaMemcpyAsync(a.p, inds, sizeof(long long) * count, cudaMemcpyHostToDevice, st));
+        const int sz[3] = {size[0], size[1], size[2]};
+        gf::iffshift_device(ctx, sz, count, a.as<long long>(), b.as<long long>());
+        GF_CUDA(cudaMemcpyAsync(out, b.p, sizeof(long long) * count, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+genfire_status genfire_select(genfire_ctx *ctx, const genfire_params *p, double phi, double theta, double psi,
+                              int64_t cap, int64_t *ind, float *dist, float *u, float *v, int64_t *count)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        need(count, "count");
+        gf::check_params(*p, false);
+        if (cap > 0) { need(ind, "ind"); need(dist, "dist"); need(u, "u"); need(v, "v"); }
+        *count = gf::select_one(ctx, *p, phi, theta, psi, cap, ind, dist, u, v);
+    });
+}
+
+genfire_status genfire_fftn(genfire_ctx *ctx, int32_t precision, void *data, int32_t n1, int32_t n2, int32_t n3,
+                            int32_t inverse)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(data, "data");
+        if (n1 < 1 || n2 < 1 || n3 < 1) gf::fail(GENFIRE_ERR_ARG, "fftn: bad size.");
+        if (precision != GENFIRE_PREC_FP64 && precision != GENFIRE_PREC_MIXED) gf::fail(GENFIRE_ERR_ARG, "bad precision.");
+        cudaStream_t st = ctx->stream;
+        const size_t nb = (size_t)n1 * n2 * n3 * 2 * real_size(precision);
+        DevBuf a(nb, st);
+        GF_CUDA(cudaMemcpyAsync(a.p, data, nb, cudaMemcpyHostToDevice, st));
+        gf::fftn_device(ctx, precision, a.p, n1, n2, n3, inverse != 0);
+        GF_CUDA(cudaMemcpyAsync(data, a.p, nb, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,780 @@
+// dr.cu -- the Fourier-constraint iteration of reconstruct.m on the GPU, the
+// recIFFT of the gridding, and the test-facing 3-D FFT.
+//
+// One iteration (reconstruct.m:117-186) is five FFT passes and two tiny
+// control kernels, captured once as a CUDA graph:
+//   ctl_begin  iteration count, constraint change points, bestErr reset
+//   F1         rows along dim 1: positivity and support, real -> half spectrum
+//   F2         dim 2 forward
+//   F3         dim 3 forward, errK terms, Fourier constraint, dim 3 inverse
+//   ctl_mid    errK = sum / sum|M|, best-object bookkeeping, output buffer
+//   I2         dim 2 inverse
+//   I1         rows along dim 1: half spectrum -> real
+// The object is held only on its "box": the Dim1 x Dim2 x Dim1 region the
+// support can be non-zero on (the whole n1 x n2 x n1 grid when the support
+// constraint is off).  Everything outside the box is multiplied by zero at
+// the next iteration and never observed (the result and the R-factor read
+// the same centred box), so the forward passes skip the zero rows and the
+// inverse passes only produce the box.
+#include "fft.cuh"
+#include "internal.h"
+
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+#include <tuple>
+
+namespace gf {
+
+// ===========================================================================
+// twiddle tables, one per (device, n, precision), kept for the process
+// ===========================================================================
+template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, void *> cache;
+    int dev = 0;
+    GF_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_tuple(dev, n, (int)sizeof(T));
+    auto it = cache.find(key);
+    if (it != cache.end()) return static_cast<const cplx<T> *>(it->second);
+    std::vector<cplx<T>> h(n);
+    const double pi = 3.14159265358979323846;
+    for (int t = 0; t < n; ++t) {
+        double a = -2.0 * pi * (double)t / (double)n;
+        h[t] = mk((T)std::cos(a), (T)std::sin(a));
+    }
+    void *d = nullptr;
+    GF_CUDA(cudaMalloc(&d, sizeof(cplx<T>) * n));
+    GF_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(cplx<T>) * n, cudaMemcpyHostToDevice, s));
+    GF_CUDA(cudaStreamSynchronize(s));
+    cache[key] = d;
+    return static_cast<const cplx<T> *>(d);
+}
+template const float2 *twiddles<float>(int, cudaStream_t);
+template const double2 *twiddles<double>(int, cudaStream_t);
+
+static FftPlan plan_or_fail(int n)
+{
+    FftPlan pl;
+    if (!make_fft_plan(n, pl))
+        fail(GENFIRE_ERR_UNSUPPORTED,
+             "FFT length " + std::to_string(n) + " has a prime factor above 7 (choose Dim*oversamplingRatio "
+             "with factors 2, 3, 5 and 7).");
+    return pl;
+}
+
+// Opt every FFT pass kernel into large dynamic shared memory once per device
+// (before any graph capture; the attribute only raises the limit).
+template <typename T> static void ensure_smem_attrs()
+{
+    static std::mutex mu;
+    static std::set<int> done;
+    int dev = 0;
+    GF_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count(dev)) return;
+    const int lim = 200 * 1024;
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_rows_r2c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_rows_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    done.insert(dev);
+}
+
+// Column pass launcher
+template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st)
+{
+    a.P = a.W + 1;
+    const size_t sm = tile_smem<T>(a.pl.n, a.W);
+    dim3 grid(cdiv(a.ncols, a.W), other);
+    k_colpass<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    GF_CHECK_LAUNCH();
+}
+
+template <typename T> static void launch_rows(RowPassArgs<T> a, bool forward, cudaStream_t st)
+{
+    a.P = a.W + 1;
+    const size_t sm = tile_smem<T>(a.pl.n, a.W);
+    const int pairs = (a.nrows + 1) / 2;
+    dim3 grid(cdiv(pairs, a.W));
+    if (forward) k_rows_r2c<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    else k_rows_c2r<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    GF_CHECK_LAUNCH();
+}
+
+// ===========================================================================
+// half spectrum of the Hermitian part of a centred grid:
+// H(q) = (M(q) + conj(M(-q))) / 2 for q1 in [0, h1), FFT order
+// ===========================================================================
+template <typename T>
+__global__ void k_half_from_centered(const cplx<T> *__restrict__ M, int n1, int n2, int h1, int ld1,
+                                     cplx<T> *__restrict__ H)
+{
+    const long long N = (long long)h1 * n2 * n1;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
+        const int q1 = (int)(o % h1);
+        const long long r = o / h1;
+        const int q2 = (int)(r % n2), q3 = (int)(r / n2);
+        const long long a = (long long)((q1 + n1 / 2) % n1) + (long long)n1 * (((q2 + n2 / 2) % n2) + (long long)n2 * ((q3 + n1 / 2) % n1));
+        const int m1 = (n1 - q1) % n1, m2 = (n2 - q2) % n2, m3 = (n1 - q3) % n1;
+        const long long b = (long long)((m1 + n1 / 2) % n1) + (long long)n1 * (((m2 + n2 / 2) % n2) + (long long)n2 * ((m3 + n1 / 2) % n1));
+        const cplx<T> x = M[a], y = M[b];
+        H[q1 + (long long)ld1 * (q2 + (long long)n2 * q3)] = mk((T)0.5 * (x.x + y.x), (T)0.5 * (x.y - y.y));
+    }
+}
+
+static unsigned grid_for(genfire_ctx *ctx, long long n, int threads)
+{
+    long long b = (n + threads - 1) / threads;
+    long long cap = (long long)ctx->sm_count * 8;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+static int round_up(int a, int b) { return (a + b - 1) / b * b; }
+
+// inverse chain: half spectrum Hs (ld1 x n2 x n1) -> real box B1 x B2 x B3
+template <typename T> struct InvChain {
+    int n1, n2, h1, ld1, B1, B2, B3;
+    FftPlan pl1, pl2, pl3;
+    const cplx<T> *tw1, *tw2, *tw3;
+    int W1, W2, W3;
+};
+
+template <typename T> static InvChain<T> make_chain(int n1, int n2, int B1, int B2, int B3, cudaStream_t st)
+{
+    InvChain<T> c;
+    c.n1 = n1; c.n2 = n2; c.h1 = n1 / 2 + 1; c.ld1 = round_up(c.h1, 8);
+    c.B1 = B1; c.B2 = B2; c.B3 = B3;
+    c.pl1 = plan_or_fail(n1); c.pl2 = plan_or_fail(n2); c.pl3 = c.pl1;
+    c.tw1 = twiddles<T>(n1, st); c.tw2 = twiddles<T>(n2, st); c.tw3 = c.tw1;
+    c.W1 = tile_width<T>(n1); c.W2 = tile_width<T>(n2); c.W3 = c.W1;
+    return c;
+}
+
+template <typename T> static ColPassArgs<T> colargs(const FftPlan &pl, const cplx<T> *tw, int W, int ncols)
+{
+    ColPassArgs<T> a;
+    std::memset(&a, 0, sizeof(a));
+    a.pl = pl; a.tw = tw; a.W = W; a.ncols = ncols; a.col_stride = 1; a.scale = (T)1;
+    return a;
+}
+
+template <typename T>
+static void rec_ifft_t(genfire_ctx *ctx, const cplx<T> *d_M, int n1, int n2, int D1, int D2, T *d_rec)
+{
+    cudaStream_t st = ctx->stream;
+    ensure_smem_attrs<T>();
+    InvChain<T> c = make_chain<T>(n1, n2, D1, D2, D1, st);
+    DevBuf H(sizeof(cplx<T>) * (size_t)c.ld1 * n2 * n1, st);
+    DevBuf Y(sizeof(cplx<T>) * (size_t)c.ld1 * n2 * D1, st);
+    DevBuf Z(sizeof(cplx<T>) * (size_t)c.ld1 * D2 * D1, st);
+    k_half_from_centered<T><<<grid_for(ctx, (long long)c.h1 * n2 * n1, 256), 256, 0, st>>>(d_M, n1, n2, c.h1, c.ld1, H.as<cplx<T>>());
+    GF_CHECK_LAUNCH();
+    // dim 3 inverse: all n1 entries in, the D1 box entries out
+    ColPassArgs<T> a = colargs<T>(c.pl3, c.tw3, c.W3, c.h1);
+    a.in = H.as<cplx<T>>(); a.in_dim = (long long)c.ld1 * n2; a.in_other = c.ld1; a.in_cnt = n1; a.in_c = 0;
+    a.out = Y.as<cplx<T>>(); a.out_dim = (long long)c.ld1 * n2; a.out_other = c.ld1; a.out_cnt = D1; a.out_c = D1 / 2;
+    a.mode = 2;
+    launch_colpass<T>(a, n2, st);
+    // dim 2 inverse
+    ColPassArgs<T> b = colargs<T>(c.pl2, c.tw2, c.W2, c.h1);
+    b.in = Y.as<cplx<T>>(); b.in_dim = c.ld1; b.in_other = (long long)c.ld1 * n2; b.in_cnt = n2; b.in_c = 0;
+    b.out = Z.as<cplx<T>>(); b.out_dim = c.ld1; b.out_other = (long long)c.ld1 * D2; b.out_cnt = D2; b.out_c = D2 / 2;
+    b.mode = 2;
+    launch_colpass<T>(b, D1, st);
+    // dim 1 C2R
+    RowPassArgs<T> r;
+    std::memset(&r, 0, sizeof(r));
+    r.pl = c.pl1; r.tw = c.tw1; r.W = c.W1; r.nrows = D2 * D1; r.B1 = D1; r.c1 = D1 / 2; r.h1 = c.h1; r.ld1 = c.ld1;
+    r.xs[0] = d_rec; r.xsel = nullptr; r.Y = Z.as<cplx<T>>();
+    r.scale = (T)(1.0 / ((double)n1 * n2 * n1));
+    launch_rows<T>(r, false, st);
+}
+
+void rec_ifft(genfire_ctx *ctx, int precision, const void *d_M, int n1, int n2, int D1, int D2, void *d_rec)
+{
+    if (precision == GENFIRE_PREC_FP64)
+        rec_ifft_t<double>(ctx, (const double2 *)d_M, n1, n2, D1, D2, (double *)d_rec);
+    else
+        rec_ifft_t<float>(ctx, (const float2 *)d_M, n1, n2, D1, D2, (float *)d_rec);
+}
+
+// ===========================================================================
+// plain 3-D FFT (fftn / ifftn) on a full complex array
+// ===========================================================================
+template <typename T> static void fftn_t(genfire_ctx *ctx, cplx<T> *d, int n1, int n2, int n3, bool inv)
+{
+    cudaStream_t st = ctx->stream;
+    ensure_smem_attrs<T>();
+    const int dims[3] = {n1, n2, n3};
+    int last = -1;
+    for (int ax = 0; ax < 3; ++ax)
+        if (dims[ax] > 1) last = ax;
+    const T sc = inv ? (T)(1.0 / ((double)n1 * n2 * n3)) : (T)1;
+    for (int ax = 0; ax < 3; ++ax) {
+        const int n = dims[ax];
+        if (n == 1) continue;
+        ColPassArgs<T> a = colargs<T>(plan_or_fail(n), twiddles<T>(n, st), tile_width<T>(n), 0);
+        a.mode = inv ? 2 : 1;
+        a.in = d; a.out = d; a.in_cnt = a.out_cnt = n; a.in_c = a.out_c = 0;
+        a.scale = (ax == last) ? sc : (T)1;
+        int other = 1;
+        if (ax == 0) {
+            a.col_stride = n1; a.ncols = n2 * n3; a.in_dim = a.out_dim = 1;
+        } else if (ax == 1) {
+            a.ncols = n1; a.in_dim = a.out_dim = n1; a.in_other = a.out_other = (long long)n1 * n2; other = n3;
+        } else {
+            a.ncols = n1; a.in_dim = a.out_dim = (long long)n1 * n2; a.in_other = a.out_other = n1; other = n2;
+        }
+        launch_colpass<T>(a, other, st);
+    }
+}
+
+void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, int n3, bool inverse)
+{
+    if (precision == GENFIRE_PREC_FP64) fftn_t<double>(ctx, (double2 *)d_data, n1, n2, n3, inverse);
+    else fftn_t<float>(ctx, (float2 *)d_data, n1, n2, n3, inverse);
+}
+
+// ===========================================================================
+// the iteration
+// ===========================================================================
+struct Ctl {
+    int it;       // iterations completed
+    int cur;      // next entry of the change-point list (0-based currentCutoffNum)
+    int cidx;     // delay indicator in force
+    int xcur;     // buffer holding the current object
+    int xnext;    // buffer the next object is written to
+    int xbest;    // buffer holding the best object (-1: none yet)
+    int m;        // number of delay indicators
+    int pad;
+    double bestErr;
+    double errK;
+};
+
+// reconstruct.m:118-124
+__global__ void k_ctl_begin(Ctl *c, const int *__restrict__ changes)
+{
+    if (threadIdx.x != 0) return;
+    c->xcur = c->xnext;
+    const int it = ++c->it;
+    if (c->cur < c->m && it == changes[c->cur]) {
+        int last = c->cur;
+        for (int k = 0; k < c->m; ++k)
+            if (changes[k] == it) last = k;
+        c->cidx = last;
+        c->cur = last + 1;
+        c->bestErr = 1e30;
+    }
+}
+
+// reconstruct.m:135 and :149-153
+__global__ void __launch_bounds__(1024) k_ctl_mid(Ctl *c, const double *__restrict__ partial, int np, double denom,
+                                                  double *__restrict__ hist)
+{
+    __shared__ double red[32];
+    double s = 0;
+    const int per = (np + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(b + per, np);
+    for (int i = b; i < e; ++i) s += partial[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) {
+            const double err = v / denom;
+            c->errK = err;
+            hist[c->it - 1] = err;
+            if (err < c->bestErr) {
+                c->bestErr = err;
+                c->xbest = c->xcur;
+            }
+            c->xnext = (c->xbest == c->xcur) ? 1 - c->xcur : c->xcur;
+        }
+    }
+}
+
+// Constraint table: one entry per half-spectrum point q with q in E or -q in E
+// (E = measuredK ~= 0 & mask, reconstruct.m:99), grouped by column q1 + h1*q2.
+struct TabGeom {
+    int n1, n2, h1, W3, m;
+    double delay[32];
+};
+
+template <typename T>
+__device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask,
+                                          const TabGeom &g, int q1, int q2, int q3, TabEntry<T> &e, double &absM)
+{
+    const int n1 = g.n1, n2 = g.n2;
+    const int c1 = (q1 + n1 / 2) % n1, c2 = (q2 + n2 / 2) % n2, c3 = (q3 + n1 / 2) % n1;
+    const int m1 = (n1 - q1) % n1, m2 = (n2 - q2) % n2, m3 = (n1 - q3) % n1;
+    const int d1 = (m1 + n1 / 2) % n1, d2 = (m2 + n2 / 2) % n2, d3 = (m3 + n1 / 2) % n1;
+    const long long a = c1 + (long long)n1 * (c2 + (long long)n2 * c3);
+    const long long b = d1 + (long long)n1 * (d2 + (long long)n2 * d3);
+    const cplx<T> Ma = M[a], Mb = M[b];
+    const bool inEq = (Ma.x != 0 || Ma.y != 0) && (!mask || mask[a]);
+    const bool inEm = (Mb.x != 0 || Mb.y != 0) && (!mask || mask[b]);
+    absM = 0;
+    if (!inEq && !inEm) return false;
+    const bool mate_stored = m1 < g.h1;
+    e.pos = (uint32_t)q3 | ((uint32_t)(q1 % g.W3) << 16);
+    e.eflags = (inEq ? 1u : 0u) | ((inEm && !mate_stored) ? 2u : 0u);
+    // constraintIndicators = 1 - Q (reconstruct.m:36-42, make_Kspace_indices.m)
+    auto kv = [](int n, int i) -> double {
+        if (n == 1) return 0.0;
+        const int r = (n % 2 == 0) ? n / 2 : (n - 1) / 2;
+        return (double)(i - r) / (double)r;
+    };
+    uint32_t cq = 0, cm = 0;
+    if (inEq) {
+        const double kx = kv(n2, c2), ky = kv(n1, c1), kz = kv(n1, c3);
+        const double ci = 1.0 - sqrt(kx * kx + ky * ky + kz * kz);
+        for (int k = 0; k < g.m; ++k) cq |= (ci > g.delay[k]) ? (1u << k) : 0u;
+        absM += sqrt((double)Ma.x * Ma.x + (double)Ma.y * Ma.y);
+    }
+    if (inEm) {
+        const double kx = kv(n2, d2), ky = kv(n1, d1), kz = kv(n1, d3);
+        const double ci = 1.0 - sqrt(kx * kx + ky * ky + kz * kz);
+        for (int k = 0; k < g.m; ++k) cm |= (ci > g.delay[k]) ? (1u << k) : 0u;
+        if (!mate_stored) absM += sqrt((double)Mb.x * Mb.x + (double)Mb.y * Mb.y);
+    }
+    e.cq = cq;
+    e.cmq = cm;
+    e.Mq = Ma;
+    e.Mmq = Mb;
+    return true;
+}
+
+template <typename T>
+__global__ void k_tab_count(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask, TabGeom g,
+                            int *__restrict__ counts, double *__restrict__ colsum)
+{
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.h1 * g.n2) return;
+    const int q1 = col % g.h1, q2 = col / g.h1;
+    int cnt = 0;
+    double s = 0;
+    for (int q3 = 0; q3 < g.n1; ++q3) {
+        TabEntry<T> e;
+        double am;
+        if (tab_point<T>(M, mask, g, q1, q2, q3, e, am)) { ++cnt; s += am; }
+    }
+    counts[col] = cnt;
+    colsum[col] = s;
+}
+
+template <typename T>
+__global__ void k_tab_write(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask, TabGeom g,
+                            const int *__restrict__ off, TabEntry<T> *__restrict__ tab)
+{
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= g.h1 * g.n2) return;
+    const int q1 = col % g.h1, q2 = col / g.h1;
+    int o = off[col];
+    for (int q3 = 0; q3 < g.n1; ++q3) {
+        TabEntry<T> e;
+        double am;
+        if (tab_point<T>(M, mask, g, q1, q2, q3, e, am)) tab[o++] = e;
+    }
+}
+
+// exclusive scan of n ints (single CTA) and the total in off[n]; also the
+// ordered sum of the column sums
+__global__ void __launch_bounds__(1024) k_scan_cols(const int *__restrict__ counts, const double *__restrict__ colsum,
+                                                    int n, int *__restrict__ off, double *__restrict__ total)
+{
+    __shared__ long long part[1024];
+    __shared__ double dpart[1024];
+    const int per = (n + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(b + per, n);
+    long long s = 0;
+    double d = 0;
+    for (int i = b; i < e; ++i) { s += counts[i]; d += colsum[i]; }
+    part[threadIdx.x] = s;
+    dpart[threadIdx.x] = d;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long run = 0;
+        double dr = 0;
+        for (int i = 0; i < (int)blockDim.x; ++i) { long long t = part[i]; part[i] = run; run += t; dr += dpart[i]; }
+        off[n] = (int)run;
+        *total = dr;
+    }
+    __syncthreads();
+    long long run = part[threadIdx.x];
+    for (int i = b; i < e; ++i) { off[i] = (int)run; run += counts[i]; }
+}
+
+// Object in box coordinates from an initial object (D1 x D2 x D1) or zeros.
+template <typename T>
+__global__ void k_place(const T *__restrict__ init, int D1, int D2, int B1, int B2, int B3, T *__restrict__ x)
+{
+    const long long N = (long long)B1 * B2 * B3;
+    const int o1 = B1 / 2 - D1 / 2, o2 = B2 / 2 - D2 / 2, o3 = B3 / 2 - D1 / 2;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        const int e1 = (int)(i % B1);
+        const long long r = i / B1;
+        const int e2 = (int)(r % B2), e3 = (int)(r / B2);
+        const int a = e1 - o1, b = e2 - o2, c = e3 - o3;
+        T v = 0;
+        if (init && a >= 0 && a < D1 && b >= 0 && b < D2 && c >= 0 && c < D1) v = init[a + (long long)D1 * (b + (long long)D2 * c)];
+        x[i] = v;
+    }
+}
+
+// reconstruction = My_stripzero(fftshift(best), [D1 D2 D1]) with the best
+// object taken after positivity and support (reconstruct.m:126-131, 152, 192)
+template <typename T>
+__global__ void k_extract(const T *const *__restrict__ xs, const Ctl *__restrict__ c, const uint8_t *__restrict__ S,
+                          int positivity, int D1, int D2, int B1, int B2, int B3, T *__restrict__ out)
+{
+    const long long N = (long long)D1 * D2 * D1;
+    const int o1 = B1 / 2 - D1 / 2, o2 = B2 / 2 - D2 / 2, o3 = B3 / 2 - D1 / 2;
+    const int sel = c->xbest;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+        T v = 0;
+        if (sel >= 0) {
+            const int a = (int)(i % D1);
+            const long long r = i / D1;
+            const int b = (int)(r % D2), cc = (int)(r / D2);
+            const long long bi = (a + o1) + (long long)B1 * ((b + o2) + (long long)B2 * (cc + o3));
+            v = xs[sel][bi];
+            if (positivity && v < (T)0) v = 0;
+            if (S) v = v * (T)S[bi];
+        }
+        out[i] = v;
+    }
+}
+
+struct ReconBase {
+    virtual ~ReconBase() {}
+    virtual void iterate(int count) = 0;
+    virtual void result(void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device) = 0;
+};
+
+template <typename T> struct ReconT : ReconBase {
+    genfire_ctx *ctx;
+    genfire_params p;
+    int n1, n2, D1, D2, h1, ld1, B1, B2, B3, W1, W2, W3;
+    FftPlan pl1, pl2;
+    const cplx<T> *tw1, *tw2;
+    DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
+    int m = 0, nparts = 0, tiles1 = 0;
+    double denom = 0;
+    int it_done = 0;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<double> errR, Rarr, Rarr2;
+
+    ~ReconT() override
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        cudaStreamSynchronize(ctx->stream);
+    }
+
+    void setup(const void *Min, const uint8_t *maskin, const uint8_t *support, const void *initial,
+               const double *projs, const double *angles, bool on_device)
+    {
+        cudaStream_t st = ctx->stream;
+        const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        D1 = p.Dim1; D2 = p.Dim2;
+        n1 = oversampled(D1, p.oversamplingRatio);
+        n2 = oversampled(D2, p.oversamplingRatio);
+        if (n1 < D1 || n2 < D2) fail(GENFIRE_ERR_ARG, "oversampled size smaller than the projection size.");
+        h1 = n1 / 2 + 1;
+        ld1 = round_up(h1, 8);
+        if (p.constraintSupport) { B1 = D1; B2 = D2; B3 = D1; }
+        else { B1 = n1; B2 = n2; B3 = n1; }
+        pl1 = plan_or_fail(n1);
+        pl2 = plan_or_fail(n2);
+        tw1 = twiddles<T>(n1, st);
+        tw2 = twiddles<T>(n2, st);
+        W1 = tile_width<T>(n1); W2 = tile_width<T>(n2); W3 = W1;
+        if (W3 > 16) fail(GENFIRE_ERR_STATE, "internal: tile width too large for the table format.");
+        const long long N = (long long)n1 * n2 * n1, NB = (long long)B1 * B2 * B3;
+
+        // delays and change points (GENFIRE_Reconstructor.m:156-165, reconstruct.m:103)
+        double delay[32];
+        int mm = 0;
+        const int mode = p.constraintEnforcementMode;
+        if (mode == 1 || mode == 2) {
+            for (int k = 0; k < 12; ++k) delay[mm++] = 0.95 + k * -0.1;
+            delay[mm++] = -10; delay[mm++] = -10;
+            if (mode == 1) {
+                delay[mm++] = -10;
+                for (int k = 0; k < 12; ++k) delay[mm++] = -0.15 + k * 0.1;
+            }
+        } else if (mode == 3) {
+            for (int k = 0; k < 5; ++k) delay[mm++] = -999;
+        } else {
+            fail(GENFIRE_ERR_ARG, "ERROR! constraintEnforcementMode value " + std::to_string(mode) + " not understood");
+        }
+        m = mm;
+        std::vector<int> ch(m);
+        const int Nit = p.numIterations;
+        for (int i = 0; i < m; ++i) {
+            double y = (m == 1) ? (double)Nit : 1.0 + ((double)i * (double)(Nit - 1)) / (double)(m - 1);
+            if (i == m - 1) y = Nit;
+            ch[i] = (int)mround(y);
+        }
+        changes.alloc(sizeof(int) * m, st);
+        GF_CUDA(cudaMemcpyAsync(changes.p, ch.data(), sizeof(int) * m, cudaMemcpyHostToDevice, st));
+
+        // measured data on the device
+        M.alloc(sizeof(cplx<T>) * N, st);
+        GF_CUDA(cudaMemcpyAsync(M.p, Min, sizeof(cplx<T>) * N, kind, st));
+        if (maskin) {
+            mask.alloc(N, st);
+            GF_CUDA(cudaMemcpyAsync(mask.p, maskin, N, kind, st));
+        }
+        // constraint table
+        TabGeom g;
+        g.n1 = n1; g.n2 = n2; g.h1 = h1; g.W3 = W3; g.m = m;
+        for (int k = 0; k < 32; ++k) g.delay[k] = k < m ? delay[k] : 0.0;
+        const int ncol = h1 * n2;
+        DevBuf counts(sizeof(int) * ncol, st), colsum(sizeof(double) * ncol, st), dtot(sizeof(double), st);
+        taboff.alloc(sizeof(int) * (ncol + 1), st);
+        k_tab_count<T><<<cdiv(ncol, 128), 128, 0, st>>>(M.as<cplx<T>>(), mask.as<uint8_t>(), g, counts.as<int>(), colsum.as<double>());
+        GF_CHECK_LAUNCH();
+        k_scan_cols<<<1, 1024, 0, st>>>(counts.as<int>(), colsum.as<double>(), ncol, taboff.as<int>(), dtot.as<double>());
+        GF_CHECK_LAUNCH();
+        int ntab = 0;
+        GF_CUDA(cudaMemcpyAsync(&ntab, taboff.as<int>() + ncol, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaMemcpyAsync(&denom, dtot.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+        tab.alloc(sizeof(TabEntry<T>) * (size_t)std::max(ntab, 1), st);
+        k_tab_write<T><<<cdiv(ncol, 128), 128, 0, st>>>(M.as<cplx<T>>(), mask.as<uint8_t>(), g, taboff.as<int>(), tab.as<TabEntry<T>>());
+        GF_CHECK_LAUNCH();
+
+        // object buffers, support
+        for (int k = 0; k < 2; ++k) xbuf[k].alloc(sizeof(T) * NB, st);
+        {
+            DevBuf init;
+            const T *dinit = nullptr;
+            if (initial) {
+                const size_t nb = sizeof(T) * (size_t)D1 * D2 * D1;
+                if (on_device) dinit = static_cast<const T *>(initial);
+                else {
+                    init.alloc(nb, st);
+                    GF_CUDA(cudaMemcpyAsync(init.p, initial, nb, cudaMemcpyHostToDevice, st));
+                    dinit = init.as<T>();
+                }
+            }
+            k_place<T><<<grid_for(ctx, NB, 256), 256, 0, st>>>(dinit, D1, D2, B1, B2, B3, xbuf[0].as<T>());
+            GF_CHECK_LAUNCH();
+            GF_CUDA(cudaStreamSynchronize(st));
+        }
+        GF_CUDA(cudaMemsetAsync(xbuf[1].p, 0, xbuf[1].bytes, st));
+        T *hp[2] = {xbuf[0].as<T>(), xbuf[1].as<T>()};
+        xptrs.alloc(sizeof(hp), st);
+        GF_CUDA(cudaMemcpyAsync(xptrs.p, hp, sizeof(hp), cudaMemcpyHostToDevice, st));
+        if (p.constraintSupport) {
+            const size_t ns = (size_t)D1 * D2 * D1;
+            S.alloc(ns, st);
+            if (support) GF_CUDA(cudaMemcpyAsync(S.p, support, ns, kind, st));
+            else GF_CUDA(cudaMemsetAsync(S.p, 1, ns, st));
+        }
+        Y1.alloc(sizeof(cplx<T>) * (size_t)ld1 * B2 * B3, st);
+        Y2.alloc(sizeof(cplx<T>) * (size_t)ld1 * n2 * B3, st);
+        tiles1 = (int)cdiv(h1, W3);
+        nparts = tiles1 * n2;
+        partial.alloc(sizeof(double) * nparts, st);
+        hist.alloc(sizeof(double) * std::max(Nit, 1), st);
+        GF_CUDA(cudaMemsetAsync(hist.p, 0, hist.bytes, st));
+        Ctl c0;
+        std::memset(&c0, 0, sizeof(c0));
+        c0.m = m; c0.xbest = -1; c0.bestErr = 1e30;
+        ctl.alloc(sizeof(Ctl), st);
+        GF_CUDA(cudaMemcpyAsync(ctl.p, &c0, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+
+        // R-factor monitor inputs (reconstruct.m:168-185; ZYZ closed-form projector)
+        if (p.monitor_R == 1) {
+            if (!projs || !angles) fail(GENFIRE_ERR_ARG, "monitor_R needs projections and angles.");
+            if (p.monitorR_loopLength < 1) fail(GENFIRE_ERR_ARG, "monitorR_loopLength must be positive.");
+            const int P = p.NumProjs;
+            const size_t npj = (size_t)D1 * D2 * P;
+            dmeas.alloc(sizeof(double) * npj, st);
+            GF_CUDA(cudaMemcpyAsync(dmeas.p, projs, sizeof(double) * npj, kind, st));
+            std::vector<double> Rs(9 * (size_t)P), ang(3 * (size_t)P);
+            if (on_device) GF_CUDA(cudaMemcpyAsync(ang.data(), angles, sizeof(double) * 3 * P, cudaMemcpyDeviceToHost, st));
+            else std::memcpy(ang.data(), angles, sizeof(double) * 3 * P);
+            GF_CUDA(cudaStreamSynchronize(st));
+            for (int i = 0; i < P; ++i) rot_zyz(ang[i], ang[i + P], ang[i + 2 * P], &Rs[9 * (size_t)i]);
+            dR.alloc(sizeof(double) * Rs.size(), st);
+            GF_CUDA(cudaMemcpyAsync(dR.p, Rs.data(), sizeof(double) * Rs.size(), cudaMemcpyHostToDevice, st));
+            dsums.alloc(sizeof(double) * 4 * P, st);
+        }
+        GF_CUDA(cudaStreamSynchronize(st));
+        build_graph();
+    }
+
+    void enqueue_iteration(cudaStream_t st)
+    {
+        Ctl *c = ctl.as<Ctl>();
+        k_ctl_begin<<<1, 32, 0, st>>>(c, changes.as<int>());
+        GF_CHECK_LAUNCH();
+        // F1: rows (dim 1) real -> half spectrum, with positivity and support
+        RowPassArgs<T> r;
+        std::memset(&r, 0, sizeof(r));
+        r.pl = pl1; r.tw = tw1; r.W = W1; r.nrows = B2 * B3; r.B1 = B1; r.c1 = B1 / 2; r.h1 = h1; r.ld1 = ld1;
+        r.xs[0] = xbuf[0].as<T>(); r.xs[1] = xbuf[1].as<T>(); r.xsel = &c->xcur;
+        r.support = p.constraintSupport ? S.as<uint8_t>() : nullptr;
+        r.positivity = p.constraintPositivity;
+        r.Y = Y1.as<cplx<T>>();
+        r.scale = (T)1;
+        launch_rows<T>(r, true, st);
+        // F2: dim 2 forward, box rows in, all n2 frequencies out
+        ColPassArgs<T> a = colargs<T>(pl2, tw2, W2, h1);
+        a.in = Y1.as<cplx<T>>(); a.in_dim = ld1; a.in_other = (long long)ld1 * B2; a.in_cnt = B2; a.in_c = B2 / 2;
+        a.out = Y2.as<cplx<T>>(); a.out_dim = ld1; a.out_other = (long long)ld1 * n2; a.out_cnt = n2; a.out_c = 0;
+        a.mode = 1;
+        launch_colpass<T>(a, B3, st);
+        // F3: dim 3 forward, constraint, dim 3 inverse (in place)
+        ColPassArgs<T> b = colargs<T>(pl1, tw1, W3, h1);
+        b.in = Y2.as<cplx<T>>(); b.in_dim = (long long)ld1 * n2; b.in_other = ld1; b.in_cnt = B3; b.in_c = B3 / 2;
+        b.out = Y2.as<cplx<T>>(); b.out_dim = (long long)ld1 * n2; b.out_other = ld1; b.out_cnt = B3; b.out_c = B3 / 2;
+        b.mode = 1 | 2 | 4;
+        b.tab_off = taboff.as<int>(); b.tab = tab.as<TabEntry<T>>(); b.h1 = h1; b.partial = partial.as<double>();
+        b.cidx = &c->cidx;
+        launch_colpass<T>(b, n2, st);
+        k_ctl_mid<<<1, 1024, 0, st>>>(c, partial.as<double>(), nparts, denom, hist.as<double>());
+        GF_CHECK_LAUNCH();
+        // I2: dim 2 inverse, box rows out
+        ColPassArgs<T> d = colargs<T>(pl2, tw2, W2, h1);
+        d.in = Y2.as<cplx<T>>(); d.in_dim = ld1; d.in_other = (long long)ld1 * n2; d.in_cnt = n2; d.in_c = 0;
+        d.out = Y1.as<cplx<T>>(); d.out_dim = ld1; d.out_other = (long long)ld1 * B2; d.out_cnt = B2; d.out_c = B2 / 2;
+        d.mode = 2;
+        launch_colpass<T>(d, B3, st);
+        // I1: rows half spectrum -> real box, 1/N
+        RowPassArgs<T> q = r;
+        q.xsel = &c->xnext;
+        q.support = nullptr;
+        q.positivity = 0;
+        q.scale = (T)(1.0 / ((double)n1 * n2 * n1));
+        launch_rows<T>(q, false, st);
+    }
+
+    void build_graph()
+    {
+        cudaStream_t st = ctx->stream;
+        ensure_smem_attrs<T>();  // kernel attributes are set outside the capture
+        cudaGraph_t graph = nullptr;
+        GF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            enqueue_iteration(st);
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        GF_CUDA(cudaStreamEndCapture(st, &graph));
+        cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        GF_CUDA(e);
+    }
+
+    void monitor()
+    {
+        cudaStream_t st = ctx->stream;
+        Ctl hc;
+        GF_CUDA(cudaMemcpyAsync(&hc, ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+        // model = fftshift(x)(Vol_ind): the centred D1 x D2 x D1 part of the box
+        const int o1 = B1 / 2 - D1 / 2, o2 = B2 / 2 - D2 / 2, o3 = B3 / 2 - D1 / 2;
+        const T *base = xbuf[hc.xnext].as<T>() + (o1 + (long long)B1 * (o2 + (long long)B2 * o3));
+        const int P = p.NumProjs;
+        project_batch(ctx, p.precision, base, D1, D2, D1, B1, (long long)B1 * B2, P, dR.as<double>(), nullptr,
+                      dmeas.as<double>(), dsums.as<double>(), st);
+        std::vector<double> sums(4 * (size_t)P);
+        GF_CUDA(cudaMemcpyAsync(sums.data(), dsums.p, sizeof(double) * 4 * P, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+        double s1 = 0;
+        for (int i = 0; i < P; ++i) {
+            const double r1 = sums[4 * i] / sums[4 * i + 1];
+            const double r2 = std::sqrt(sums[4 * i + 2]) / std::sqrt(sums[4 * i + 3]);
+            Rarr.push_back(r1);
+            Rarr2.push_back(r2);
+            s1 += r1;
+        }
+        errR.push_back(s1 / P);
+    }
+
+    void iterate(int count) override
+    {
+        if (count < 0 || it_done + count > p.numIterations)
+            fail(GENFIRE_ERR_STATE, "iterate: more iterations requested than numIterations.");
+        cudaStream_t st = ctx->stream;
+        for (int i = 0; i < count; ++i) {
+            GF_CUDA(cudaGraphLaunch(exec, st));
+            ++it_done;
+            if (p.monitor_R == 1 && it_done % p.monitorR_loopLength == 0) monitor();
+        }
+        GF_CUDA(cudaStreamSynchronize(st));
+    }
+
+    void result(void *rec, double *errK, double *eR, double *RA, double *RA2, bool on_device) override
+    {
+        cudaStream_t st = ctx->stream;
+        const size_t nv = (size_t)D1 * D2 * D1;
+        DevBuf out;
+        T *dout;
+        if (on_device) dout = static_cast<T *>(rec);
+        else { out.alloc(sizeof(T) * nv, st); dout = out.as<T>(); }
+        if (rec) {
+            k_extract<T><<<grid_for(ctx, (long long)nv, 256), 256, 0, st>>>(
+                xptrs.as<T *>(), ctl.as<Ctl>(), p.constraintSupport ? S.as<uint8_t>() : nullptr,
+                p.constraintPositivity, D1, D2, B1, B2, B3, dout);
+            GF_CHECK_LAUNCH();
+            if (!on_device) GF_CUDA(cudaMemcpyAsync(rec, dout, sizeof(T) * nv, cudaMemcpyDeviceToHost, st));
+        }
+        if (errK) {
+            if (on_device) GF_CUDA(cudaMemcpyAsync(errK, hist.p, sizeof(double) * it_done, cudaMemcpyDeviceToDevice, st));
+            else GF_CUDA(cudaMemcpyAsync(errK, hist.p, sizeof(double) * it_done, cudaMemcpyDeviceToHost, st));
+        }
+        GF_CUDA(cudaStreamSynchronize(st));
+        const size_t nm = errR.size(), P = (size_t)p.NumProjs;
+        if (eR && nm) std::memcpy(eR, errR.data(), sizeof(double) * nm);
+        if (RA && nm) std::memcpy(RA, Rarr.data(), sizeof(double) * nm * P);
+        if (RA2 && nm) std::memcpy(RA2, Rarr2.data(), sizeof(double) * nm * P);
+    }
+};
+
+genfire_recon *recon_create(genfire_ctx *ctx, const genfire_params &p, const void *M, const uint8_t *mask,
+                            const uint8_t *support, const void *initial, const double *projs,
+                            const double *angles, bool on_device)
+{
+    check_params(p, p.monitor_R == 1);
+    if (p.numIterations < 0) fail(GENFIRE_ERR_ARG, "numIterations must be non-negative.");
+    if (!M) fail(GENFIRE_ERR_ARG, "measuredK is NULL.");
+    ReconBase *impl;
+    if (p.precision == GENFIRE_PREC_FP64) {
+        auto *r = new ReconT<double>();
+        r->ctx = ctx; r->p = p;
+        try { r->setup(M, mask, support, initial, projs, angles, on_device); } catch (...) { delete r; throw; }
+        impl = r;
+    } else {
+        auto *r = new ReconT<float>();
+        r->ctx = ctx; r->p = p;
+        try { r->setup(M, mask, support, initial, projs, angles, on_device); } catch (...) { delete r; throw; }
+        impl = r;
+    }
+    return new genfire_recon{ctx, impl};
+}
+
+void recon_iterate(genfire_recon *r, int count) { r->impl->iterate(count); }
+void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device)
+{
+    r->impl->result(rec, errK, errR, Rarr, Rarr2, on_device);
+}
+void recon_destroy(genfire_recon *r)
+{
+    delete r->impl;
+    delete r;
+}
+
+}  // namespace gf

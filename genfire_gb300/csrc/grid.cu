@@ -1,0 +1,691 @@
+// grid.cu -- DFT gridding (fillInFourierGrid_DFT) and the index/symmetry kernels.
+//
+// Pipeline for P projections (all on the context stream):
+//   1. k_sel_count   every grid point x every projection, FP32 plane test;
+//                    one count per 4096-point chunk
+//   2. k_sel_scan    per-projection exclusive scan of the chunk counts
+//   3. k_sel_write   ordered compaction: (index, D, u, v) in ascending index
+//                    order within each projection, i.e. the order of find()
+//   4. k_dft         F_j = sum_b E_v(j,b) sum_a E_u(j,a) P(a,b) per point
+//   5. k_accum       one launch per projection, in projection order: weighted
+//                    sums in FP64 and the exact-hit overwrite, so repeated
+//                    points accumulate in the reference's order and the last
+//                    exact hit wins (fillInFourierGrid_DFT.m:268-291)
+//   6. k_finalize    FS = sum(w F) / sum(w), exact override, CentroSymmetricity
+//                    mirror, cast to the output precision
+#include "fft.cuh"
+#include "internal.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace gf {
+
+// ===========================================================================
+// host geometry
+// ===========================================================================
+int oversampled(int dim, double ratio) { return (int)mround((double)dim * ratio); }
+
+// MatrixQuaternionRot (fillInFourierGrid_DFT.m:353-363, src/MatrixQuaternionRot.m:1-12)
+void quat_rot(const double v[3], double theta_deg, double R[9])
+{
+    const double pi = 3.14159265358979323846;
+    double th = theta_deg * pi / 180.0;
+    double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    double a = v[0] / nv, b = v[1] / nv, c = v[2] / nv;
+    double w = std::cos(th / 2), s = -std::sin(th / 2);
+    double x = s * a, y = s * b, z = s * c;
+    R[0] = 1 - 2 * y * y - 2 * z * z; R[3] = 2 * x * y + 2 * w * z;     R[6] = 2 * x * z - 2 * w * y;
+    R[1] = 2 * x * y - 2 * w * z;     R[4] = 1 - 2 * x * x - 2 * z * z; R[7] = 2 * y * z + 2 * w * x;
+    R[2] = 2 * x * z + 2 * w * y;     R[5] = 2 * y * z - 2 * w * x;     R[8] = 1 - 2 * x * x - 2 * y * y;
+}
+
+static void mat3(const double A[9], const double B[9], double C[9])
+{
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i)
+            C[i + 3 * j] = A[i] * B[3 * j] + A[i + 3] * B[3 * j + 1] + A[i + 6] * B[3 * j + 2];
+}
+
+void euler_rot(const double v1[3], const double v2[3], const double v3[3], double phi, double theta,
+               double psi, double R[9])
+{
+    double A[9], B[9], Cm[9], T[9];
+    quat_rot(v1, phi, A);
+    quat_rot(v2, theta, B);
+    quat_rot(v3, psi, Cm);
+    mat3(A, B, T);
+    mat3(T, Cm, R);
+}
+
+// sind / cosd with exact reduction in degrees
+static void sincosd(double x, double *s, double *c)
+{
+    const double pi = 3.14159265358979323846;
+    double r = std::remainder(x, 360.0);
+    double q = std::nearbyint(r / 90.0);
+    double t = (r - 90.0 * q) * (pi / 180.0);
+    double st = std::sin(t), ct = std::cos(t);
+    int qi = (((int)q) % 4 + 4) % 4;
+    switch (qi) {
+    case 0: *s = st; *c = ct; break;
+    case 1: *s = ct; *c = -st; break;
+    case 2: *s = -st; *c = -ct; break;
+    default: *s = -ct; *c = st; break;
+    }
+}
+
+// closed-form ZYZ matrix (src/calculate3Dprojection_RealSpaceinterp.m:13-15)
+void rot_zyz(double phi, double theta, double psi, double R[9])
+{
+    double sf, cf, st, ct, sp, cp;
+    sincosd(phi, &sf, &cf);
+    sincosd(theta, &st, &ct);
+    sincosd(psi, &sp, &cp);
+    R[0] = cp * ct * cf - sp * sf;  R[3] = -sp * ct * cf - cp * sf; R[6] = st * cf;
+    R[1] = cp * ct * sf + sp * cf;  R[4] = -sp * ct * sf + cp * cf; R[7] = st * sf;
+    R[2] = -cp * st;                R[5] = sp * st;                 R[8] = ct;
+}
+
+void proj_geometry(const genfire_params &p, double phi, double theta, double psi, ProjGeom &g)
+{
+    double R[9];
+    euler_rot(p.vector1, p.vector2, p.vector3, phi, theta, psi, R);
+    for (int i = 0; i < 9; ++i) g.R[i] = (float)R[i];
+    g.nrm[0] = g.R[6]; g.nrm[1] = g.R[7]; g.nrm[2] = g.R[8];
+    float nn = std::sqrt(g.nrm[0] * g.nrm[0] + g.nrm[1] * g.nrm[1] + g.nrm[2] * g.nrm[2]);
+    g.h[0] = g.nrm[0] / nn; g.h[1] = g.nrm[1] / nn; g.h[2] = g.nrm[2] / nn;
+    g.nsq = g.nrm[0] * g.nrm[0] + g.nrm[1] * g.nrm[1] + g.nrm[2] * g.nrm[2];
+    // LU with partial pivoting (first largest pivot), reciprocal column scaling
+    float *A = g.lu;
+    std::memcpy(A, g.R, sizeof(float) * 9);
+    for (int k = 0; k < 3; ++k) {
+        int pv = k;
+        float best = std::fabs(A[k + 3 * k]);
+        for (int i = k + 1; i < 3; ++i)
+            if (std::fabs(A[i + 3 * k]) > best) { best = std::fabs(A[i + 3 * k]); pv = i; }
+        g.piv[k] = pv;
+        if (pv != k)
+            for (int j = 0; j < 3; ++j) std::swap(A[k + 3 * j], A[pv + 3 * j]);
+        if (A[k + 3 * k] != 0.0f && k < 2) {
+            float r = 1.0f / A[k + 3 * k];
+            for (int i = k + 1; i < 3; ++i) A[i + 3 * k] = A[i + 3 * k] * r;
+        }
+        for (int j = k + 1; j < 3; ++j)
+            for (int i = k + 1; i < 3; ++i) A[i + 3 * j] = A[i + 3 * j] - A[i + 3 * k] * A[k + 3 * j];
+    }
+}
+
+GridSpec make_grid(int n1, int n2, int centro)
+{
+    GridSpec g;
+    if (centro) {
+        g.lo1 = -(n1 / 2); g.l1 = n1 / 2 + 1;
+        g.lo2 = -(n2 / 2); g.l2 = 2 * (n2 / 2) + 1;
+        g.lo3 = -(n1 / 2); g.l3 = 2 * (n1 / 2) + 1;
+    } else {
+        g.lo1 = -(n1 / 2); g.l1 = n1;
+        g.lo2 = -(n2 / 2); g.l2 = n2;
+        g.lo3 = -(n1 / 2); g.l3 = n1;
+    }
+    g.total = (long long)g.l1 * g.l2 * g.l3;
+    return g;
+}
+
+void check_params(const genfire_params &p, bool need_projs)
+{
+    if (p.Dim1 < 2 || p.Dim2 < 2) fail(GENFIRE_ERR_ARG, "Dim1 and Dim2 must be at least 2.");
+    if (need_projs && p.NumProjs < 1) fail(GENFIRE_ERR_ARG, "NumProjs must be positive.");
+    if (!(p.oversamplingRatio >= 1.0) || p.oversamplingRatio > 64.0)
+        fail(GENFIRE_ERR_ARG, "oversamplingRatio must be in [1, 64].");
+    if (!(p.interpolationCutoffDistance > 0.0)) fail(GENFIRE_ERR_ARG, "interpolationCutoffDistance must be positive.");
+    if (p.precision != GENFIRE_PREC_FP64 && p.precision != GENFIRE_PREC_MIXED)
+        fail(GENFIRE_ERR_ARG, "precision must be GENFIRE_PREC_FP64 or GENFIRE_PREC_MIXED.");
+    for (const double *v : {p.vector1, p.vector2, p.vector3})
+        if (v[0] == 0 && v[1] == 0 && v[2] == 0) fail(GENFIRE_ERR_ARG, "rotation axis vectors must be non-zero.");
+    int n1 = oversampled(p.Dim1, p.oversamplingRatio), n2 = oversampled(p.Dim2, p.oversamplingRatio);
+    GridSpec g = make_grid(n1, n2, p.DFT_CentroSymmetricity);
+    if ((long long)n1 * n2 * n1 >= (1LL << 31) || g.total >= (1LL << 31) - 8192)
+        fail(GENFIRE_ERR_ARG, "oversampled grid too large (n1*n2*n1 must stay below 2^31).");
+    if (n1 > 65535 || n2 > 65535) fail(GENFIRE_ERR_ARG, "oversampled size too large.");
+}
+
+// ===========================================================================
+// selection kernels
+// ===========================================================================
+struct SelParams {
+    int lo1, lo2, lo3, l1, l2;
+    int total;
+    int nchunks;
+    double cutoff, half1, half2;
+};
+
+constexpr int kSelThreads = 256;
+constexpr int kSelItems = 16;
+constexpr int kSelChunk = kSelThreads * kSelItems;
+
+// FP32 plane test of grid point li (distancePointsPlane_YY, closestpoint,
+// R \ CP, box filter), with every rounding step explicit.
+__device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp, int li, float &D, float &u,
+                                         float &v)
+{
+    const int i1 = li % sp.l1;
+    const int r = li / sp.l1;
+    const int i2 = r % sp.l2;
+    const int i3 = r / sp.l2;
+    const float K1 = (float)(sp.lo1 + i1), K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
+    D = fabsf(__fadd_rn(__fadd_rn(__fmul_rn(K1, g.h[0]), __fmul_rn(K2, g.h[1])), __fmul_rn(K3, g.h[2])));
+    if (!((double)D < sp.cutoff)) return false;
+    const float s = __fadd_rn(__fadd_rn(__fmul_rn(K1, g.nrm[0]), __fmul_rn(K2, g.nrm[1])), __fmul_rn(K3, g.nrm[2]));
+    const float t = __fdiv_rn(__fsub_rn(0.0f, s), g.nsq);
+    float b[3] = {__fadd_rn(K1, __fmul_rn(t, g.nrm[0])), __fadd_rn(K2, __fmul_rn(t, g.nrm[1])),
+                  __fadd_rn(K3, __fmul_rn(t, g.nrm[2]))};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int pv = g.piv[k];
+        if (pv != k) { float tmp = b[k]; b[k] = b[pv]; b[pv] = tmp; }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int i = k + 1; i < 3; ++i) b[i] = __fsub_rn(b[i], __fmul_rn(b[k], g.lu[i + 3 * k]));
+#pragma unroll
+    for (int k = 2; k >= 0; --k) {
+        b[k] = __fdiv_rn(b[k], g.lu[k + 3 * k]);
+#pragma unroll
+        for (int i = 0; i < k; ++i) b[i] = __fsub_rn(b[i], __fmul_rn(b[k], g.lu[i + 3 * k]));
+    }
+    u = b[0];
+    v = b[1];
+    return fabs((double)b[0]) <= sp.half1 && fabs((double)b[1]) <= sp.half2;
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__restrict__ geo, SelParams sp,
+                                                          int *__restrict__ counts)
+{
+    const int p = blockIdx.y, chunk = blockIdx.x;
+    const ProjGeom g = geo[p];
+    int total = 0;
+    for (int it = 0; it < kSelItems; ++it) {
+        const int li = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
+        float D, u, v;
+        const bool pred = li < sp.total && sel_test(g, sp, li, D, u, v);
+        total += __syncthreads_count(pred);
+    }
+    if (threadIdx.x == 0) counts[(long long)p * sp.nchunks + chunk] = total;
+}
+
+// In-place exclusive scan of each projection's chunk counts; totals[p] = sum.
+__global__ void __launch_bounds__(1024) k_sel_scan(int *counts, int nchunks, long long *totals)
+{
+    __shared__ long long part[1024];
+    int *c = counts + (long long)blockIdx.x * nchunks;
+    const int per = (nchunks + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(b + per, nchunks);
+    long long s = 0;
+    for (int i = b; i < e; ++i) s += c[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long run = 0;
+        for (int i = 0; i < (int)blockDim.x; ++i) { long long t = part[i]; part[i] = run; run += t; }
+        totals[blockIdx.x] = run;
+    }
+    __syncthreads();
+    long long run = part[threadIdx.x];
+    for (int i = b; i < e; ++i) { int t = c[i]; c[i] = (int)run; run += t; }
+}
+
+__global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__restrict__ geo, SelParams sp,
+                                                          const int *__restrict__ chunk_off,
+                                                          const long long *__restrict__ proj_off,
+                                                          uint32_t *__restrict__ ind, float *__restrict__ dist,
+                                                          float *__restrict__ uu, float *__restrict__ vv)
+{
+    __shared__ int wsum[kSelThreads / 32];
+    const int p = blockIdx.y, chunk = blockIdx.x;
+    const ProjGeom g = geo[p];
+    long long base = proj_off[p] + chunk_off[(long long)p * sp.nchunks + chunk];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int it = 0; it < kSelItems; ++it) {
+        const int li = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
+        float D = 0, u = 0, v = 0;
+        const bool pred = li < sp.total && sel_test(g, sp, li, D, u, v);
+        const unsigned m = __ballot_sync(0xffffffffu, pred);
+        if (lane == 0) wsum[w] = __popc(m);
+        __syncthreads();
+        int woff = 0, tot = 0;
+#pragma unroll
+        for (int k = 0; k < kSelThreads / 32; ++k) {
+            const int c = wsum[k];
+            woff += (k < w) ? c : 0;
+            tot += c;
+        }
+        if (pred) {
+            const long long o = base + woff + __popc(m & ((1u << lane) - 1u));
+            ind[o] = (uint32_t)li;
+            dist[o] = D;
+            uu[o] = u;
+            vv[o] = v;
+        }
+        base += tot;
+        __syncthreads();
+    }
+}
+
+// ===========================================================================
+// DFT at the selected points
+// ===========================================================================
+// exp(-2 pi i a w / n) with the phase reduced in FP64: a*w is exact (w is
+// FP32, |a| < 2^20), r = frac(a*w/n) in [-1/2, 1/2].
+template <typename T> __device__ __forceinline__ cplx<T> phase(int a, float w, double inv_n);
+template <> __device__ __forceinline__ double2 phase<double>(int a, float w, double inv_n)
+{
+    double t = (double)a * (double)w * inv_n;
+    t -= rint(t);
+    double s, c;
+    sincospi(-2.0 * t, &s, &c);
+    return make_double2(c, s);
+}
+template <> __device__ __forceinline__ float2 phase<float>(int a, float w, double inv_n)
+{
+    double t = (double)a * (double)w * inv_n;
+    t -= rint(t);
+    float s, c;
+    sincospif((float)(-2.0 * t), &s, &c);
+    return make_float2(c, s);
+}
+
+constexpr int kDftJ = 8;      // points per CTA (one warp each)
+constexpr int kDftA = 16;     // projection rows per shared-memory chunk
+constexpr int kDftB = 256;    // projection columns per pass (8 per lane)
+constexpr int kDftPitch = kDftB + 1;
+
+struct DftTile {
+    int proj;
+    int nj;
+    long long j0;
+};
+
+// One CTA: kDftJ points of one projection.  Warp w owns point j0 + w and
+// accumulates Q(b) = sum_a E_u(a) P(a,b) for its lane's 8 columns b, then
+// contracts with E_v(b) and reduces across the warp.
+template <typename T>
+__global__ void __launch_bounds__(256) k_dft(const T *__restrict__ proj, int D1, int D2, int n1, int n2,
+                                            const DftTile *__restrict__ tiles, const float *__restrict__ uu,
+                                            const float *__restrict__ vv, cplx<T> *__restrict__ F)
+{
+    __shared__ T Ps[kDftA * kDftPitch];
+    __shared__ cplx<T> Eu[kDftJ * kDftA];
+    const DftTile tl = tiles[blockIdx.x];
+    const T *P = proj + (long long)tl.proj * D1 * D2;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int amin = -(D1 / 2), bmin = -(D2 / 2);
+    const double inv1 = 1.0 / (double)n1, inv2 = 1.0 / (double)n2;
+    const bool active = w < tl.nj;
+    const float my_v = active ? vv[tl.j0 + w] : 0.f;
+    cplx<T> acc = mk((T)0, (T)0);
+    for (int b0 = 0; b0 < D2; b0 += kDftB) {
+        const int nb = min(kDftB, D2 - b0);
+        cplx<T> q[kDftB / 32];
+#pragma unroll
+        for (int m = 0; m < kDftB / 32; ++m) q[m] = mk((T)0, (T)0);
+        for (int a0 = 0; a0 < D1; a0 += kDftA) {
+            const int na = min(kDftA, D1 - a0);
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < kDftA * kDftB; idx += blockDim.x) {
+                const int a = idx % kDftA, b = idx / kDftA;
+                Ps[a * kDftPitch + b] = (a < na && b < nb) ? P[(a0 + a) + (long long)D1 * (b0 + b)] : (T)0;
+            }
+            if (threadIdx.x < kDftJ * kDftA) {
+                const int j = threadIdx.x / kDftA, a = threadIdx.x % kDftA;
+                Eu[threadIdx.x] = (j < tl.nj && a < na) ? phase<T>(amin + a0 + a, uu[tl.j0 + j], inv1)
+                                                        : mk((T)0, (T)0);
+            }
+            __syncthreads();
+            for (int a = 0; a < na; ++a) {
+                const cplx<T> e = Eu[w * kDftA + a];
+#pragma unroll
+                for (int m = 0; m < kDftB / 32; ++m) {
+                    const T pv = Ps[a * kDftPitch + lane + 32 * m];
+                    q[m].x += e.x * pv;
+                    q[m].y += e.y * pv;
+                }
+            }
+        }
+        if (active) {
+#pragma unroll
+            for (int m = 0; m < kDftB / 32; ++m) {
+                const int b = lane + 32 * m;
+                if (b < nb) acc = cadd(acc, cmul(q[m], phase<T>(bmin + b0 + b, my_v, inv2)));
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if (active && lane == 0) F[tl.j0 + w] = acc;
+}
+
+// ===========================================================================
+// accumulation, average, mirror
+// ===========================================================================
+template <typename T>
+__global__ void k_accum(const uint32_t *__restrict__ ind, const float *__restrict__ dist,
+                        const cplx<T> *__restrict__ F, long long j0, long long nj, double2 *__restrict__ num,
+                        double *__restrict__ wsum, double2 *__restrict__ ex, uint8_t *__restrict__ hx)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nj; j += (long long)gridDim.x * blockDim.x) {
+        const long long o = j0 + j;
+        const uint32_t li = ind[o];
+        const double d = (double)dist[o];
+        const cplx<T> f = F[o];
+        if (d < 1e-7) {
+            ex[li] = make_double2((double)f.x, (double)f.y);
+            hx[li] = 1;
+        } else {
+            const double wgt = 1.0 / d;
+            double2 a = num[li];
+            a.x += (double)f.x * wgt;
+            a.y += (double)f.y * wgt;
+            num[li] = a;
+            wsum[li] += wgt;
+        }
+    }
+}
+
+// Linear index into the gridded space of the centred full-grid position
+// (c1, c2, c3); conj is set when CentroSymmetricity mirrors k1 > 0 onto -k
+// (CentroSymmetricity.m:2-72 reduces to M(k) = conj(FS(-k)) for k1 > 0).
+__device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2, int centro, int c1, int c2,
+                                               int c3, bool &conj)
+{
+    int k1 = c1 - n1 / 2, k2 = c2 - n2 / 2, k3 = c3 - n1 / 2;
+    conj = false;
+    if (centro && k1 > 0) { k1 = -k1; k2 = -k2; k3 = -k3; conj = true; }
+    return (long long)(k1 - g.lo1) + (long long)g.l1 * ((k2 - g.lo2) + (long long)g.l2 * (k3 - g.lo3));
+}
+
+template <typename TO>
+__global__ void k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
+                           const double2 *__restrict__ ex, const uint8_t *__restrict__ hx, GridSpec g, int n1,
+                           int n2, int centro, cplx<TO> *__restrict__ M)
+{
+    const long long N = (long long)n1 * n2 * n1;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
+        const int c1 = (int)(o % n1);
+        const long long r = o / n1;
+        const int c2 = (int)(r % n2), c3 = (int)(r / n2);
+        bool cj;
+        const long long li = src_index(g, n1, n2, centro, c1, c2, c3, cj);
+        double2 v;
+        if (hx[li]) v = ex[li];
+        else {
+            v = num[li];
+            const double ws = wsum[li];
+            if (ws > 0) { v.x /= ws; v.y /= ws; }
+        }
+        M[o] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
+    }
+}
+
+__global__ void k_centro(const double2 *__restrict__ FS, GridSpec g, int n1, int n2, double2 *__restrict__ M)
+{
+    const long long N = (long long)n1 * n2 * n1;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
+        const int c1 = (int)(o % n1);
+        const long long r = o / n1;
+        const int c2 = (int)(r % n2), c3 = (int)(r / n2);
+        bool cj;
+        const long long li = src_index(g, n1, n2, 1, c1, c2, c3, cj);
+        const double2 v = FS[li];
+        M[o] = make_double2(v.x, cj ? -v.y : v.y);
+    }
+}
+
+// hermitianSymmetrize (src/hermitianSymmetrize.m:22-65): mate of (i,j,k) is
+// (e1-1-i, e2-1-j, e3-1-k) on the odd-extended grid; values beyond the input
+// are zero.
+__global__ void k_hermitian(const double2 *__restrict__ in, int d1, int d2, int d3, double2 *__restrict__ out)
+{
+    const long long N = (long long)d1 * d2 * d3;
+    const int e1 = d1 + (d1 % 2 == 0), e2 = d2 + (d2 % 2 == 0), e3 = d3 + (d3 % 2 == 0);
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(o % d1);
+        const long long r = o / d1;
+        const int j = (int)(r % d2), k = (int)(r / d2);
+        const int mi = e1 - 1 - i, mj = e2 - 1 - j, mk_ = e3 - 1 - k;
+        const double2 a = in[o];
+        double2 b = make_double2(0.0, 0.0);
+        if (mi < d1 && mj < d2 && mk_ < d3) b = in[mi + (long long)d1 * (mj + (long long)d2 * mk_)];
+        double re = a.x + b.x, im = a.y - b.y;
+        const int cnt = (a.x != 0 || a.y != 0) + (b.x != 0 || b.y != 0);
+        if (cnt) { re /= cnt; im /= cnt; }
+        out[o] = make_double2(re, im);
+    }
+}
+
+// make_Kspace_indices (src/make_Kspace_indices.m:16-62)
+__device__ __forceinline__ double kvec(int n, int i)
+{
+    if (n == 1) return 0.0;
+    const int r = (n % 2 == 0) ? n / 2 : (n - 1) / 2;
+    return (double)(i - r) / (double)r;
+}
+
+__global__ void k_kspace(int d1, int d2, int d3, double *__restrict__ Q)
+{
+    const long long N = (long long)d1 * d2 * d3;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(o % d1);
+        const long long r = o / d1;
+        const int j = (int)(r % d2), k = (int)(r / d2);
+        const double kx = kvec(d2, j), ky = kvec(d1, i), kz = kvec(d3, k);
+        Q[o] = sqrt(kx * kx + ky * ky + kz * kz);
+    }
+}
+
+// My_iffshift3_ind (src/My_iffshift3_ind.m:1-7), 1-based in and out
+__global__ void k_iffshift(int s1, int s2, int s3, long long count, const long long *__restrict__ in,
+                           long long *__restrict__ out)
+{
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count; t += (long long)gridDim.x * blockDim.x) {
+        const long long i = in[t] - 1;
+        long long i1 = i % s1, i2 = (i / s1) % s2, i3 = i / ((long long)s1 * s2);
+        i1 = (i1 + (s1 + 1) / 2) % s1;
+        i2 = (i2 + (s2 + 1) / 2) % s2;
+        i3 = (i3 + (s3 + 1) / 2) % s3;
+        out[t] = i1 + (long long)s1 * (i2 + (long long)s2 * i3) + 1;
+    }
+}
+
+__global__ void k_d2f(const double *__restrict__ in, float *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+static unsigned grid_for(genfire_ctx *ctx, long long n, int threads)
+{
+    long long b = (n + threads - 1) / threads;
+    long long cap = (long long)ctx->sm_count * 8;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+// ===========================================================================
+// host orchestration
+// ===========================================================================
+struct Selection {
+    DevBuf ind, dist, u, v;
+    std::vector<long long> nk, off;
+    long long total = 0;
+};
+
+static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, int n1, int n2,
+                          const std::vector<ProjGeom> &geo, Selection &sel)
+{
+    cudaStream_t st = ctx->stream;
+    const int P = (int)geo.size();
+    SelParams sp;
+    sp.lo1 = g.lo1; sp.lo2 = g.lo2; sp.lo3 = g.lo3; sp.l1 = g.l1; sp.l2 = g.l2;
+    sp.total = (int)g.total;
+    sp.nchunks = (int)cdiv(g.total, kSelChunk);
+    sp.cutoff = cutoff; sp.half1 = n1 / 2.0; sp.half2 = n2 / 2.0;
+    DevBuf dgeo(sizeof(ProjGeom) * P, st);
+    GF_CUDA(cudaMemcpyAsync(dgeo.p, geo.data(), sizeof(ProjGeom) * P, cudaMemcpyHostToDevice, st));
+    DevBuf counts(sizeof(int) * (size_t)sp.nchunks * P, st), totals(sizeof(long long) * P, st);
+    dim3 grid(sp.nchunks, P);
+    k_sel_count<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>());
+    GF_CHECK_LAUNCH();
+    k_sel_scan<<<P, 1024, 0, st>>>(counts.as<int>(), sp.nchunks, totals.as<long long>());
+    GF_CHECK_LAUNCH();
+    sel.nk.assign(P, 0);
+    GF_CUDA(cudaMemcpyAsync(sel.nk.data(), totals.p, sizeof(long long) * P, cudaMemcpyDeviceToHost, st));
+    GF_CUDA(cudaStreamSynchronize(st));
+    sel.off.assign(P + 1, 0);
+    for (int p = 0; p < P; ++p) sel.off[p + 1] = sel.off[p] + sel.nk[p];
+    sel.total = sel.off[P];
+    const size_t nt = (size_t)std::max<long long>(sel.total, 1);
+    sel.ind.alloc(nt * sizeof(uint32_t), st);
+    sel.dist.alloc(nt * sizeof(float), st);
+    sel.u.alloc(nt * sizeof(float), st);
+    sel.v.alloc(nt * sizeof(float), st);
+    DevBuf doff(sizeof(long long) * P, st);
+    GF_CUDA(cudaMemcpyAsync(doff.p, sel.off.data(), sizeof(long long) * P, cudaMemcpyHostToDevice, st));
+    k_sel_write<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), doff.as<long long>(),
+                                              sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
+                                              sel.v.as<float>());
+    GF_CHECK_LAUNCH();
+    GF_CUDA(cudaStreamSynchronize(st));  // keeps the host-side staging buffers alive until the copies ran
+}
+
+template <typename T>
+static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
+                       void *d_M, void *d_rec, int64_t *nk_out)
+{
+    cudaStream_t st = ctx->stream;
+    const int D1 = p.Dim1, D2 = p.Dim2, P = p.NumProjs;
+    const int n1 = oversampled(D1, p.oversamplingRatio), n2 = oversampled(D2, p.oversamplingRatio);
+    const GridSpec g = make_grid(n1, n2, p.DFT_CentroSymmetricity);
+    std::vector<ProjGeom> geo(P);
+    for (int i = 0; i < P; ++i) proj_geometry(p, angles[i], angles[i + P], angles[i + 2 * P], geo[i]);
+
+    Selection sel;
+    select_points(ctx, g, p.interpolationCutoffDistance, n1, n2, geo, sel);
+    if (nk_out)
+        for (int i = 0; i < P; ++i) nk_out[i] = sel.nk[i];
+
+    // DFT tiles: kDftJ consecutive points of one projection
+    std::vector<DftTile> tiles;
+    tiles.reserve((size_t)(sel.total / kDftJ + P));
+    for (int i = 0; i < P; ++i)
+        for (long long j = 0; j < sel.nk[i]; j += kDftJ)
+            tiles.push_back(DftTile{i, (int)std::min<long long>(kDftJ, sel.nk[i] - j), sel.off[i] + j});
+    DevBuf F(sizeof(cplx<T>) * (size_t)std::max<long long>(sel.total, 1), st);
+    const T *d_projT;
+    DevBuf projF;
+    if (sizeof(T) == sizeof(double)) {
+        d_projT = reinterpret_cast<const T *>(d_proj);
+    } else {
+        const long long np = (long long)D1 * D2 * P;
+        projF.alloc(sizeof(float) * np, st);
+        k_d2f<<<grid_for(ctx, np, 256), 256, 0, st>>>(d_proj, projF.as<float>(), np);
+        GF_CHECK_LAUNCH();
+        d_projT = reinterpret_cast<const T *>(projF.p);
+    }
+    if (!tiles.empty()) {
+        DevBuf dt(sizeof(DftTile) * tiles.size(), st);
+        GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(DftTile) * tiles.size(), cudaMemcpyHostToDevice, st));
+        k_dft<T><<<(unsigned)tiles.size(), 256, 0, st>>>(d_projT, D1, D2, n1, n2, dt.as<DftTile>(),
+                                                         sel.u.as<float>(), sel.v.as<float>(), F.as<cplx<T>>());
+        GF_CHECK_LAUNCH();
+        GF_CUDA(cudaStreamSynchronize(st));
+    }
+
+    // weighted average in FP64, projection by projection
+    const size_t G = (size_t)g.total;
+    DevBuf num(sizeof(double2) * G, st), wsum(sizeof(double) * G, st), ex(sizeof(double2) * G, st), hx(G, st);
+    GF_CUDA(cudaMemsetAsync(num.p, 0, num.bytes, st));
+    GF_CUDA(cudaMemsetAsync(wsum.p, 0, wsum.bytes, st));
+    GF_CUDA(cudaMemsetAsync(hx.p, 0, hx.bytes, st));
+    for (int i = 0; i < P; ++i) {
+        if (sel.nk[i] == 0) continue;
+        k_accum<T><<<grid_for(ctx, sel.nk[i], 256), 256, 0, st>>>(
+            sel.ind.as<uint32_t>(), sel.dist.as<float>(), F.as<cplx<T>>(), sel.off[i], sel.nk[i],
+            num.as<double2>(), wsum.as<double>(), ex.as<double2>(), hx.as<uint8_t>());
+        GF_CHECK_LAUNCH();
+    }
+    const long long N = (long long)n1 * n2 * n1;
+    k_finalize<T><<<grid_for(ctx, N, 256), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(), ex.as<double2>(),
+                                                         hx.as<uint8_t>(), g, n1, n2, p.DFT_CentroSymmetricity,
+                                                         reinterpret_cast<cplx<T> *>(d_M));
+    GF_CHECK_LAUNCH();
+    if (d_rec) rec_ifft(ctx, p.precision, d_M, n1, n2, D1, D2, d_rec);
+    GF_CUDA(cudaStreamSynchronize(st));
+}
+
+void grid_dft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles, void *d_M,
+              void *d_rec, int64_t *nk)
+{
+    if (p.precision == GENFIRE_PREC_FP64) grid_dft_t<double>(ctx, p, d_proj, angles, d_M, d_rec, nk);
+    else grid_dft_t<float>(ctx, p, d_proj, angles, d_M, d_rec, nk);
+}
+
+long long select_one(genfire_ctx *ctx, const genfire_params &p, double phi, double theta, double psi,
+                     long long cap, int64_t *ind, float *dist, float *u, float *v)
+{
+    const int n1 = oversampled(p.Dim1, p.oversamplingRatio), n2 = oversampled(p.Dim2, p.oversamplingRatio);
+    const GridSpec g = make_grid(n1, n2, p.DFT_CentroSymmetricity);
+    std::vector<ProjGeom> geo(1);
+    proj_geometry(p, phi, theta, psi, geo[0]);
+    Selection sel;
+    select_points(ctx, g, p.interpolationCutoffDistance, n1, n2, geo, sel);
+    const long long n = sel.total;
+    if (n > cap) fail(GENFIRE_ERR_ARG, "select: cap smaller than the number of selected points.");
+    std::vector<uint32_t> hi(n);
+    cudaStream_t st = ctx->stream;
+    if (n) {
+        GF_CUDA(cudaMemcpyAsync(hi.data(), sel.ind.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaMemcpyAsync(dist, sel.dist.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaMemcpyAsync(u, sel.u.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaMemcpyAsync(v, sel.v.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    }
+    for (long long i = 0; i < n; ++i) ind[i] = hi[i];
+    return n;
+}
+
+void centro_device(genfire_ctx *ctx, const double2 *d_FS, int n1, int n_k1, int n2, double2 *d_M)
+{
+    (void)n_k1;
+    const GridSpec g = make_grid(n1, n2, 1);
+    const long long N = (long long)n1 * n2 * n1;
+    k_centro<<<grid_for(ctx, N, 256), 256, 0, ctx->stream>>>(d_FS, g, n1, n2, d_M);
+    GF_CHECK_LAUNCH();
+}
+
+void hermitian_device(genfire_ctx *ctx, const double2 *d_in, int d1, int d2, int d3, double2 *d_out)
+{
+    const long long N = (long long)d1 * d2 * d3;
+    k_hermitian<<<grid_for(ctx, N, 256), 256, 0, ctx->stream>>>(d_in, d1, d2, d3, d_out);
+    GF_CHECK_LAUNCH();
+}
+
+void kspace_device(genfire_ctx *ctx, int d1, int d2, int d3, double *d_Q)
+{
+    const long long N = (long long)d1 * d2 * d3;
+    k_kspace<<<grid_for(ctx, N, 256), 256, 0, ctx->stream>>>(d1, d2, d3, d_Q);
+    GF_CHECK_LAUNCH();
+}
+
+void iffshift_device(genfire_ctx *ctx, const int sz[3], long long count, const long long *d_in, long long *d_out)
+{
+    k_iffshift<<<grid_for(ctx, count, 256), 256, 0, ctx->stream>>>(sz[0], sz[1], sz[2], count, d_in, d_out);
+    GF_CHECK_LAUNCH();
+}
+
+}  // namespace gf

@@ -1,0 +1,225 @@
+/*
+ * genfire.h -- C ABI of libgenfire.so, the GB300 (sm_103a) implementation of
+ * the GENFIRE v2 reconstruction hot path.
+ *
+ * Each entry point replaces one method or function of the MATLAB reference
+ * (paths are relative to the GENFIRE source tree).  Arrays use MATLAB's
+ * memory layout: column-major (dimension 1 fastest), complex data
+ * interleaved (re, im), which is what a MEX gateway receives from
+ * mxGetComplexDoubles / mxGetComplexSingles.
+ *
+ * Conventions
+ *   - Every function returns a genfire_status; GENFIRE_OK is 0.  On failure
+ *     genfire_last_error(ctx) holds a message of the form "GENFIRE: ...".
+ *   - Calls are synchronous: outputs are complete when the call returns.
+ *   - A context owns one CUDA stream on one device.  A context is not
+ *     thread-safe; use one context per host thread.
+ *   - Host-pointer entry points copy inputs to the device and results back.
+ *     The *_device variants take device pointers (e.g. from cudaMalloc or a
+ *     torch tensor) and leave results on the device.
+ *   - precision GENFIRE_PREC_FP64 is the drop-in: gridding DFT, averaging,
+ *     FFTs and the iteration in FP64, measuredK complex128.
+ *     GENFIRE_PREC_MIXED computes the gridding DFT in reduced precision with
+ *     FP32 accumulation and FP64 phase reduction and weight sums, keeps
+ *     measuredK as complex64 (as runGridding does, GENFIRE_Reconstructor.m:182)
+ *     and runs the iteration on complex64 with FP64 error accumulation.
+ */
+#ifndef GENFIRE_H
+#define GENFIRE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GENFIRE_ABI_VERSION 1
+
+typedef enum genfire_status {
+    GENFIRE_OK = 0,
+    GENFIRE_ERR_ARG = 1,          /* invalid argument (sizes, NULL, modes) */
+    GENFIRE_ERR_OOM = 2,          /* device memory exhausted */
+    GENFIRE_ERR_CUDA = 3,         /* CUDA runtime error */
+    GENFIRE_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up */
+    GENFIRE_ERR_UNSUPPORTED = 5,  /* e.g. an FFT length with a prime factor > 7 */
+    GENFIRE_ERR_STATE = 6         /* handle used out of order */
+} genfire_status;
+
+typedef enum genfire_precision {
+    GENFIRE_PREC_FP64 = 0,
+    GENFIRE_PREC_MIXED = 1
+} genfire_precision;
+
+/* The GENFIRE_Reconstructor properties read by the hot path
+ * (GENFIRE_Reconstructor.m:30-70; names kept).  Dim1, Dim2 and NumProjs are
+ * what CheckPrepareData derives from the projection stack
+ * (GENFIRE_Reconstructor.m:118-121). */
+typedef struct genfire_params {
+    int32_t Dim1;
+    int32_t Dim2;
+    int32_t NumProjs;
+    int32_t DFT_CentroSymmetricity;       /* 1: grid the k1<=0 half and mirror */
+    double  oversamplingRatio;            /* n = round(Dim * ratio) */
+    double  interpolationCutoffDistance;  /* plane-distance cutoff, grid units */
+    double  vector1[3];                   /* rotation axes for phi, theta, psi */
+    double  vector2[3];
+    double  vector3[3];
+    int32_t numIterations;
+    int32_t constraintEnforcementMode;    /* 1, 2 or 3 */
+    int32_t constraintPositivity;
+    int32_t constraintSupport;
+    int32_t monitor_R;                    /* R-factor every monitorR_loopLength */
+    int32_t monitorR_loopLength;
+    int32_t precision;                    /* genfire_precision */
+    int32_t reserved[9];                  /* zero */
+} genfire_params;
+
+typedef struct genfire_ctx genfire_ctx;
+typedef struct genfire_recon genfire_recon;
+
+/* ---- library ----------------------------------------------------------- */
+
+int32_t genfire_abi_version(void);
+const char *genfire_status_string(genfire_status s);
+
+/* Class defaults (GENFIRE_Reconstructor.m:30-70) with precision = FP64. */
+genfire_status genfire_params_init(genfire_params *p);
+
+/* Oversampled grid size n1 = round(Dim1*ratio), n2 = round(Dim2*ratio)
+ * (CheckPrepareData, GENFIRE_Reconstructor.m:168-169). */
+genfire_status genfire_grid_size(const genfire_params *p, int32_t *n1, int32_t *n2);
+
+/* ---- context ----------------------------------------------------------- */
+
+genfire_status genfire_create(int32_t device, genfire_ctx **out);
+genfire_status genfire_destroy(genfire_ctx *ctx);
+const char *genfire_last_error(const genfire_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work against the *_device entry points. */
+void *genfire_stream(genfire_ctx *ctx);
+
+/* ---- gridding: fillInFourierGrid_DFT ------------------------------------
+ * Replaces obj = fillInFourierGrid_DFT(obj)
+ * (@GENFIRE_Reconstructor/fillInFourierGrid_DFT.m:85-310) as called by
+ * runGridding (GENFIRE_Reconstructor.m:172-186).
+ *   projections  Dim1 x Dim2 x NumProjs, double
+ *   angles       NumProjs x 3 (phi, theta, psi in degrees), double
+ *   measuredK    n1 x n2 x n1 complex, centred (k=0 at floor(n/2)+1):
+ *                complex128 for FP64, complex64 for MIXED
+ *   recIFFT      Dim1 x Dim2 x Dim1 = My_stripzero(real(my_ifft(measuredK)))
+ *                (fillInFourierGrid_DFT.m:304); double for FP64, float for
+ *                MIXED; NULL to skip
+ *   nk           NumProjs counts of gridded K-points per projection; NULL ok
+ * Index sets are bit-exact with the FP32 selection of the reference
+ * (:175-192) evaluated with a fixed operation order. */
+genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p,
+                                const double *projections, const double *angles,
+                                void *measuredK, void *recIFFT, int64_t *nk);
+genfire_status genfire_grid_dft_device(genfire_ctx *ctx, const genfire_params *p,
+                                       const double *d_projections, const double *angles,
+                                       void *d_measuredK, void *d_recIFFT, int64_t *nk);
+
+/* ---- iteration: reconstruct ---------------------------------------------
+ * Replaces obj = reconstruct(obj) (@GENFIRE_Reconstructor/reconstruct.m:28-194).
+ *   measuredK       n1 x n2 x n1 complex, centred (type as for grid_dft)
+ *   measuredK_mask  n1 x n2 x n1 bytes; NULL means measuredK ~= 0 (the value
+ *                   runGridding sets, GENFIRE_Reconstructor.m:183)
+ *   support         Dim1 x Dim2 x Dim1 bytes; NULL means all ones
+ *   initialObject   Dim1 x Dim2 x Dim1 (double for FP64, float for MIXED);
+ *                   NULL means zeros
+ *   projections, angles   needed only when monitor_R == 1
+ *   reconstruction  Dim1 x Dim2 x Dim1 (double for FP64, float for MIXED)
+ *   errK            numIterations doubles
+ *   errR            floor(numIterations/monitorR_loopLength) doubles (or NULL)
+ *   Rarr, Rarr2     NumProjs x that count (or NULL) */
+genfire_status genfire_reconstruct(genfire_ctx *ctx, const genfire_params *p,
+                                   const void *measuredK, const uint8_t *measuredK_mask,
+                                   const uint8_t *support, const void *initialObject,
+                                   const double *projections, const double *angles,
+                                   void *reconstruction, double *errK,
+                                   double *errR, double *Rarr, double *Rarr2);
+
+/* Staged form of genfire_reconstruct for callers that drive the iterations
+ * themselves (timing, checkpoints).  on_device selects whether the array
+ * pointers are device (1) or host (0) pointers.  iterate() continues the
+ * iteration count where the last call stopped; the total may not exceed
+ * numIterations.  The loop body of one iteration is replayed as a CUDA
+ * graph. */
+genfire_status genfire_recon_create(genfire_ctx *ctx, const genfire_params *p,
+                                    const void *measuredK, const uint8_t *measuredK_mask,
+                                    const uint8_t *support, const void *initialObject,
+                                    const double *projections, const double *angles,
+                                    int32_t on_device, genfire_recon **out);
+genfire_status genfire_recon_iterate(genfire_recon *r, int32_t count);
+/* Copies out the best object (after positivity and support, cropped), errK
+ * of the iterations run so far, and the R-factor records. */
+genfire_status genfire_recon_result(genfire_recon *r, void *reconstruction, double *errK,
+                                    double *errR, double *Rarr, double *Rarr2,
+                                    int32_t on_device);
+genfire_status genfire_recon_destroy(genfire_recon *r);
+
+/* ---- projector -----------------------------------------------------------
+ * Replaces Proj = calculate3Dprojection_RealSpaceinterp(Vol,phi,theta,psi)
+ * (src/calculate3Dprojection_RealSpaceinterp.m:1-57; vectors == NULL: the
+ * closed-form ZYZ matrix of :13-15) and
+ * calculate3Dprojection_RealSpaceinterp_general(Vol,phi,theta,psi,v1,v2,v3)
+ * (src/calculate3Dprojection_RealSpaceinterp_general.m:1-49; vectors = the 9
+ * values v1, v2, v3).  Interpolation is trilinear, samples outside the volume
+ * are 0.  Vol is n1 x n2 x n3; each projection is n1 x n2.  NumProj angle
+ * rows (NumProj x 3, column-major like InputAngles).  vol/projs are double
+ * for FP64 and float for MIXED. */
+genfire_status genfire_project(genfire_ctx *ctx, int32_t precision,
+                               const void *vol, int32_t n1, int32_t n2, int32_t n3,
+                               int32_t num_proj, const double *angles, const double *vectors,
+                               void *projs);
+/* R-factors of reconstruct.m:168-185: per projection
+ * Rarr = sum|bp - pj| / sum|pj| and Rarr2 = ||bp - pj||_F / ||pj||_F of the
+ * projection bp of vol against the measured pj; errR = mean(Rarr).
+ * measured is n1 x n2 x num_proj double. */
+genfire_status genfire_rfactor(genfire_ctx *ctx, int32_t precision,
+                               const void *vol, int32_t n1, int32_t n2, int32_t n3,
+                               int32_t num_proj, const double *angles, const double *vectors,
+                               const double *measured, double *Rarr, double *Rarr2,
+                               double *errR);
+
+/* ---- index and symmetry kernels (host pointers, FP64) -------------------- */
+
+/* CentroSymmetricity(obj, FS, n1, n_k1, n2)
+ * (@GENFIRE_Reconstructor/CentroSymmetricity.m:2-72): FS is the
+ * (n_k1+1) x (2*floor(n2/2)+1) x (2*floor(n1/2)+1) half grid (k1 <= 0),
+ * measuredK the n1 x n2 x n1 full grid. */
+genfire_status genfire_centro_symmetricity(genfire_ctx *ctx, const double *FS, int32_t n1,
+                                           int32_t n_k1, int32_t n2, double *measuredK);
+/* hermitianSymmetrize(in) (src/hermitianSymmetrize.m:22-65). */
+genfire_status genfire_hermitian_symmetrize(genfire_ctx *ctx, const double *in, int32_t d1,
+                                            int32_t d2, int32_t d3, double *out);
+/* Q = make_Kspace_indices(obj) for size(obj) = [d1 d2 d3]
+ * (src/make_Kspace_indices.m:16-62). */
+genfire_status genfire_make_kspace_indices(genfire_ctx *ctx, int32_t d1, int32_t d2, int32_t d3,
+                                           double *Q);
+/* My_volumn_index(big_size, ori_size) (src/My_volumn_index.m:3-34): out is
+ * 3 x 2 column-major, 1-based [start end]. */
+genfire_status genfire_volumn_index(const int32_t big[3], const int32_t ori[3], int32_t out[6]);
+/* My_iffshift3_ind(VolSize, Inds) (src/My_iffshift3_ind.m:1-7), 1-based. */
+genfire_status genfire_iffshift3_ind(genfire_ctx *ctx, const int32_t size[3], int64_t count,
+                                     const int64_t *inds, int64_t *out);
+/* K-point selection of one projection (fillInFourierGrid_DFT.m:175-192):
+ * the grid points within interpolationCutoffDistance of the rotated plane
+ * that pass the in-plane box filter, in ascending 0-based linear index of
+ * the half grid (the order of find()).  dist = D, u/v = CP_plane(1:2,:).
+ * *count receives the number found; cap bounds the outputs. */
+genfire_status genfire_select(genfire_ctx *ctx, const genfire_params *p,
+                              double phi, double theta, double psi, int64_t cap,
+                              int64_t *ind, float *dist, float *u, float *v, int64_t *count);
+/* The library's 3-D FFT (fftn / ifftn semantics: unnormalised forward, 1/N
+ * inverse) on an n1 x n2 x n3 complex array, in place; complex128 for FP64,
+ * complex64 for MIXED. */
+genfire_status genfire_fftn(genfire_ctx *ctx, int32_t precision, void *data, int32_t n1,
+                            int32_t n2, int32_t n3, int32_t inverse);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GENFIRE_H */

@@ -1,0 +1,256 @@
+"""Second, independent restatement of the reference in numpy (test infrastructure only).
+
+It follows the MATLAB source statement by statement (flips, permutes,
+meshgrid, find, accumarray) rather than the reduced index formulas of
+genfire_oracle.c, so the two restatements check each other.  It is meant
+for small sizes only.  FP32 steps use numpy float32 arithmetic, which is
+evaluated element-wise without fused multiply-add.
+"""
+import numpy as np
+
+
+def mround(x):
+    """MATLAB round: half away from zero."""
+    x = np.asarray(x, dtype=np.float64)
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def quat_rot(vector, theta):
+    """fillInFourierGrid_DFT.m:353-363."""
+    theta = theta * np.pi / 180
+    v = np.asarray(vector, dtype=np.float64)
+    v = v / np.sqrt(np.dot(v, v))
+    w = np.cos(theta / 2)
+    x, y, z = (-np.sin(theta / 2) * v[0], -np.sin(theta / 2) * v[1], -np.sin(theta / 2) * v[2])
+    return np.array([[1 - 2 * y ** 2 - 2 * z ** 2, 2 * x * y + 2 * w * z, 2 * x * z - 2 * w * y],
+                     [2 * x * y - 2 * w * z, 1 - 2 * x ** 2 - 2 * z ** 2, 2 * y * z + 2 * w * x],
+                     [2 * x * z + 2 * w * y, 2 * y * z - 2 * w * x, 1 - 2 * x ** 2 - 2 * y ** 2]])
+
+
+def rotmat(v1, v2, v3, phi, theta, psi):
+    return quat_rot(v1, phi) @ quat_rot(v2, theta) @ quat_rot(v3, psi)
+
+
+def lu_solve_f32(R, B):
+    """R \\ B in float32 by LU with partial pivoting (getf2 order), vectorised over columns."""
+    A = np.array(R, dtype=np.float32)
+    piv = []
+    for k in range(3):
+        p = k + int(np.argmax(np.abs(A[k:, k])))
+        piv.append(p)
+        if p != k:
+            A[[k, p], :] = A[[p, k], :]
+        if A[k, k] != 0 and k < 2:
+            r = np.float32(1.0) / A[k, k]
+            A[k + 1:, k] = A[k + 1:, k] * r
+        for j in range(k + 1, 3):
+            for i in range(k + 1, 3):
+                A[i, j] = A[i, j] - A[i, k] * A[k, j]
+    b = [np.array(B[i], dtype=np.float32) for i in range(3)]
+    for k in range(3):
+        if piv[k] != k:
+            b[k], b[piv[k]] = b[piv[k]], b[k]
+    for k in range(3):
+        for i in range(k + 1, 3):
+            b[i] = b[i] - b[k] * A[i, k]
+    for k in range(2, -1, -1):
+        b[k] = b[k] / A[k, k]
+        for i in range(k):
+            b[i] = b[i] - b[k] * A[i, k]
+    return np.stack(b)
+
+
+def half_grid(n1, n2, centro):
+    """fillInFourierGrid_DFT.m:122-144: K1, K2, K3 flattened column-major."""
+    if centro:
+        k1 = np.arange(-(n1 // 2), 1, dtype=np.float32)
+        k2 = np.arange(-(n2 // 2), n2 // 2 + 1, dtype=np.float32)
+        k3 = np.arange(-(n1 // 2), n1 // 2 + 1, dtype=np.float32)
+    else:
+        k1 = np.arange(-int(np.ceil((n1 - 1) / 2)), int(np.floor((n1 - 1) / 2)) + 1, dtype=np.float32)
+        k2 = np.arange(-int(np.ceil((n2 - 1) / 2)), int(np.floor((n2 - 1) / 2)) + 1, dtype=np.float32)
+        k3 = k1
+    K1, K2, K3 = np.meshgrid(k1, k2, k3, indexing="ij")
+    return (K1.reshape(-1, order="F"), K2.reshape(-1, order="F"), K3.reshape(-1, order="F"),
+            (k1.size, k2.size, k3.size))
+
+
+def select(n1, n2, centro, cutoff, R32, nrm32):
+    """Per-projection K-point selection (fillInFourierGrid_DFT.m:175-192)."""
+    K1, K2, K3, _ = half_grid(n1, n2, centro)
+    n = np.asarray(nrm32, dtype=np.float32)
+    nn = np.sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2])
+    h = n / nn
+    D = np.abs(K1 * h[0] + K2 * h[1] + K3 * h[2])
+    Dind = np.nonzero(D.astype(np.float64) < cutoff)[0]
+    p1, p2, p3 = K1[Dind], K2[Dind], K3[Dind]
+    s = p1 * n[0] + p2 * n[1] + p3 * n[2]
+    t = (np.float32(0) - s) / (n[0] * n[0] + n[1] * n[1] + n[2] * n[2])
+    CP = np.stack([p1 + t * n[0], p2 + t * n[1], p3 + t * n[2]])
+    X = lu_solve_f32(np.asarray(R32, dtype=np.float32).reshape(3, 3, order="F"), CP)
+    good = (np.abs(X[0].astype(np.float64)) <= n1 / 2) & (np.abs(X[1].astype(np.float64)) <= n2 / 2)
+    G = Dind[good]
+    return G, D[G], X[0, good], X[1, good]
+
+
+def centro(FS, n1, n_k1, n2):
+    """CentroSymmetricity.m:2-72, literally (flips and permutes)."""
+    FS = np.asarray(FS).reshape(-1, order="F")
+    M = np.zeros((n1, n2, n1), dtype=np.complex128)
+
+    def flips(a):
+        a = a[:, ::-1, :]          # fliplr
+        a = a[:, :, ::-1]          # permute(flipud(permute(a,[3 1 2])),[2 3 1])
+        return a[::-1, :, :]       # flipud
+    if n2 % 2 == 1:
+        if n1 % 2 == 1:
+            half = FS.reshape(n_k1 + 1, n2, n1, order="F")
+            M[:n_k1 + 1] = half
+            M[n_k1 + 1:] = np.conj(flips(half[:-1]))
+        else:
+            ext = FS.reshape(n_k1 + 1, n2, n1 + 1, order="F")
+            M[:n_k1 + 1] = ext[:, :, :-1]
+            M[n_k1 + 1:] = np.conj(flips(ext[1:-1])[:, :, :-1])
+    else:
+        if n1 % 2 == 1:
+            ext = FS.reshape(n_k1 + 1, n2 + 1, n1, order="F")
+            M[:n_k1 + 1] = ext[:, :-1, :]
+            M[n_k1 + 1:] = np.conj(flips(ext[:-1])[:, :-1, :])
+        else:
+            ext = FS.reshape(n_k1 + 1, n2 + 1, n1 + 1, order="F")
+            M[:n_k1 + 1] = ext[:, :-1, :-1]
+            M[n_k1 + 1:] = np.conj(flips(ext[1:-1])[:, :-1, :-1])
+    return M
+
+
+def hermitian_symmetrize(a):
+    """hermitianSymmetrize.m:22-65, literally."""
+    d = a.shape
+    e = tuple(x + (x % 2 == 0) for x in d)
+    inp = np.zeros(e, dtype=np.complex128)
+    inp[:d[0], :d[1], :d[2]] = a
+    out = inp + np.conj(inp[::-1, ::-1, ::-1])
+    nv = (inp != 0).astype(np.float64)
+    nv = nv + nv[::-1, ::-1, ::-1]
+    nz = nv != 0
+    out[nz] = out[nz] / nv[nz]
+    return out[:d[0], :d[1], :d[2]]
+
+
+def make_kspace_indices(shape):
+    """make_Kspace_indices.m:16-62."""
+    vecs = []
+    for n in shape:
+        if n % 2 == 0:
+            r = n // 2
+            vecs.append(np.arange(-r, r) / r)
+        elif n == 1:
+            vecs.append(np.zeros(1))
+        else:
+            r = (n - 1) // 2
+            vecs.append(np.arange(-r, r + 1) / r)
+    Ky, Kx, Kz = np.meshgrid(vecs[0], vecs[1], vecs[2], indexing="ij")
+    return np.sqrt(Kx ** 2 + Ky ** 2 + Kz ** 2)
+
+
+def crop_range(big, ori):
+    """1-based [start, end] (My_volumn_index.m:11-28)."""
+    if big % 2 == 0:
+        s = 1 + (big - ori) // 2 if ori % 2 == 0 else 1 + (big - ori + 1) // 2
+    else:
+        s = 1 + (big - ori - 1) // 2 if ori % 2 == 0 else 1 + (big - ori) // 2
+    return s, s + ori - 1
+
+
+def paddzero(vol, size):
+    out = np.zeros(size, dtype=np.float64)
+    sl = tuple(slice(crop_range(b, o)[0] - 1, crop_range(b, o)[1]) for b, o in zip(size, vol.shape))
+    out[sl] = vol
+    return out
+
+
+def stripzero(pad, size):
+    sl = tuple(slice(crop_range(b, o)[0] - 1, crop_range(b, o)[1]) for b, o in zip(pad.shape, size))
+    return pad[sl].copy()
+
+
+def delay_indicators(mode):
+    if mode == 1:
+        return np.concatenate([0.95 - 0.1 * np.arange(12), [-10, -10, -10], -0.15 + 0.1 * np.arange(12)])
+    if mode == 2:
+        return np.concatenate([0.95 - 0.1 * np.arange(12), [-10, -10]])
+    return np.full(5, -999.0)
+
+
+def reconstruct(M, n_iter, support, mode=3, positivity=True, use_support=True, initial=None, mask=None):
+    """reconstruct.m:28-194 without the R-factor monitor, with numpy FFTs."""
+    n = M.shape
+    D = support.shape
+    S = np.fft.ifftshift(paddzero(support.astype(np.float64), n))
+    x = np.fft.ifftshift(paddzero(initial if initial is not None else np.zeros(D), n))
+    Q = make_kspace_indices(n)
+    if mask is None:
+        mask = M != 0
+    Emask = (M != 0) & mask
+    ci = np.zeros(n)
+    ci[Emask] = 1 - Q[Emask]
+    delay = delay_indicators(mode)
+    m = len(delay)
+    changes = mround(1 + np.arange(m) * (n_iter - 1) / (m - 1)).astype(int) if m > 1 else np.array([n_iter])
+    Ms = np.fft.ifftshift(M)
+    Es = np.fft.ifftshift(Emask)
+    cis = np.fft.ifftshift(ci)
+    denom = np.abs(M[Emask]).sum()
+    best_err = 1e30
+    best = None
+    cur = 0
+    Cs = None
+    errK = np.zeros(n_iter)
+    for it in range(1, n_iter + 1):
+        if cur < m and it == changes[cur]:
+            last = np.nonzero(changes == it)[0][-1]
+            Cs = (cis > delay[last]) & Es
+            cur = last + 1
+            best_err = 1e30
+        if positivity:
+            x[x < 0] = 0
+        if use_support:
+            x = x * S
+        k = np.fft.fftn(x)
+        errK[it - 1] = np.abs(np.abs(k[Es]) - np.abs(Ms[Es])).sum() / denom
+        if errK[it - 1] < best_err:
+            best_err = errK[it - 1]
+            best = x.copy()
+        k[Cs] = Ms[Cs]
+        x = np.real(np.fft.ifftn(k))
+    return stripzero(np.fft.fftshift(best), D), errK
+
+
+def project(vol, R):
+    """Trilinear projector, sum over dim 3 of Vol(R*[X;Y;Z]) with 0 outside."""
+    n1, n2, n3 = vol.shape
+    X, Y, Z = np.meshgrid(np.arange(n1) - n1 // 2, np.arange(n2) - n2 // 2, np.arange(n3) - n3 // 2,
+                          indexing="ij")
+    pos = np.stack([X.ravel(), Y.ravel(), Z.ravel()]).astype(np.float64)
+    r = R @ pos
+    x = r[0] + n1 // 2
+    y = r[1] + n2 // 2
+    z = r[2] + n3 // 2
+    inside = (x >= 0) & (y >= 0) & (z >= 0) & (x <= n1 - 1) & (y <= n2 - 1) & (z <= n3 - 1)
+    i = np.clip(np.floor(x).astype(int), 0, n1 - 2)
+    j = np.clip(np.floor(y).astype(int), 0, n2 - 2)
+    k = np.clip(np.floor(z).astype(int), 0, n3 - 2)
+    fx, fy, fz = x - i, y - j, z - k
+    i, j, k = (np.where(inside, a, 0) for a in (i, j, k))
+    V = vol
+
+    def g(a, b, c):
+        return V[a, b, c]
+    c00 = g(i, j, k) * (1 - fx) + g(i + 1, j, k) * fx
+    c10 = g(i, j + 1, k) * (1 - fx) + g(i + 1, j + 1, k) * fx
+    c01 = g(i, j, k + 1) * (1 - fx) + g(i + 1, j, k + 1) * fx
+    c11 = g(i, j + 1, k + 1) * (1 - fx) + g(i + 1, j + 1, k + 1) * fx
+    c0 = c00 * (1 - fy) + c10 * fy
+    c1 = c01 * (1 - fy) + c11 * fy
+    val = np.where(inside, c0 * (1 - fz) + c1 * fz, 0.0)
+    return val.reshape(n1, n2, n3).sum(axis=2)

@@ -1,0 +1,133 @@
+"""The Fourier-constraint iteration (reconstruct.m) on the GPU, against the
+oracle.  Bar: FP64 reconstruction and errK within relative L2 1e-10; MIXED
+within 1e-4 relative on the volume."""
+import numpy as np
+import pytest
+
+from oracle import np_restate as NR
+from tests.conftest import params, rel
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+
+
+def _measured(seed, D1, D2, os_, keep=0.4, support=None):
+    """A centred grid from a positive object, with most points left unmeasured."""
+    rng = np.random.default_rng(seed)
+    n1, n2 = int(np.floor(D1 * os_ + 0.5)), int(np.floor(D2 * os_ + 0.5))
+    vol = rng.random((D1, D2, D1))
+    if support is not None:
+        vol = vol * support
+    M = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(NR.paddzero(vol, (n1, n2, n1)))))
+    M[rng.random(M.shape) > keep] = 0
+    return np.asfortranarray(M), vol
+
+
+def _support(D1, D2, shrink=1):
+    s = np.zeros((D1, D2, D1), bool)
+    s[shrink:D1 - shrink, shrink:D2 - shrink, shrink:D1 - shrink] = True
+    return s
+
+
+CASES = [
+    # D1, D2, os, mode, positivity, support-on, N
+    (8, 8, 2.0, 3, 1, 1, 12), (8, 8, 2.0, 1, 1, 1, 30), (8, 8, 2.0, 2, 1, 1, 30), (9, 9, 2.0, 3, 1, 1, 10),
+    (8, 10, 2.0, 3, 1, 1, 10), (7, 7, 3.0, 3, 0, 1, 10), (8, 8, 2.0, 3, 1, 0, 8), (10, 8, 2.5, 3, 0, 0, 8),
+    (16, 16, 2.0, 3, 1, 1, 20), (12, 12, 2.0, 1, 1, 1, 27),
+]
+
+
+@pytest.mark.parametrize("D1,D2,os_,mode,pos,sup,N", CASES)
+def test_reconstruct_fp64_parity(lib, ctx, oracle, D1, D2, os_, mode, pos, sup, N):
+    support = _support(D1, D2)
+    M, _ = _measured(D1 * 13 + N, D1, D2, os_, support=support)
+    kw = dict(oversamplingRatio=os_, numIterations=N, constraintEnforcementMode=mode, constraintPositivity=pos,
+              constraintSupport=sup)
+    rec, errK, _, _, _ = ctx.reconstruct(params(lib, D1, D2, 1, **kw), M, support=support)
+    reco, errKo, _, _, _ = oracle.reconstruct(oracle.make_params(D1, D2, 1, **kw), M, support=support)
+    assert rel(rec, reco) < FP64_TOL
+    assert np.abs(errK - errKo).max() < FP64_TOL * max(1.0, np.abs(errKo).max())
+
+
+def test_reconstruct_initial_object_and_mask(lib, ctx, oracle):
+    D, os_ = 8, 2.0
+    support = _support(D, D)
+    M, vol = _measured(3, D, D, os_, support=support)
+    rng = np.random.default_rng(4)
+    mask = (M != 0) & (rng.random(M.shape) < 0.7)
+    init = rng.standard_normal((D, D, D))
+    kw = dict(oversamplingRatio=os_, numIterations=15, constraintEnforcementMode=3)
+    rec, errK, _, _, _ = ctx.reconstruct(params(lib, D, D, 1, **kw), M, support=support, initial=init, mask=mask)
+    reco, errKo, _, _, _ = oracle.reconstruct(oracle.make_params(D, D, 1, **kw), M, support=support, initial=init,
+                                              mask=mask)
+    assert rel(rec, reco) < FP64_TOL
+    assert np.abs(errK - errKo).max() < FP64_TOL
+
+
+def test_reconstruct_staged_equals_one_shot(lib, ctx):
+    D, os_ = 8, 2.0
+    M, _ = _measured(5, D, D, os_)
+    p = params(lib, D, D, 1, oversamplingRatio=os_, numIterations=20, constraintEnforcementMode=1)
+    rec, errK, _, _, _ = ctx.reconstruct(p, M)
+    r = ctx.recon(p, M)
+    for c in (1, 5, 14):
+        r.iterate(c)
+    rec2, errK2, _, _, _ = r.result()
+    r.close()
+    assert np.array_equal(rec, rec2) and np.array_equal(errK, errK2)
+    r = ctx.recon(p, M)
+    with pytest.raises(lib.GenfireError) as e:
+        r.iterate(21)
+    assert e.value.status == 6
+
+
+def test_reconstruct_fixed_point(lib, ctx):
+    """All points measured and consistent: the object is returned unchanged."""
+    rng = np.random.default_rng(6)
+    D, n = 8, 16
+    vol = rng.random((D, D, D))
+    M = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(NR.paddzero(vol, (n, n, n)))))
+    rec, errK, _, _, _ = ctx.reconstruct(params(lib, D, D, 1, oversamplingRatio=2, numIterations=3,
+                                                constraintEnforcementMode=3), M, initial=vol)
+    assert np.abs(rec - vol).max() < 1e-12
+    assert errK[0] < 1e-13
+
+
+@pytest.mark.parametrize("D1,D2,os_,mode", [(16, 16, 2.0, 3), (12, 10, 2.0, 1), (15, 15, 2.0, 3)])
+def test_reconstruct_mixed_tolerance(lib, ctx, oracle, D1, D2, os_, mode):
+    support = _support(D1, D2)
+    M, _ = _measured(D1 + 77, D1, D2, os_, support=support)
+    M = M.astype(np.complex64)
+    kw = dict(oversamplingRatio=os_, numIterations=25, constraintEnforcementMode=mode)
+    rec, errK, _, _, _ = ctx.reconstruct(params(lib, D1, D2, 1, precision="mixed", **kw), M, support=support)
+    reco, errKo, _, _, _ = oracle.reconstruct(oracle.make_params(D1, D2, 1, **kw), M.astype(np.complex128),
+                                              support=support)
+    assert rec.dtype == np.float32
+    assert rel(rec, reco) < 1e-4
+    assert np.abs(errK - errKo).max() < 1e-5
+
+
+def test_monitor_rfactor_matches_oracle(lib, ctx, oracle):
+    rng = np.random.default_rng(8)
+    D, P = 10, 4
+    vol = rng.random((D, D, D))
+    angles = np.asfortranarray(np.stack([rng.uniform(0, 360, P), rng.uniform(-60, 60, P), rng.uniform(0, 360, P)], 1))
+    projs = np.asfortranarray(np.stack([oracle.project(vol, *a) for a in angles], 2))
+    kw = dict(oversamplingRatio=2.0, interpolationCutoffDistance=0.5, numIterations=6, constraintEnforcementMode=3,
+              monitor_R=1, monitorR_loopLength=2, vector3=(0, 0, 1))
+    M, _, _ = ctx.grid_dft(params(lib, D, D, P, **kw), projs, angles)
+    rec, errK, errR, Rarr, Rarr2 = ctx.reconstruct(params(lib, D, D, P, **kw), M, projections=projs, angles=angles)
+    op = oracle.make_params(D, D, P, **kw)
+    Mo, _, _ = oracle.grid_dft(op, projs, angles)
+    reco, errKo, errRo, Rarro, Rarr2o = oracle.reconstruct(op, Mo, projs=projs, angles=angles)
+    assert errR.shape == (3,) and Rarr.shape == (P, 3)
+    assert np.abs(errR - errRo).max() < 1e-9
+    assert np.abs(Rarr - Rarro).max() < 1e-9 and np.abs(Rarr2 - Rarr2o).max() < 1e-9
+
+
+def test_reconstruct_rejects_bad_mode(lib, ctx):
+    M, _ = _measured(1, 8, 8, 2.0)
+    with pytest.raises(lib.GenfireError) as e:
+        ctx.reconstruct(params(lib, 8, 8, 1, oversamplingRatio=2, constraintEnforcementMode=4), M)
+    assert e.value.status == 1 and "not understood" in str(e.value)
