@@ -1,0 +1,409 @@
+#!/usr/bin/env python
+"""Headline benchmark: DR iterations/s and gridding GFLOP/s at a 256^3 object
+(512^3 Fourier grid), mixed precision against the FP64 GPU path.
+
+Workload (seeded synthetic, no dataset): 256^3 volume of 2000 Gaussian atoms
+(sigma 1, amplitudes U[0.3,1]) in a 110/110/80 ellipsoid, 90 projections
+256 x 256 at random Euler angles (theta in [-72, 72]), 0.3 degree angle
+jitter given to the reconstructor, oversampling 2, cutoff 0.125, mode 3,
+positivity and the ellipsoid support on.
+
+A "step" is one iteration of the Fourier-constraint loop (reconstruct.m:117-186)
+on the 512^3 grid.  `value` is mixed-precision iterations/s with inputs
+resident in HBM, timed with CUDA events on the library's stream; `e2e` is the
+same metric through the host-pointer C ABI (genfire_reconstruct), host<->device
+copies included.  `--impl reference` times the CPU restatement of the
+reference (the oracle) on the host cores instead.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "DR iters/s + gridding GFLOP/s at 256³: mixed vs FP64 GPU at equal R-factor"
+WORKLOAD = "euler256"
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fp64-steps", type=int, default=30, help="timed FP64 iterations")
+    ap.add_argument("--rfactor-iters", type=int, default=50, help="iterations for the equal-R-factor comparison")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="small workload (for checking the script)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        pg = dist
+    return ws, rank, local, pg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.th:
+            self.th.join(timeout=2)
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if "Active" in r[5 + i]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(HERE, "profiles", "dr_iteration_euler256_traffic.txt")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch"):
+                return float(line.split("=")[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+def gridding_flops(nk, D1, D2):
+    """Useful DFT flops: sum_p (4 Nk D1 D2 + 8 Nk D2) (E_u P products and the E_v contraction)."""
+    nk = np.asarray(nk, dtype=np.float64)
+    return float((4.0 * nk * D1 * D2 + 8.0 * nk * D2).sum())
+
+
+def make_inputs(G, ctx, quick):
+    from genfire_gb300 import synth
+
+    def proj(vol, angles, vectors):
+        return ctx.project(vol.astype(np.float64), angles, vectors=np.asarray(vectors, float).reshape(-1))
+    if quick:
+        return synth.make_workload(WORKLOAD, proj, D=64, n_proj=30, atoms=120)
+    return synth.make_workload(WORKLOAD, proj)
+
+
+def params_for(G, w, precision, iters):
+    p = G.default_params()
+    D = w["D"]
+    p.Dim1, p.Dim2, p.NumProjs = D, D, w["projections"].shape[2]
+    p.oversamplingRatio = w["os"]
+    p.interpolationCutoffDistance = 0.125
+    for k, v in zip(("vector1", "vector2", "vector3"), w["vectors"]):
+        getattr(p, k)[:] = [float(x) for x in v]
+    p.numIterations = iters
+    p.constraintEnforcementMode = 3
+    p.constraintPositivity = 1
+    p.constraintSupport = 1
+    p.precision = precision
+    return p
+
+
+def run_ours(args, ws, rank, local, pg):
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    import genfire_gb300 as G
+
+    torch.cuda.set_device(local)
+    ctx = G.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    w = make_inputs(G, ctx, args.quick)
+    D = w["D"]
+    P = w["projections"].shape[2]
+    n1, _ = G.grid_size(params_for(G, w, G.PREC_FP64, 1))
+    N3 = n1 ** 3
+    d_proj = torch.from_numpy(np.ascontiguousarray(w["projections"].reshape(-1, order="F"))).cuda()
+    d_sup = torch.from_numpy(np.ascontiguousarray(w["support"].reshape(-1, order="F").astype(np.uint8))).cuda()
+    d_M32 = torch.empty(N3, dtype=torch.complex64, device="cuda")
+    d_M64 = torch.empty(N3, dtype=torch.complex128, device="cuda")
+    angles = w["angles_in"]
+
+    def time_call(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    # ---- gridding (fillInFourierGrid_DFT incl. recIFFT), device-resident projections
+    pm = params_for(G, w, G.PREC_MIXED, 1)
+    pf = params_for(G, w, G.PREC_FP64, 1)
+    ctx.grid_dft_device(pm, d_proj.data_ptr(), angles, d_M32.data_ptr())          # warm-up
+    nk, t_grid_mixed = time_call(lambda: ctx.grid_dft_device(pm, d_proj.data_ptr(), angles, d_M32.data_ptr()))
+    nk64, t_grid_fp64 = time_call(lambda: ctx.grid_dft_device(pf, d_proj.data_ptr(), angles, d_M64.data_ptr()))
+    flops = gridding_flops(nk, D, D)
+    grid_err = float(torch.linalg.vector_norm(d_M32.to(torch.complex128) - d_M64) / torch.linalg.vector_norm(d_M64))
+
+    # ---- DR loop, mixed (value): warm-up, then exactly K timed iterations
+    K, W = args.steps, args.warmup
+    pmr = params_for(G, w, G.PREC_MIXED, W + K + 20)
+    rec = ctx.recon(pmr, d_M32.data_ptr(), support=d_sup.data_ptr(), on_device=True)
+    rec.iterate(W)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    rec.iterate(K)
+    ev1.record(stream)
+    ev1.synchronize()
+    t_dr = ev0.elapsed_time(ev1) / 1e3
+    clk = clocks.stop()
+    if pg:
+        pg.barrier()
+        t = torch.tensor([t_dr], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_dr = float(t.item())
+    names, ms, by = rec.profile(20)
+    rec.close()
+
+    # ---- DR loop, FP64
+    K64 = max(3, min(args.fp64_steps, K))
+    pfr = params_for(G, w, G.PREC_FP64, 3 + K64)
+    rec64 = ctx.recon(pfr, d_M64.data_ptr(), support=d_sup.data_ptr(), on_device=True)
+    rec64.iterate(3)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    rec64.iterate(K64)
+    ev1.record(stream)
+    ev1.synchronize()
+    t_dr64 = ev0.elapsed_time(ev1) / 1e3
+    rec64.close()
+
+    # ---- equal-iteration R-factors (reconstruct.m:176 form, ZYZ projector at the input angles)
+    NR_ = args.rfactor_iters
+    out = {}
+    for prec, dM in ((G.PREC_MIXED, d_M32), (G.PREC_FP64, d_M64)):
+        pr = params_for(G, w, prec, NR_)
+        r = ctx.recon(pr, dM.data_ptr(), support=d_sup.data_ptr(), on_device=True)
+        r.iterate(NR_)
+        vol, errK, _, _, _ = r.result()
+        r.close()
+        errR, _, _ = ctx.rfactor(vol.astype(np.float64), angles, w["projections"], vectors=None)
+        out[prec] = (errR, float(errK[-1]), vol)
+    r_mixed, r_fp64 = out[G.PREC_MIXED][0], out[G.PREC_FP64][0]
+    vol_err = float(np.linalg.norm(out[G.PREC_MIXED][2] - out[G.PREC_FP64][2]) / np.linalg.norm(out[G.PREC_FP64][2]))
+    gt_err = float(np.linalg.norm(out[G.PREC_MIXED][2] - w["vol"]) / np.linalg.norm(w["vol"]))
+
+    # ---- e2e: the host-pointer C ABI (genfire_reconstruct), copies included
+    e2e = None
+    if not args.no_e2e:
+        hM = d_M32.cpu().numpy().reshape((n1, n1, n1), order="F")
+        hM = np.asfortranarray(hM)
+        hS = np.asfortranarray(w["support"].astype(np.uint8))
+        pe = params_for(G, w, G.PREC_MIXED, K)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vol_e, errK_e, _, _, _ = ctx.reconstruct(pe, hM, support=hS)
+        t_e2e = time.perf_counter() - t0
+        h2d = hM.nbytes + hS.nbytes
+        d2h = vol_e.nbytes + errK_e.nbytes
+        e2e = {"value": K / t_e2e, "unit": "iters/s", "h2d_bytes_per_step": h2d / K, "d2h_bytes_per_step": d2h / K,
+               "note": "one genfire_reconstruct call of %d iterations from host buffers: measuredK and support "
+                       "copied in, reconstruction and errK copied out, setup included" % K}
+
+    # ---- roofline of the dominant kernel (live CUDA events per kernel)
+    peak, peak_kind = measured_peaks()
+    k = int(np.argmax(ms))
+    achieved = by[k] / (ms[k] * 1e-3) / 1e9
+    roof = {"kernel": names[k], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": "of " + peak_kind, "traffic": committed_traffic(),
+            "algorithmic_bytes_per_launch": by[k], "ms_per_launch": ms[k],
+            "per_kernel": [{"kernel": names[i], "ms": ms[i], "bytes": by[i],
+                            "GB/s": (by[i] / (ms[i] * 1e-3) / 1e9) if ms[i] > 0 else None} for i in range(7)]}
+
+    # ---- CPU baseline (oracle, bounded sample), rank 0 at N=1 only
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(w, d_M64)
+        except Exception as e:  # reported, not fatal
+            cpu = {"value": None, "error": str(e)[:200]}
+
+    iters_per_s = K / t_dr * ws
+    res = {
+        "metric": METRIC, "value": iters_per_s, "unit": "iters/s", "n_gpus": ws, "steps": K, "warmup": W,
+        "ms_per_step": t_dr / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%s: %d^3 object, %d^3 Fourier grid, %d projections %dx%d, mixed precision "
+                               "(complex64 FFT passes, FP64 errK/weight/phase sums)" % (WORKLOAD, D, n1, P, D, D),
+                   "oversamplingRatio": w["os"], "interpolationCutoffDistance": 0.125,
+                   "constraintEnforcementMode": 3, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "per-iteration working set (object, half spectra, constraint table) exceeds the 129 MB L2"},
+        "gridding_gflops": flops / t_grid_mixed / 1e9,
+        "gridding_ms": t_grid_mixed * 1e3,
+        "gridding_rel_l2_vs_fp64": grid_err,
+        "fp64": {"dr_iters_per_s": K64 / t_dr64, "gridding_gflops": flops / t_grid_fp64 / 1e9,
+                 "gridding_ms": t_grid_fp64 * 1e3, "timed_iterations": K64},
+        "mixed_over_fp64_dr": (K / t_dr) / (K64 / t_dr64),
+        "rfactor": {"iterations": NR_, "mixed": r_mixed, "fp64": r_fp64, "abs_diff": abs(r_mixed - r_fp64),
+                    "errK_mixed": out[G.PREC_MIXED][1], "errK_fp64": out[G.PREC_FP64][1],
+                    "volume_rel_l2_mixed_vs_fp64": vol_err, "volume_rel_l2_vs_ground_truth": gt_err},
+        "gridded_points": int(np.sum(nk)),
+        "e2e": e2e,
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": 7 * K,
+    }
+    ctx.close()
+    return res
+
+
+def cpu_baseline(w, d_M64):
+    """The oracle (FP64 CPU restatement) on the host cores: one iteration of the
+    full 512^3 loop, and the gridding of 4 of the 90 projections."""
+    from oracle import oracle as O
+    D = w["D"]
+    n1 = O.oversampled(D, w["os"])
+    prm = O.make_params(D, D, 4, oversamplingRatio=w["os"], interpolationCutoffDistance=0.125,
+                        vector1=w["vectors"][0], vector2=w["vectors"][1], vector3=w["vectors"][2],
+                        numIterations=1, constraintEnforcementMode=3)
+    sub = [0, 30, 60, 89] if w["projections"].shape[2] >= 90 else [0, 1, 2, 3]
+    t0 = time.perf_counter()
+    FS, nk = O.grid_fs(prm, w["projections"][:, :, sub], w["angles_in"][sub])
+    t_grid = time.perf_counter() - t0
+    M = d_M64.cpu().numpy().reshape((n1, n1, n1), order="F")
+    O.reconstruct(prm, M, support=w["support"])
+    t_loop = O.last_loop_seconds()
+    return {"value": 1.0 / t_loop, "unit": "iters/s", "cores": O.num_threads(), "kind": "port",
+            "sample": "1 iteration of the %d^3 FP64 loop (full complex FFTs, as reconstruct.m); gridding of "
+                      "projections %s" % (n1, sub),
+            "gridding_gflops": gridding_flops(nk, D, D) / t_grid / 1e9, "cpu": cpu_model()}
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if "Model name" in line:
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
+
+
+def run_reference(args, ws, rank):
+    """The reference's CPU path restated (the oracle), all host threads, on the same workload."""
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    import genfire_gb300.synth as synth
+    # inputs: the same seeded workload, projected by the oracle's own projector
+    from genfire_gb300.synth import WORKLOADS
+    wl = WORKLOADS[WORKLOAD]
+
+    def proj(vol, angles, vectors):
+        v = np.asarray(vectors, float).reshape(-1)
+        return np.stack([O.project(vol.astype(np.float64), *a, vectors=v) for a in angles], axis=2)
+    kw = dict(D=64, n_proj=30, atoms=120) if args.quick else {}
+    w = synth.make_workload(WORKLOAD, proj, **kw)
+    D = w["D"]
+    P = w["projections"].shape[2]
+    steps = max(1, min(args.steps, 2 if not args.quick else 5))
+    prm = O.make_params(D, D, P, oversamplingRatio=wl["os"], interpolationCutoffDistance=0.125,
+                        vector1=w["vectors"][0], vector2=w["vectors"][1], vector3=w["vectors"][2],
+                        numIterations=steps, constraintEnforcementMode=3)
+    t0 = time.perf_counter()
+    M, _, nk = O.grid_dft(prm, w["projections"], w["angles_in"], want_rec=False)
+    t_grid = time.perf_counter() - t0
+    O.reconstruct(prm, M, support=w["support"])
+    t_loop = O.last_loop_seconds()
+    v = steps / t_loop
+    n1 = O.oversampled(D, wl["os"])
+    sample = "%d iterations of the %d^3 FP64 loop; gridding of all %d projections" % (steps, n1, P)
+    return {"metric": METRIC, "value": v, "unit": "iters/s", "n_gpus": ws, "steps": steps, "warmup": 0,
+            "ms_per_step": t_loop / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "%s: %d^3 object, %d^3 Fourier grid, %d projections (CPU restatement of the "
+                                   "reference's host path, FP64)" % (WORKLOAD, D, n1, P)},
+            "gridding_gflops": gridding_flops(nk, D, D) / t_grid / 1e9,
+            "cpu_baseline": {"value": v, "unit": "iters/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": sample, "cpu": cpu_model()},
+            "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    ws, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        res = run_reference(args, ws, rank)
+    else:
+        res = run_ours(args, ws, rank, local, pg)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -30,7 +30,7 @@ EXPORTS = [
     "genfire_create", "genfire_destroy", "genfire_last_error", "genfire_stream",
     "genfire_grid_dft", "genfire_grid_dft_device",
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
-    "genfire_recon_destroy",
+    "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
     "genfire_project", "genfire_rfactor",
     "genfire_centro_symmetricity", "genfire_hermitian_symmetrize", "genfire_make_kspace_indices",
     "genfire_volumn_index", "genfire_iffshift3_ind", "genfire_select", "genfire_fftn",
@@ -89,6 +89,8 @@ def load():
         "genfire_recon_iterate": (C.c_int, [vp, C.c_int32]),
         "genfire_recon_result": (C.c_int, [vp, vp, vp, dp, dp, dp, C.c_int32]),
         "genfire_recon_destroy": (C.c_int, [vp]),
+        "genfire_recon_profile": (C.c_int, [vp, C.c_int32, dp, dp]),
+        "genfire_profile_kernel_name": (C.c_char_p, [C.c_int32]),
         "genfire_project": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp, dp, vp]),
         "genfire_rfactor": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp, dp, dp,
                                       dp, dp, dp]),
@@ -356,6 +358,15 @@ class Recon:
         self.ctx.check(load().genfire_recon_result(self._h, ptr(rec), ptr(errK), ptr(errR, C.c_double),
                                                    ptr(Rarr, C.c_double), ptr(Rarr2, C.c_double), 0))
         return rec, errK[:self.done], errR[:nmon], Rarr[:, :nmon], Rarr2[:, :nmon]
+
+    def profile(self, iterations):
+        """Per-kernel mean ms and algorithmic bytes per launch over `iterations` iterations."""
+        ms = np.zeros(7)
+        by = np.zeros(7)
+        self.ctx.check(load().genfire_recon_profile(self._h, iterations, ptr(ms, C.c_double), ptr(by, C.c_double)))
+        self.done += iterations
+        names = [load().genfire_profile_kernel_name(k).decode() for k in range(7)]
+        return names, ms, by
 
     def result_device(self, d_rec_ptr, d_errK_ptr=None):
         self.ctx.check(load().genfire_recon_result(self._h, C.c_void_p(d_rec_ptr),

@@ -209,6 +209,22 @@ genfire_status genfire_recon_destroy(genfire_recon *r)
     return guarded(ctx, [&] { gf::recon_destroy(r); });
 }
 
+genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes)
+{
+    if (!r) return GENFIRE_ERR_ARG;
+    genfire_ctx *ctx = r->ctx;
+    return guarded(ctx, [&] { gf::recon_profile(r, iterations, ms, bytes); });
+}
+
+const char *genfire_profile_kernel_name(int32_t k)
+{
+    static const char *names[GENFIRE_PROFILE_KERNELS] = {
+        "k_ctl_begin", "k_rows_r2c (F1: dim-1 real->half, positivity, support)",
+        "k_colpass (F2: dim-2 forward)", "k_colpass (F3: dim-3 forward, Fourier constraint, errK, dim-3 inverse)",
+        "k_ctl_mid (errK, best object)", "k_colpass (I2: dim-2 inverse)", "k_rows_c2r (I1: half->real dim-1)"};
+    return (k >= 0 && k < GENFIRE_PROFILE_KERNELS) ? names[k] : "";
+}
+
 genfire_status genfire_reconstruct(genfire_ctx *ctx, const genfire_params *p, const void *measuredK,
                                    const uint8_t *measuredK_mask, const uint8_t *support, const void *initialObject,
                                    const double *projections, const double *angles, void *reconstruction,

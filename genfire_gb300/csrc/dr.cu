@@ -307,6 +307,12 @@ struct TabGeom {
     double delay[32];
 };
 
+// |k| / (n/2) of make_Kspace_indices, rounded step by step as the oracle does
+__device__ __forceinline__ double q_radius(double kx, double ky, double kz)
+{
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz)));
+}
+
 template <typename T>
 __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask,
                                           const TabGeom &g, int q1, int q2, int q3, TabEntry<T> &e, double &absM)
@@ -333,14 +339,12 @@ __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const u
     };
     uint32_t cq = 0, cm = 0;
     if (inEq) {
-        const double kx = kv(n2, c2), ky = kv(n1, c1), kz = kv(n1, c3);
-        const double ci = 1.0 - sqrt(kx * kx + ky * ky + kz * kz);
+        const double ci = 1.0 - q_radius(kv(n2, c2), kv(n1, c1), kv(n1, c3));
         for (int k = 0; k < g.m; ++k) cq |= (ci > g.delay[k]) ? (1u << k) : 0u;
         absM += sqrt((double)Ma.x * Ma.x + (double)Ma.y * Ma.y);
     }
     if (inEm) {
-        const double kx = kv(n2, d2), ky = kv(n1, d1), kz = kv(n1, d3);
-        const double ci = 1.0 - sqrt(kx * kx + ky * ky + kz * kz);
+        const double ci = 1.0 - q_radius(kv(n2, d2), kv(n1, d1), kv(n1, d3));
         for (int k = 0; k < g.m; ++k) cm |= (ci > g.delay[k]) ? (1u << k) : 0u;
         if (!mate_stored) absM += sqrt((double)Mb.x * Mb.x + (double)Mb.y * Mb.y);
     }
@@ -455,6 +459,7 @@ __global__ void k_extract(const T *const *__restrict__ xs, const Ctl *__restrict
 struct ReconBase {
     virtual ~ReconBase() {}
     virtual void iterate(int count) = 0;
+    virtual void profile(int count, double *ms, double *bytes) = 0;
     virtual void result(void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device) = 0;
 };
 
@@ -465,7 +470,7 @@ template <typename T> struct ReconT : ReconBase {
     FftPlan pl1, pl2;
     const cplx<T> *tw1, *tw2;
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
-    int m = 0, nparts = 0, tiles1 = 0;
+    int m = 0, nparts = 0, tiles1 = 0, ntab = 0;
     double denom = 0;
     int it_done = 0;
     cudaGraphExec_t exec = nullptr;
@@ -543,7 +548,7 @@ template <typename T> struct ReconT : ReconBase {
         GF_CHECK_LAUNCH();
         k_scan_cols<<<1, 1024, 0, st>>>(counts.as<int>(), colsum.as<double>(), ncol, taboff.as<int>(), dtot.as<double>());
         GF_CHECK_LAUNCH();
-        int ntab = 0;
+        ntab = 0;
         GF_CUDA(cudaMemcpyAsync(&ntab, taboff.as<int>() + ncol, sizeof(int), cudaMemcpyDeviceToHost, st));
         GF_CUDA(cudaMemcpyAsync(&denom, dtot.p, sizeof(double), cudaMemcpyDeviceToHost, st));
         GF_CUDA(cudaStreamSynchronize(st));
@@ -613,11 +618,16 @@ template <typename T> struct ReconT : ReconBase {
         build_graph();
     }
 
-    void enqueue_iteration(cudaStream_t st)
+    // ev (optional) receives an event before each of the 7 kernels and one after
+    void enqueue_iteration(cudaStream_t st, cudaEvent_t *ev = nullptr)
     {
         Ctl *c = ctl.as<Ctl>();
+        int ek = 0;
+        auto mark = [&]() { if (ev) GF_CUDA(cudaEventRecord(ev[ek++], st)); };
+        mark();
         k_ctl_begin<<<1, 32, 0, st>>>(c, changes.as<int>());
         GF_CHECK_LAUNCH();
+        mark();
         // F1: rows (dim 1) real -> half spectrum, with positivity and support
         RowPassArgs<T> r;
         std::memset(&r, 0, sizeof(r));
@@ -628,12 +638,14 @@ template <typename T> struct ReconT : ReconBase {
         r.Y = Y1.as<cplx<T>>();
         r.scale = (T)1;
         launch_rows<T>(r, true, st);
+        mark();
         // F2: dim 2 forward, box rows in, all n2 frequencies out
         ColPassArgs<T> a = colargs<T>(pl2, tw2, W2, h1);
         a.in = Y1.as<cplx<T>>(); a.in_dim = ld1; a.in_other = (long long)ld1 * B2; a.in_cnt = B2; a.in_c = B2 / 2;
         a.out = Y2.as<cplx<T>>(); a.out_dim = ld1; a.out_other = (long long)ld1 * n2; a.out_cnt = n2; a.out_c = 0;
         a.mode = 1;
         launch_colpass<T>(a, B3, st);
+        mark();
         // F3: dim 3 forward, constraint, dim 3 inverse (in place)
         ColPassArgs<T> b = colargs<T>(pl1, tw1, W3, h1);
         b.in = Y2.as<cplx<T>>(); b.in_dim = (long long)ld1 * n2; b.in_other = ld1; b.in_cnt = B3; b.in_c = B3 / 2;
@@ -642,14 +654,17 @@ template <typename T> struct ReconT : ReconBase {
         b.tab_off = taboff.as<int>(); b.tab = tab.as<TabEntry<T>>(); b.h1 = h1; b.partial = partial.as<double>();
         b.cidx = &c->cidx;
         launch_colpass<T>(b, n2, st);
+        mark();
         k_ctl_mid<<<1, 1024, 0, st>>>(c, partial.as<double>(), nparts, denom, hist.as<double>());
         GF_CHECK_LAUNCH();
+        mark();
         // I2: dim 2 inverse, box rows out
         ColPassArgs<T> d = colargs<T>(pl2, tw2, W2, h1);
         d.in = Y2.as<cplx<T>>(); d.in_dim = ld1; d.in_other = (long long)ld1 * n2; d.in_cnt = n2; d.in_c = 0;
         d.out = Y1.as<cplx<T>>(); d.out_dim = ld1; d.out_other = (long long)ld1 * B2; d.out_cnt = B2; d.out_c = B2 / 2;
         d.mode = 2;
         launch_colpass<T>(d, B3, st);
+        mark();
         // I1: rows half spectrum -> real box, 1/N
         RowPassArgs<T> q = r;
         q.xsel = &c->xnext;
@@ -657,6 +672,52 @@ template <typename T> struct ReconT : ReconBase {
         q.positivity = 0;
         q.scale = (T)(1.0 / ((double)n1 * n2 * n1));
         launch_rows<T>(q, false, st);
+        mark();
+    }
+
+    // Algorithmic HBM bytes per launch of each kernel of the iteration.
+    void kernel_bytes(double *b) const
+    {
+        const double S = sizeof(cplx<T>), Rs = sizeof(T);
+        const double box = (double)B1 * B2 * B3;
+        const double half_box = (double)h1 * B2 * B3, half_mid = (double)h1 * n2 * B3;
+        b[0] = 0;
+        b[1] = box * Rs + (p.constraintSupport ? box : 0.0) + half_box * S;
+        b[2] = half_box * S + half_mid * S;
+        b[3] = 2 * half_mid * S + ntab * (double)sizeof(TabEntry<T>) + (h1 * (double)n2 + 1) * 4 + nparts * 8.0;
+        b[4] = nparts * 8.0;
+        b[5] = half_mid * S + half_box * S;
+        b[6] = half_box * S + box * Rs;
+    }
+
+    void profile(int count, double *ms, double *bytes) override
+    {
+        if (count < 1 || it_done + count > p.numIterations)
+            fail(GENFIRE_ERR_STATE, "profile: iteration count out of range.");
+        cudaStream_t st = ctx->stream;
+        cudaEvent_t ev[8];
+        for (auto &e : ev) GF_CUDA(cudaEventCreate(&e));
+        double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+        try {
+            for (int i = 0; i < count; ++i) {
+                enqueue_iteration(st, ev);
+                GF_CUDA(cudaEventSynchronize(ev[7]));
+                for (int k = 0; k < 7; ++k) {
+                    float t = 0;
+                    GF_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+                    acc[k] += t;
+                }
+                ++it_done;
+                if (p.monitor_R == 1 && it_done % p.monitorR_loopLength == 0) monitor();
+            }
+        } catch (...) {
+            for (auto &e : ev) cudaEventDestroy(e);
+            throw;
+        }
+        for (auto &e : ev) cudaEventDestroy(e);
+        if (ms)
+            for (int k = 0; k < 7; ++k) ms[k] = acc[k] / count;
+        if (bytes) kernel_bytes(bytes);
     }
 
     void build_graph()
@@ -767,6 +828,7 @@ genfire_recon *recon_create(genfire_ctx *ctx, const genfire_params &p, const voi
 }
 
 void recon_iterate(genfire_recon *r, int count) { r->impl->iterate(count); }
+void recon_profile(genfire_recon *r, int count, double *ms, double *bytes) { r->impl->profile(count, ms, bytes); }
 void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device)
 {
     r->impl->result(rec, errK, errR, Rarr, Rarr2, on_device);

@@ -475,6 +475,13 @@ __device__ __forceinline__ double kvec(int n, int i)
     return (double)(i - r) / (double)r;
 }
 
+// sqrt(Kx.^2 + Ky.^2 + Kz.^2) rounded step by step (no contraction), so the
+// constraint thresholds 1 - Q > delay resolve exactly as in the oracle
+__device__ __forceinline__ double q_radius(double kx, double ky, double kz)
+{
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz)));
+}
+
 __global__ void k_kspace(int d1, int d2, int d3, double *__restrict__ Q)
 {
     const long long N = (long long)d1 * d2 * d3;
@@ -482,8 +489,7 @@ __global__ void k_kspace(int d1, int d2, int d3, double *__restrict__ Q)
         const int i = (int)(o % d1);
         const long long r = o / d1;
         const int j = (int)(r % d2), k = (int)(r / d2);
-        const double kx = kvec(d2, j), ky = kvec(d1, i), kz = kvec(d3, k);
-        Q[o] = sqrt(kx * kx + ky * ky + kz * kz);
+        Q[o] = q_radius(kvec(d2, j), kvec(d1, i), kvec(d3, k));
     }
 }
 

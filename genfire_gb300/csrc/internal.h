@@ -82,6 +82,7 @@ void recon_iterate(genfire_recon *r, int count);
 void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, double *Rarr, double *Rarr2,
                   bool on_device);
 void recon_destroy(genfire_recon *r);
+void recon_profile(genfire_recon *r, int iterations, double *ms, double *bytes);
 
 // ---------------------------------------------------------------- projector
 // Trilinear projections of a volume view (base pointer, strides vs1 = stride

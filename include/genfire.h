@@ -159,6 +159,17 @@ genfire_status genfire_recon_result(genfire_recon *r, void *reconstruction, doub
                                     int32_t on_device);
 genfire_status genfire_recon_destroy(genfire_recon *r);
 
+/* Per-kernel timing of the iteration (tracing; the reference only prints
+ * wall times, reconstruct.m:74,188-190).  Runs `iterations` further
+ * iterations (they count toward numIterations) with each kernel of the
+ * iteration launched on its own and bracketed by CUDA events on the context
+ * stream.  For kernel k < GENFIRE_PROFILE_KERNELS, ms[k] receives its mean
+ * duration and bytes[k] its algorithmic HBM traffic per launch (compulsory
+ * reads plus writes); genfire_profile_kernel_name(k) names it. */
+#define GENFIRE_PROFILE_KERNELS 7
+genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes);
+const char *genfire_profile_kernel_name(int32_t k);
+
 /* ---- projector -----------------------------------------------------------
  * Replaces Proj = calculate3Dprojection_RealSpaceinterp(Vol,phi,theta,psi)
  * (src/calculate3Dprojection_RealSpaceinterp.m:1-57; vectors == NULL: the

@@ -308,6 +308,33 @@ void orc_grid_extent(int n1, int n2, int centro, int out[6])
  * linear index into the l1 x l2 x l3 grid; dist is D (FP32); u, v are
  * CP_plane(1,:), CP_plane(2,:).  *offplane counts |CP_plane(3,:)| > 1e-4
  * (the reference prints "something wrong!" when it is non-zero). */
+/* one point of the selection; returns 1 when selected */
+static int select_point(const gridspec *g, int64_t li, float h0, float h1, float h2, const float nrm[3], float nsq,
+                        const lu3f *lu, double cutoff, double half1, double half2,
+                        float *D_, float *u_, float *v_, int *off_)
+{
+    int i1 = (int)(li % g->l1), i2 = (int)((li / g->l1) % g->l2), i3 = (int)(li / ((int64_t)g->l1 * g->l2));
+    float K1 = (float)(g->lo1 + i1), K2 = (float)(g->lo2 + i2), K3 = (float)(g->lo3 + i3);
+    float D = fabsf(K1 * h0 + K2 * h1 + K3 * h2);
+    *off_ = 0;
+    if (!((double)D < cutoff)) return 0;
+    float s = K1 * nrm[0] + K2 * nrm[1] + K3 * nrm[2];
+    float t = (0.0f - s) / nsq;
+    float b[3] = {K1 + t * nrm[0], K2 + t * nrm[1], K3 + t * nrm[2]};
+    lu3f_solve(lu, b);
+    if (fabsf(b[2]) > 0.0001f) *off_ = 1;
+    if (!(fabs((double)b[0]) <= half1 && fabs((double)b[1]) <= half2)) return 0;
+    *D_ = D; *u_ = b[0]; *v_ = b[1];
+    return 1;
+}
+
+/* Returns the number of selected points written (ascending linear index, the
+ * order of MATLAB's find), or -1 when cap is too small.  ind is the 0-based
+ * linear index into the l1 x l2 x l3 grid; dist is D (FP32); u, v are
+ * CP_plane(1,:), CP_plane(2,:).  *offplane counts |CP_plane(3,:)| > 1e-4
+ * (the reference prints "something wrong!" when it is non-zero).  The grid is
+ * scanned in chunks in parallel; the chunk counts are prefix-summed so the
+ * output order is the serial order. */
 int64_t orc_select(int n1, int n2, int centro, double cutoff, const float Rf[9], const float nrm[3],
                    int64_t cap, int64_t *ind, float *dist, float *u, float *v, int64_t *offplane)
 {
@@ -320,25 +347,40 @@ int64_t orc_select(int n1, int n2, int centro, double cutoff, const float Rf[9],
     lu3f lu;
     lu3f_factor(Rf, &lu);
     double half1 = n1 / 2.0, half2 = n2 / 2.0;
-    int64_t cnt = 0, off = 0;
     int64_t total = (int64_t)g.l1 * g.l2 * g.l3;
-    for (int64_t li = 0; li < total; ++li) {
-        int i1 = (int)(li % g.l1), i2 = (int)((li / g.l1) % g.l2), i3 = (int)(li / ((int64_t)g.l1 * g.l2));
-        float K1 = (float)(g.lo1 + i1), K2 = (float)(g.lo2 + i2), K3 = (float)(g.lo3 + i3);
-        float D = fabsf(K1 * h0 + K2 * h1 + K3 * h2);
-        if (!((double)D < cutoff)) continue;
-        float s = K1 * nrm[0] + K2 * nrm[1] + K3 * nrm[2];
-        float t = (0.0f - s) / nsq;
-        float b[3] = {K1 + t * nrm[0], K2 + t * nrm[1], K3 + t * nrm[2]};
-        lu3f_solve(&lu, b);
-        if (fabsf(b[2]) > 0.0001f) ++off;
-        if (!(fabs((double)b[0]) <= half1 && fabs((double)b[1]) <= half2)) continue;
-        if (cnt >= cap) return -1;
-        ind[cnt] = li; dist[cnt] = D; u[cnt] = b[0]; v[cnt] = b[1];
-        ++cnt;
+    const int64_t CH = 1 << 16;
+    int64_t nch = (total + CH - 1) / CH;
+    int64_t *cnt = (int64_t *)calloc((size_t)nch + 1, sizeof(int64_t));
+    int64_t off = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : off)
+    for (int64_t c = 0; c < nch; ++c) {
+        int64_t e = (c + 1) * CH < total ? (c + 1) * CH : total, k = 0;
+        for (int64_t li = c * CH; li < e; ++li) {
+            float D, uu, vv;
+            int o;
+            k += select_point(&g, li, h0, h1, h2, nrm, nsq, &lu, cutoff, half1, half2, &D, &uu, &vv, &o);
+            off += o;
+        }
+        cnt[c + 1] = k;
     }
+    for (int64_t c = 0; c < nch; ++c) cnt[c + 1] += cnt[c];
+    if (cnt[nch] > cap) { free(cnt); return -1; }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t c = 0; c < nch; ++c) {
+        int64_t e = (c + 1) * CH < total ? (c + 1) * CH : total, k = cnt[c];
+        for (int64_t li = c * CH; li < e; ++li) {
+            float D, uu, vv;
+            int o;
+            if (select_point(&g, li, h0, h1, h2, nrm, nsq, &lu, cutoff, half1, half2, &D, &uu, &vv, &o)) {
+                ind[k] = li; dist[k] = D; u[k] = uu; v[k] = vv;
+                ++k;
+            }
+        }
+    }
+    int64_t n = cnt[nch];
+    free(cnt);
     if (offplane) *offplane = off;
-    return cnt;
+    return n;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -730,6 +772,21 @@ void orc_change_points(int N, int m, int *out)
  * (nullable: zeros).  projs/angles are needed only when monitor_R.
  * rec_out: D1 x D2 x D1.  errK: numIterations.  errR/Rarr/Rarr2: per monitor
  * point (floor(N/loopLength), Rarr/Rarr2 NumProjs per point). */
+static double g_loop_seconds = 0.0;
+
+/* Wall time of the iteration loop of the last orc_reconstruct call (the
+ * setup before reconstruct.m:117 excluded). */
+double orc_last_loop_seconds(void) { return g_loop_seconds; }
+
+static double wall(void)
+{
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
 int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsigned char *mask,
                     const unsigned char *support, const double *initial,
                     const double *projs, const double *angles,
@@ -803,6 +860,7 @@ int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsign
     double *model = (double *)malloc(sizeof(double) * NV);
     double *bp = (double *)malloc(sizeof(double) * (size_t)D1 * D2);
 
+    double t_loop = wall();
     for (int it = 1; it <= prm->numIterations; ++it) {
         if (cur < m && it == changes[cur]) {
             int last = cur;
@@ -811,11 +869,16 @@ int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsign
             cur = last + 1;
             bestErr = 1e30;
         }
-        if (prm->constraintPositivity)
-            for (size_t i = 0; i < N; ++i) if (x[i] < 0) x[i] = 0;
-        if (prm->constraintSupport)
-            for (size_t i = 0; i < N; ++i) x[i] *= S[i];
-        for (size_t i = 0; i < N; ++i) { k[2 * i] = x[i]; k[2 * i + 1] = 0; }
+        if (prm->constraintPositivity) {
+#pragma omp parallel for
+            for (int64_t i = 0; i < (int64_t)N; ++i) if (x[i] < 0) x[i] = 0;
+        }
+        if (prm->constraintSupport) {
+#pragma omp parallel for
+            for (int64_t i = 0; i < (int64_t)N; ++i) x[i] *= S[i];
+        }
+#pragma omp parallel for
+        for (int64_t i = 0; i < (int64_t)N; ++i) { k[2 * i] = x[i]; k[2 * i + 1] = 0; }
         orc_fftn(k, n1, n2, n1, 0);
         double num = 0;
         for (int64_t e = 0; e < nE; ++e) {
@@ -831,7 +894,8 @@ int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsign
                 k[2 * a] = measuredK[2 * b]; k[2 * a + 1] = measuredK[2 * b + 1];
             }
         orc_fftn(k, n1, n2, n1, 1);
-        for (size_t i = 0; i < N; ++i) x[i] = k[2 * i];
+#pragma omp parallel for
+        for (int64_t i = 0; i < (int64_t)N; ++i) x[i] = k[2 * i];
 
         if (prm->monitor_R == 1 && prm->monitorR_loopLength > 0 && it % prm->monitorR_loopLength == 0) {
             /* model = fftshift(x)(Vol_ind) (:173-174) */
@@ -855,6 +919,7 @@ int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsign
             ++nmon;
         }
     }
+    g_loop_seconds = wall() - t_loop;
     /* reconstruction = My_stripzero(fftshift(best), [D1 D2 D1]) (:192) */
     for (int i3 = 0; i3 < D1; ++i3)
         for (int i2 = 0; i2 < D2; ++i2)

@@ -73,6 +73,7 @@ def lib():
         L.orc_reconstruct.restype = C.c_int
         L.orc_reconstruct.argtypes = [C.POINTER(OrcParams), dp, up, up, dp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_num_threads.restype = C.c_int
+        L.orc_last_loop_seconds.restype = C.c_double
         _lib = L
     return _lib
 
@@ -321,6 +322,11 @@ def reconstruct(prm, measuredK, support=None, initial=None, mask=None, projs=Non
 
 def num_threads():
     return lib().orc_num_threads()
+
+
+def last_loop_seconds():
+    """Wall time of the iteration loop of the last reconstruct() call."""
+    return lib().orc_last_loop_seconds()
 
 
 __all__ = [n for n in dir() if not n.startswith("_")]

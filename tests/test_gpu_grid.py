@@ -57,7 +57,7 @@ def _random_case(seed, D1, D2, P):
 GRID_CASES = [
     # D1, D2, P, os, cutoff, centro
     (16, 16, 6, 2.0, 0.3, 1), (15, 15, 5, 2.0, 0.5, 1), (16, 16, 4, 3.0, 0.125, 1), (12, 14, 5, 2.0, 0.4, 1),
-    (10, 10, 4, 2.5, 0.7, 1), (11, 11, 3, 2.0, 0.5, 0), (16, 16, 3, 2.0, 0.3, 0), (9, 10, 4, 3.0, 0.6, 1),
+    (10, 10, 4, 2.5, 0.7, 1), (11, 11, 3, 2.5, 0.5, 0), (16, 16, 3, 2.0, 0.3, 0), (9, 10, 4, 3.0, 0.6, 1),
 ]
 
 
