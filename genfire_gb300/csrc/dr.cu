@@ -17,6 +17,7 @@
 // the same centred box), so the forward passes skip the zero rows and the
 // inverse passes only produce the box.
 #include "fft.cuh"
+#include "fft_reg.cuh"
 #include "internal.h"
 
 #include <cstring>
@@ -66,6 +67,53 @@ static FftPlan plan_or_fail(int n)
     return pl;
 }
 
+template <typename T, int N> static void set_reg_attrs()
+{
+    const int sm = (int)reg_smem<T, N>();
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_col_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_row_r2c_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_row_c2r_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+}
+
+// Register-resident passes for power-of-two lengths 64..1024.
+template <typename T, int N> static void col_reg(const ColPassArgs<T> &a, int other, cudaStream_t st)
+{
+    constexpr int W = reg_width<T>(N);
+    if (a.W != W) fail(GENFIRE_ERR_STATE, "internal: column tile width mismatch.");
+    dim3 grid(cdiv(a.ncols, W), other);
+    k_col_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
+}
+template <typename T, int N> static void rows_reg(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
+{
+    constexpr int W = reg_width<T>(N);
+    if (a.W != W) fail(GENFIRE_ERR_STATE, "internal: row tile width mismatch.");
+    dim3 grid(cdiv((a.nrows + 1) / 2, W));
+    if (forward) k_row_r2c_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
+    else k_row_c2r_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
+}
+template <typename T> static bool try_col_reg(const ColPassArgs<T> &a, int other, cudaStream_t st)
+{
+    switch (a.pl.n) {
+    case 64: col_reg<T, 64>(a, other, st); return true;
+    case 128: col_reg<T, 128>(a, other, st); return true;
+    case 256: col_reg<T, 256>(a, other, st); return true;
+    case 512: col_reg<T, 512>(a, other, st); return true;
+    case 1024: col_reg<T, 1024>(a, other, st); return true;
+    default: return false;
+    }
+}
+template <typename T> static bool try_rows_reg(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
+{
+    switch (a.pl.n) {
+    case 64: rows_reg<T, 64>(a, forward, st); return true;
+    case 128: rows_reg<T, 128>(a, forward, st); return true;
+    case 256: rows_reg<T, 256>(a, forward, st); return true;
+    case 512: rows_reg<T, 512>(a, forward, st); return true;
+    case 1024: rows_reg<T, 1024>(a, forward, st); return true;
+    default: return false;
+    }
+}
+
 // Opt every FFT pass kernel into large dynamic shared memory once per device
 // (before any graph capture; the attribute only raises the limit).
 template <typename T> static void ensure_smem_attrs()
@@ -80,6 +128,11 @@ template <typename T> static void ensure_smem_attrs()
     GF_CUDA(cudaFuncSetAttribute((const void *)k_colpass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
     GF_CUDA(cudaFuncSetAttribute((const void *)k_rows_r2c<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
     GF_CUDA(cudaFuncSetAttribute((const void *)k_rows_c2r<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    set_reg_attrs<T, 64>();
+    set_reg_attrs<T, 128>();
+    set_reg_attrs<T, 256>();
+    set_reg_attrs<T, 512>();
+    set_reg_attrs<T, 1024>();
     done.insert(dev);
 }
 
@@ -87,20 +140,24 @@ template <typename T> static void ensure_smem_attrs()
 template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st)
 {
     a.P = a.W + 1;
-    const size_t sm = tile_smem<T>(a.pl.n, a.W);
-    dim3 grid(cdiv(a.ncols, a.W), other);
-    k_colpass<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    if (!try_col_reg<T>(a, other, st)) {
+        const size_t sm = tile_smem<T>(a.pl.n, a.W);
+        dim3 grid(cdiv(a.ncols, a.W), other);
+        k_colpass<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    }
     GF_CHECK_LAUNCH();
 }
 
 template <typename T> static void launch_rows(RowPassArgs<T> a, bool forward, cudaStream_t st)
 {
     a.P = a.W + 1;
-    const size_t sm = tile_smem<T>(a.pl.n, a.W);
-    const int pairs = (a.nrows + 1) / 2;
-    dim3 grid(cdiv(pairs, a.W));
-    if (forward) k_rows_r2c<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
-    else k_rows_c2r<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    if (!try_rows_reg<T>(a, forward, st)) {
+        const size_t sm = tile_smem<T>(a.pl.n, a.W);
+        const int pairs = (a.nrows + 1) / 2;
+        dim3 grid(cdiv(pairs, a.W));
+        if (forward) k_rows_r2c<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+        else k_rows_c2r<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    }
     GF_CHECK_LAUNCH();
 }
 

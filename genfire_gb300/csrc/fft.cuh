@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(kTileMaxThreads<T>) k_rows_r2c(RowPassArgs<T> 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     const int n = a.pl.n, W = a.W, P = a.P, tid = threadIdx.x, nt = blockDim.x;
-    const T *x = a.xsel ? a.xs[*a.xsel] : a.xs[0];
+    const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0base = blockIdx.x * W * 2;
     for (int i = tid; i < n * P; i += nt) s[i] = mk((T)0, (T)0);
     __syncthreads();
@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(kTileMaxThreads<T>) k_rows_c2r(RowPassArgs<T> 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     const int n = a.pl.n, W = a.W, P = a.P, tid = threadIdx.x, nt = blockDim.x;
-    T *x = a.xsel ? a.xs[*a.xsel] : a.xs[0];
+    T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0base = blockIdx.x * W * 2;
     for (int idx = tid; idx < W * a.h1; idx += nt) {
         const int c = idx / a.h1, q = idx - c * a.h1;

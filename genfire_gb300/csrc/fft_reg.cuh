@@ -1,0 +1,295 @@
+// fft_reg.cuh -- register-resident Stockham FFT for power-of-two lengths.
+//
+// Each thread owns 8 elements of one column: before every stage it holds
+// x[j + k*N/8] (k = 0..7) of the stage's input.  A stage of radix R runs 8/R
+// butterflies in registers; between stages the outputs are exchanged through
+// one of two shared-memory buffers (ping-pong, one barrier per exchange).  A
+// 512-point transform is three radix-8 stages and two exchanges; the first
+// stage reads straight from global memory and the last stage's outputs go
+// straight back, so zero-padded inputs and cropped outputs cost nothing.
+// Radix schedule and twiddle strides are compile-time constants.
+#pragma once
+
+#include "fft.cuh"
+
+namespace gf {
+
+constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+template <int N> struct P2Plan {
+    static constexpr int L = ilog2c(N);
+    static constexpr int N8 = L / 3;          // radix-8 stages
+    static constexpr int REM = L % 3;         // then one radix-4 (REM 2) or radix-2 (REM 1) stage
+    static constexpr int NST = N8 + (REM ? 1 : 0);
+    static constexpr int radix(int s) { return s < N8 ? 8 : (REM == 2 ? 4 : 2); }
+    static constexpr int ns(int s) { return s == 0 ? 1 : ns(s - 1) * radix(s - 1); }
+};
+
+// shared-memory layouts with one padding row every 8 rows (bank spreading)
+template <int N, int W> struct ColLayout {   // the W columns interleaved, column fastest
+    static constexpr int SIZE = (N + N / 8) * W;
+    static __device__ __forceinline__ int idx(int i, int c) { return (i + (i >> 3)) * W + c; }
+};
+template <int N, int W> struct RowLayout {   // each column contiguous
+    static constexpr int PC = N + N / 8;
+    static constexpr int SIZE = PC * W;
+    static __device__ __forceinline__ int idx(int i, int c) { return c * PC + i + (i >> 3); }
+};
+
+template <typename T, int N, int S>
+__device__ __forceinline__ void reg_stage(cplx<T> (&v)[8], int j, const cplx<T> *__restrict__ tw, bool inv)
+{
+    constexpr int R = P2Plan<N>::radix(S);
+    constexpr int NS = P2Plan<N>::ns(S);
+    constexpr int NB = 8 / R;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int jp = j + b * (N / 8);
+        cplx<T> u[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) u[r] = v[b + r * NB];
+        if (NS > 1) {
+            const int kk = jp & (NS - 1);
+            constexpr int step = N / (NS * R);
+#pragma unroll
+            for (int r = 1; r < R; ++r) u[r] = ctw(u[r], __ldg(&tw[kk * r * step]), inv);
+        }
+        Dft<R, T>::run(u, inv, tw, N);
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b + r * NB] = u[r];
+    }
+}
+
+// FFT index held by register k after stage S
+template <int N, int S> __device__ __forceinline__ int reg_out_index(int j, int k)
+{
+    constexpr int R = P2Plan<N>::radix(S);
+    constexpr int NS = P2Plan<N>::ns(S);
+    constexpr int NB = 8 / R;
+    const int b = k % NB, r = k / NB;
+    const int jp = j + b * (N / 8);
+    const int kk = jp & (NS - 1);
+    return (jp - kk) * R + kk + r * NS;
+}
+template <int N> __device__ __forceinline__ int reg_final_index(int j, int k)
+{
+    return reg_out_index<N, P2Plan<N>::NST - 1>(j, k);
+}
+
+template <typename T, int N, class Lay, int S = 0>
+__device__ __forceinline__ void reg_fft(cplx<T> (&v)[8], cplx<T> *sA, cplx<T> *sB, int &buf, int j, int c,
+                                        const cplx<T> *__restrict__ tw, bool inv)
+{
+    reg_stage<T, N, S>(v, j, tw, inv);
+    if constexpr (S + 1 < P2Plan<N>::NST) {
+        cplx<T> *s = buf ? sB : sA;
+        buf ^= 1;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) s[Lay::idx(reg_out_index<N, S>(j, k), c)] = v[k];
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = s[Lay::idx(j + k * (N / 8), c)];
+        reg_fft<T, N, Lay, S + 1>(v, sA, sB, buf, j, c, tw, inv);
+    }
+}
+
+// Fourier constraint and errK terms on one shared-memory tile (see k_colpass);
+// returns this thread's errK partial.
+template <typename T, class Lay>
+__device__ __forceinline__ double apply_table(cplx<T> *s, const ColPassArgs<T> &a, int tile, int W, int other)
+{
+    const int cid0 = other * a.h1 + tile * W;
+    const int cid1 = min(cid0 + W, other * a.h1 + a.h1);
+    const int e0 = a.tab_off[cid0], e1 = a.tab_off[cid1];
+    const int ci = *a.cidx;
+    double acc = 0.0;
+    for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const TabEntry<T> t = a.tab[e];
+        const int q3 = t.pos & 0xFFFF, cl = t.pos >> 16;
+        const int si = Lay::idx(q3, cl);
+        const cplx<T> k = s[si];
+        const T mk_ = sqrt(k.x * k.x + k.y * k.y);
+        if (t.eflags & 1u) acc += fabs((double)mk_ - (double)sqrt(t.Mq.x * t.Mq.x + t.Mq.y * t.Mq.y));
+        if (t.eflags & 2u) acc += fabs((double)mk_ - (double)sqrt(t.Mmq.x * t.Mmq.x + t.Mmq.y * t.Mmq.y));
+        const bool eq = (t.cq >> ci) & 1u, emq = (t.cmq >> ci) & 1u;
+        if (eq || emq) {
+            const cplx<T> A = eq ? t.Mq : k;
+            const cplx<T> B = emq ? cconj(t.Mmq) : k;
+            s[si] = mk((T)0.5 * (A.x + B.x), (T)0.5 * (A.y + B.y));
+        }
+    }
+    return acc;
+}
+
+__device__ __forceinline__ void block_partial(double acc, double *out)
+{
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) *out = v;
+    }
+}
+
+template <typename T> constexpr int reg_width(int n)
+{
+    return sizeof(T) == 4 ? (n * 8 > 4096 ? 4096 / n : 8) : (n * 4 > 2048 ? 2048 / n : 4);
+}
+
+// Column pass (same contract as k_colpass) for N a power of two.
+template <typename T, int N>
+__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_col_reg(ColPassArgs<T> a)
+{
+    constexpr int W = reg_width<T>(N);
+    using Lay = ColLayout<N, W>;
+    constexpr int NST = P2Plan<N>::NST;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *sB = sA + Lay::SIZE;
+    const int c = threadIdx.x % W, j = threadIdx.x / W;
+    const int tile = blockIdx.x, other = blockIdx.y;
+    const int col = tile * W + c;
+    const bool valid = col < a.ncols;
+    const cplx<T> zero = mk((T)0, (T)0);
+    cplx<T> v[8];
+    {
+        const cplx<T> *in = a.in + (long long)other * a.in_other + (long long)col * a.col_stride;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            int e = j + k * (N / 8) + a.in_c;
+            if (e >= N) e -= N;
+            v[k] = (valid && e < a.in_cnt) ? in[(long long)e * a.in_dim] : zero;
+        }
+    }
+    int buf = 0;
+    if (a.mode & 1) reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, false);
+    if (a.mode & 2) {
+        if (a.mode & 1) {
+            cplx<T> *s = buf ? sB : sA;
+            buf ^= 1;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) s[Lay::idx(reg_final_index<N>(j, k), c)] = v[k];
+            __syncthreads();
+            if (a.mode & 4) {
+                const double acc = apply_table<T, Lay>(s, a, tile, W, other);
+                block_partial(acc, a.partial + (long long)other * gridDim.x + tile);
+                __syncthreads();
+            }
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = s[Lay::idx(j + k * (N / 8), c)];
+        }
+        reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, true);
+    }
+    (void)NST;
+    cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int e = reg_final_index<N>(j, k) + a.out_c;
+        if (e >= N) e -= N;
+        if (valid && e < a.out_cnt) out[(long long)e * a.out_dim] = mk(v[k].x * a.scale, v[k].y * a.scale);
+    }
+}
+
+// Row passes (same contract as k_rows_r2c / k_rows_c2r) for N a power of two.
+template <typename T, int N>
+__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_row_r2c_reg(RowPassArgs<T> a)
+{
+    constexpr int W = reg_width<T>(N);
+    constexpr int TPC = N / 8;
+    using Lay = RowLayout<N, W>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *sB = sA + Lay::SIZE;
+    const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
+    const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
+    const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
+    cplx<T> v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int e = j + k * TPC + a.c1;
+        if (e >= N) e -= N;
+        T va = 0, vb = 0;
+        if (e < a.B1) {
+            if (r0 < a.nrows) {
+                const long long o = (long long)r0 * a.B1 + e;
+                va = x[o];
+                if (a.positivity && va < (T)0) va = 0;
+                if (a.support) va = va * (T)a.support[o];
+            }
+            if (r1 < a.nrows) {
+                const long long o = (long long)r1 * a.B1 + e;
+                vb = x[o];
+                if (a.positivity && vb < (T)0) vb = 0;
+                if (a.support) vb = vb * (T)a.support[o];
+            }
+        }
+        v[k] = mk(va, vb);
+    }
+    int buf = 0;
+    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, false);
+    cplx<T> *s = buf ? sB : sA;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s[Lay::idx(reg_final_index<N>(j, k), c)] = v[k];
+    __syncthreads();
+    const int rbase = blockIdx.x * W * 2;
+    for (int idx = threadIdx.x; idx < W * a.h1; idx += blockDim.x) {
+        const int cc = idx / a.h1, q = idx - cc * a.h1;
+        const int q0 = rbase + 2 * cc, q1 = q0 + 1;
+        const cplx<T> Z = s[Lay::idx(q, cc)];
+        const cplx<T> Zm = s[Lay::idx(q == 0 ? 0 : N - q, cc)];
+        const cplx<T> Xa = mk((T)0.5 * (Z.x + Zm.x), (T)0.5 * (Z.y - Zm.y));
+        const cplx<T> Xb = mk((T)0.5 * (Z.y + Zm.y), (T)0.5 * (Zm.x - Z.x));
+        if (q0 < a.nrows) a.Y[(long long)q0 * a.ld1 + q] = Xa;
+        if (q1 < a.nrows) a.Y[(long long)q1 * a.ld1 + q] = Xb;
+    }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_row_c2r_reg(RowPassArgs<T> a)
+{
+    constexpr int W = reg_width<T>(N);
+    constexpr int TPC = N / 8;
+    using Lay = RowLayout<N, W>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
+    cplx<T> *sB = sA + Lay::SIZE;
+    const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
+    T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
+    const int rbase = blockIdx.x * W * 2;
+    for (int idx = threadIdx.x; idx < W * a.h1; idx += blockDim.x) {
+        const int cc = idx / a.h1, q = idx - cc * a.h1;
+        const int q0 = rbase + 2 * cc, q1 = q0 + 1;
+        cplx<T> ha = mk((T)0, (T)0), hb = ha;
+        if (q0 < a.nrows) ha = a.Y[(long long)q0 * a.ld1 + q];
+        if (q1 < a.nrows) hb = a.Y[(long long)q1 * a.ld1 + q];
+        if (q == 0 || 2 * q == N) { ha.y = 0; hb.y = 0; }
+        sA[Lay::idx(q, cc)] = mk(ha.x - hb.y, ha.y + hb.x);
+        if (q != 0 && N - q >= a.h1) sA[Lay::idx(N - q, cc)] = mk(ha.x + hb.y, hb.x - ha.y);
+    }
+    __syncthreads();
+    cplx<T> v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = sA[Lay::idx(j + k * TPC, c)];
+    int buf = 1;
+    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, true);
+    const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        int e = reg_final_index<N>(j, k) + a.c1;
+        if (e >= N) e -= N;
+        if (e < a.B1) {
+            if (r0 < a.nrows) x[(long long)r0 * a.B1 + e] = v[k].x * a.scale;
+            if (r1 < a.nrows) x[(long long)r1 * a.B1 + e] = v[k].y * a.scale;
+        }
+    }
+}
+
+template <typename T, int N> constexpr size_t reg_smem()
+{
+    return 2 * (size_t)ColLayout<N, reg_width<T>(N)>::SIZE * sizeof(cplx<T>);
+}
+
+}  // namespace gf
