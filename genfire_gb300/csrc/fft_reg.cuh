@@ -94,23 +94,24 @@ __device__ __forceinline__ void reg_fft(cplx<T> (&v)[8], cplx<T> *sA, cplx<T> *s
 }
 
 // Fourier constraint and errK terms on one shared-memory tile (see k_colpass);
-// returns this thread's errK partial.
+// returns this thread's errK terms (a handful per thread, summed in FP32; the
+// block and grid sums are FP64).
 template <typename T, class Lay>
-__device__ __forceinline__ double apply_table(cplx<T> *s, const ColPassArgs<T> &a, int tile, int W, int other)
+__device__ __forceinline__ float apply_table(cplx<T> *s, const ColPassArgs<T> &a, int tile, int W, int other)
 {
     const int cid0 = other * a.h1 + tile * W;
     const int cid1 = min(cid0 + W, other * a.h1 + a.h1);
     const int e0 = a.tab_off[cid0], e1 = a.tab_off[cid1];
     const int ci = *a.cidx;
-    double acc = 0.0;
+    float acc = 0.f;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const TabEntry<T> t = a.tab[e];
         const int q3 = t.pos & 0xFFFF, cl = t.pos >> 16;
         const int si = Lay::idx(q3, cl);
         const cplx<T> k = s[si];
-        const T mk_ = sqrt(k.x * k.x + k.y * k.y);
-        if (t.eflags & 1u) acc += fabs((double)mk_ - (double)sqrt(t.Mq.x * t.Mq.x + t.Mq.y * t.Mq.y));
-        if (t.eflags & 2u) acc += fabs((double)mk_ - (double)sqrt(t.Mmq.x * t.Mmq.x + t.Mmq.y * t.Mmq.y));
+        const float mk_ = (float)sqrt(k.x * k.x + k.y * k.y);
+        if (t.eflags & 1u) acc += fabsf(mk_ - (float)sqrt(t.Mq.x * t.Mq.x + t.Mq.y * t.Mq.y));
+        if (t.eflags & 2u) acc += fabsf(mk_ - (float)sqrt(t.Mmq.x * t.Mmq.x + t.Mmq.y * t.Mmq.y));
         const bool eq = (t.cq >> ci) & 1u, emq = (t.cmq >> ci) & 1u;
         if (eq || emq) {
             const cplx<T> A = eq ? t.Mq : k;
@@ -134,6 +135,10 @@ __device__ __forceinline__ void block_partial(double acc, double *out)
     }
 }
 
+// CTAs per SM the register-resident kernels are built for (registers per
+// thread <= 65536 / (threads * this)); shared memory (2 x 37 KB) allows 3.
+template <typename T> constexpr int kRegMinBlocks = sizeof(T) == 4 ? 3 : 2;
+
 template <typename T> constexpr int reg_width(int n)
 {
     return sizeof(T) == 4 ? (n * 8 > 4096 ? 4096 / n : 8) : (n * 4 > 2048 ? 2048 / n : 4);
@@ -141,7 +146,7 @@ template <typename T> constexpr int reg_width(int n)
 
 // Column pass (same contract as k_colpass) for N a power of two.
 template <typename T, int N>
-__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_col_reg(ColPassArgs<T> a)
+__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_col_reg(ColPassArgs<T> a)
 {
     constexpr int W = reg_width<T>(N);
     using Lay = ColLayout<N, W>;
@@ -157,14 +162,16 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_col_reg(ColPassA
     cplx<T> v[8];
     {
         const cplx<T> *in = a.in + (long long)other * a.in_other + (long long)col * a.col_stride;
+        const unsigned idim = (unsigned)a.in_dim;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
             int e = j + k * (N / 8) + a.in_c;
             if (e >= N) e -= N;
-            v[k] = (valid && e < a.in_cnt) ? in[(long long)e * a.in_dim] : zero;
+            v[k] = (valid && e < a.in_cnt) ? in[(unsigned)e * idim] : zero;
         }
     }
     int buf = 0;
+    float err = 0.f;
     if (a.mode & 1) reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, false);
     if (a.mode & 2) {
         if (a.mode & 1) {
@@ -174,8 +181,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_col_reg(ColPassA
             for (int k = 0; k < 8; ++k) s[Lay::idx(reg_final_index<N>(j, k), c)] = v[k];
             __syncthreads();
             if (a.mode & 4) {
-                const double acc = apply_table<T, Lay>(s, a, tile, W, other);
-                block_partial(acc, a.partial + (long long)other * gridDim.x + tile);
+                err = apply_table<T, Lay>(s, a, tile, W, other);
                 __syncthreads();
             }
 #pragma unroll
@@ -185,17 +191,19 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_col_reg(ColPassA
     }
     (void)NST;
     cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
+    const unsigned odim = (unsigned)a.out_dim;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         int e = reg_final_index<N>(j, k) + a.out_c;
         if (e >= N) e -= N;
-        if (valid && e < a.out_cnt) out[(long long)e * a.out_dim] = mk(v[k].x * a.scale, v[k].y * a.scale);
+        if (valid && e < a.out_cnt) out[(unsigned)e * odim] = mk(v[k].x * a.scale, v[k].y * a.scale);
     }
+    if (a.mode & 4) block_partial((double)err, a.partial + (long long)other * gridDim.x + tile);
 }
 
 // Row passes (same contract as k_rows_r2c / k_rows_c2r) for N a power of two.
 template <typename T, int N>
-__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_row_r2c_reg(RowPassArgs<T> a)
+__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_row_r2c_reg(RowPassArgs<T> a)
 {
     constexpr int W = reg_width<T>(N);
     constexpr int TPC = N / 8;
@@ -248,7 +256,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_row_r2c_reg(RowP
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), 2) k_row_c2r_reg(RowPassArgs<T> a)
+__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_row_c2r_reg(RowPassArgs<T> a)
 {
     constexpr int W = reg_width<T>(N);
     constexpr int TPC = N / 8;
