@@ -122,16 +122,20 @@ __device__ __forceinline__ float apply_table(cplx<T> *s, const ColPassArgs<T> &a
     return acc;
 }
 
-__device__ __forceinline__ void block_partial(double acc, double *out)
+// CTA sum of the per-thread errK terms: warp sums in FP32 (a few terms per
+// thread), the per-warp partials in FP64.  FP64 arithmetic is kept to one warp
+// because its throughput on this part is a small fraction of FP32's.
+__device__ __forceinline__ void block_partial(float acc, double *out)
 {
     __shared__ double red[32];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)acc;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        double v = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) *out = v;
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        const int nw = (blockDim.x + 31) / 32;
+        for (int w = 0; w < nw; ++w) v += red[w];
+        *out = v;
     }
 }
 
@@ -198,7 +202,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_c
         if (e >= N) e -= N;
         if (valid && e < a.out_cnt) out[(unsigned)e * odim] = mk(v[k].x * a.scale, v[k].y * a.scale);
     }
-    if (a.mode & 4) block_partial((double)err, a.partial + (long long)other * gridDim.x + tile);
+    if (a.mode & 4) block_partial(err, a.partial + (long long)other * gridDim.x + tile);
 }
 
 // Row passes (same contract as k_rows_r2c / k_rows_c2r) for N a power of two.
