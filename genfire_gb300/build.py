@@ -34,7 +34,8 @@ def sources():
 
 
 def _deps():
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, "genfire.h")]
+    return ([os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(INCLUDE, "genfire.h")]
+            + [os.path.join(HERE, "harness", f) for f in os.listdir(os.path.join(HERE, "harness"))])
 
 
 def _stale(target, deps):
@@ -72,7 +73,22 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    build_harness()
     return LIB
+
+
+HARNESS_SRC = os.path.join(HERE, "harness", "genfire_run.c")
+HARNESS = os.path.join(OUT_DIR, "genfire_run")
+
+
+def build_harness():
+    """The standalone C driver (harness/genfire_run.c), linked against libgenfire.so."""
+    cmd = ["gcc", "-O2", "-std=c11", "-I", INCLUDE, HARNESS_SRC, "-o", HARNESS, "-L", OUT_DIR, "-lgenfire",
+           "-Wl,-rpath,$ORIGIN", "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("harness build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    return HARNESS
 
 
 if __name__ == "__main__":
