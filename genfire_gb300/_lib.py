@@ -31,7 +31,7 @@ EXPORTS = [
     "genfire_grid_dft", "genfire_grid_dft_device",
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
-    "genfire_project", "genfire_rfactor",
+    "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc",
     "genfire_centro_symmetricity", "genfire_hermitian_symmetrize", "genfire_make_kspace_indices",
     "genfire_volumn_index", "genfire_iffshift3_ind", "genfire_select", "genfire_fftn",
 ]
@@ -94,6 +94,8 @@ def load():
         "genfire_project": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp, dp, vp]),
         "genfire_rfactor": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp, dp, dp,
                                       dp, dp, dp]),
+        "genfire_rfactor_noalloc": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp,
+                                              dp, vp, dp, dp, dp]),
         "genfire_centro_symmetricity": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32, dp]),
         "genfire_hermitian_symmetrize": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32, dp]),
         "genfire_make_kspace_indices": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, dp]),

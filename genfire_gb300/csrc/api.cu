@@ -317,6 +317,34 @@ genfire_status genfire_rfactor(genfire_ctx *ctx, int32_t precision, const void *
     });
 }
 
+// Allocation-free: no std::function wrapper, no heap buffers; errors are
+// caught here directly.
+genfire_status genfire_rfactor_noalloc(genfire_ctx *ctx, int32_t precision, const void *d_vol, int32_t n1,
+                                       int32_t n2, int32_t n3, int32_t num_proj, const double *angles,
+                                       const double *vectors, const double *d_measured, double *Rarr,
+                                       double *Rarr2, double *errR)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    try {
+        GF_CUDA(cudaSetDevice(ctx->device));
+        ctx->last_error.clear();
+        need(d_vol, "vol");
+        need(angles, "angles");
+        need(d_measured, "measured");
+        if (precision != GENFIRE_PREC_FP64 && precision != GENFIRE_PREC_MIXED) gf::fail(GENFIRE_ERR_ARG, "bad precision.");
+        if (num_proj < 1) gf::fail(GENFIRE_ERR_ARG, "num_proj must be positive.");
+        if (n1 < 2 || n2 < 2 || n3 < 2) gf::fail(GENFIRE_ERR_ARG, "projector: every volume dimension must be at least 2.");
+        gf::rfactor_noalloc(ctx, precision, d_vol, n1, n2, n3, num_proj, angles, vectors, d_measured, Rarr, Rarr2, errR);
+        return GENFIRE_OK;
+    } catch (const Error &e) {
+        ctx->last_error = e.msg;
+        return e.st;
+    } catch (...) {
+        ctx->last_error = "GENFIRE: unexpected internal error";
+        return GENFIRE_ERR_STATE;
+    }
+}
+
 // ---------------------------------------------------------------- index and symmetry kernels
 genfire_status genfire_centro_symmetricity(genfire_ctx *ctx, const double *FS, int32_t n1, int32_t n_k1, int32_t n2,
                                            double *measuredK)

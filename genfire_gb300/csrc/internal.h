@@ -94,4 +94,11 @@ void project_batch(genfire_ctx *ctx, int precision, const void *d_vol, int n1, i
                    long long vs1, long long vs2, int P, const double *d_R, void *d_proj,
                    const double *d_measured, double *d_sums, cudaStream_t stream);
 
+// R-factors with the scratch in a static device array (no allocation); host
+// angles/vectors and outputs as genfire_rfactor.
+size_t rfactor_noalloc_bytes(int n1, int n2, int P);
+void rfactor_noalloc(genfire_ctx *ctx, int precision, const void *d_vol, int n1, int n2, int n3, int P,
+                     const double *angles, const double *vectors, const double *d_measured, double *Rarr,
+                     double *Rarr2, double *errR);
+
 }  // namespace gf

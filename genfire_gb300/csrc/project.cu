@@ -10,6 +10,9 @@
 // and reduced with warp shuffles, per projection, in a fixed order.
 #include "internal.h"
 
+#include <map>
+#include <mutex>
+
 namespace gf {
 
 template <typename T> struct Coord;
@@ -144,6 +147,103 @@ void project_batch(genfire_ctx *ctx, int precision, const void *d_vol, int n1, i
     else
         project_t<float>(ctx, (const float *)d_vol, n1, n2, n3, vs1, vs2, P, d_R, (float *)d_proj, d_measured,
                          d_sums, stream);
+}
+
+// ===========================================================================
+// R-factors without allocation (genfire_rfactor_noalloc)
+//
+// For callers that hold their data in device memory they do not own and may
+// not allocate more (for example a MEX function working on gpuArray data inside
+// MATLAB's memory manager, or a service that reserves the device's memory for
+// its own pool): the rotation matrices, the per-block partial sums and the
+// per-projection sums live in this file-scope device array instead of
+// cudaMalloc'd buffers.  Every GPU that loads the library holds the array until
+// the process exits.  All calls share it: calls whose GPU work overlaps (two
+// host threads, or two streams) race on it.  Nothing in it needs to start at
+// zero: each call writes every value it reads before reading it.
+// ===========================================================================
+constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB
+static __device__ __align__(256) unsigned char g_rfactor_scratch[kNoAllocScratchBytes];
+
+// Device address of the array on the current device.  The first call on a
+// device looks it up (cudaGetSymbolAddress) and caches it.
+static unsigned char *noalloc_scratch(int device)
+{
+    static std::mutex mu;
+    static std::map<int, unsigned char *> addr;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = addr.find(device);
+    if (it != addr.end()) return it->second;
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_rfactor_scratch);
+    if (e != cudaSuccess || !p)
+        fail(GENFIRE_ERR_CUDA, std::string("cudaGetSymbolAddress of the R-factor scratch array failed: ") +
+                                   cudaGetErrorString(e));
+    addr[device] = static_cast<unsigned char *>(p);
+    return static_cast<unsigned char *>(p);
+}
+
+size_t rfactor_noalloc_bytes(int n1, int n2, int P)
+{
+    const size_t nblk = cdiv((size_t)n1 * n2, kProjThreads);
+    const size_t a = (sizeof(double) * 9 * (size_t)P + 255) / 256 * 256;     // rotation matrices
+    const size_t b = (sizeof(double) * 4 * nblk * (size_t)P + 255) / 256 * 256;  // block partials
+    return a + b + sizeof(double) * 4 * (size_t)P;                          // per-projection sums
+}
+
+// Rotation matrices go up and the per-projection sums come back through
+// fixed-size chunks on the stack, so the call makes no heap allocation either.
+void rfactor_noalloc(genfire_ctx *ctx, int precision, const void *d_vol, int n1, int n2, int n3, int P,
+                     const double *angles, const double *vectors, const double *d_measured, double *Rarr,
+                     double *Rarr2, double *errR)
+{
+    const size_t need = rfactor_noalloc_bytes(n1, n2, P);
+    if (need > kNoAllocScratchBytes)
+        fail(GENFIRE_ERR_ARG, "rfactor_noalloc: the inputs need more than the 4 MiB static scratch "
+                              "(fewer projections per call, or genfire_rfactor).");
+    cudaStream_t st = ctx->stream;
+    unsigned char *base = noalloc_scratch(ctx->device);
+    const unsigned nblk = cdiv((size_t)n1 * n2, kProjThreads);
+    double *dR = reinterpret_cast<double *>(base);
+    double *part = reinterpret_cast<double *>(base + (sizeof(double) * 9 * (size_t)P + 255) / 256 * 256);
+    double *dsum = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(part) +
+                                              (sizeof(double) * 4 * nblk * (size_t)P + 255) / 256 * 256);
+    constexpr int CH = 64;
+    double chunk[CH * 9];
+    for (int c0 = 0; c0 < P; c0 += CH) {
+        const int cn = P - c0 < CH ? P - c0 : CH;
+        for (int i = 0; i < cn; ++i) {
+            const int q = c0 + i;
+            if (vectors) euler_rot(vectors, vectors + 3, vectors + 6, angles[q], angles[q + P], angles[q + 2 * P], chunk + 9 * i);
+            else rot_zyz(angles[q], angles[q + P], angles[q + 2 * P], chunk + 9 * i);
+        }
+        // pageable source: the copy is staged before the call returns, so the chunk can be refilled
+        GF_CUDA(cudaMemcpyAsync(dR + 9 * (size_t)c0, chunk, sizeof(double) * 9 * cn, cudaMemcpyHostToDevice, st));
+    }
+    dim3 grid(nblk, P);
+    if (precision == GENFIRE_PREC_FP64)
+        k_project<double><<<grid, kProjThreads, 0, st>>>((const double *)d_vol, n1, n2, n3, n1, (long long)n1 * n2,
+                                                        dR, nullptr, d_measured, part);
+    else
+        k_project<float><<<grid, kProjThreads, 0, st>>>((const float *)d_vol, n1, n2, n3, n1, (long long)n1 * n2,
+                                                       dR, nullptr, d_measured, part);
+    GF_CHECK_LAUNCH();
+    k_project_sums<<<P, 32, 0, st>>>(part, (int)nblk, dsum);
+    GF_CHECK_LAUNCH();
+    double tot = 0;
+    for (int c0 = 0; c0 < P; c0 += CH) {
+        const int cn = P - c0 < CH ? P - c0 : CH;
+        GF_CUDA(cudaMemcpyAsync(chunk, dsum + 4 * (size_t)c0, sizeof(double) * 4 * cn, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+        for (int i = 0; i < cn; ++i) {
+            const double *sm = chunk + 4 * i;
+            const double r1 = sm[0] / sm[1], r2 = std::sqrt(sm[2]) / std::sqrt(sm[3]);
+            if (Rarr) Rarr[c0 + i] = r1;
+            if (Rarr2) Rarr2[c0 + i] = r2;
+            tot += r1;
+        }
+    }
+    if (errR) *errR = tot / P;
 }
 
 }  // namespace gf

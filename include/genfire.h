@@ -194,6 +194,26 @@ genfire_status genfire_rfactor(genfire_ctx *ctx, int32_t precision,
                                const double *measured, double *Rarr, double *Rarr2,
                                double *errR);
 
+/* The R-factors of genfire_rfactor computed without allocating device memory.
+ * No counterpart in the reference.  It is for callers whose device memory is
+ * owned by someone else and who may not call cudaMalloc: for example a MEX
+ * function working on gpuArray data under MATLAB's memory manager, or a
+ * service that has reserved the device's memory for its own pool.  vol
+ * (n1 x n2 x n3, double for FP64, float for MIXED) and measured (n1 x n2 x
+ * num_proj double) are device pointers; angles and vectors are host arrays as
+ * for genfire_rfactor; Rarr, Rarr2 and errR are host outputs.  The scratch
+ * (rotation matrices and partial sums) is a 4 MiB static device array in the
+ * library, so the call allocates nothing; inputs needing more than 4 MiB of
+ * scratch (about 9 * num_proj + 4 * num_proj * (ceil(n1*n2/256) + 1) doubles)
+ * are rejected with GENFIRE_ERR_ARG.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  Every call uses the same array: calls whose GPU work
+ * overlaps (from two host threads, or on two streams) race on it. */
+genfire_status genfire_rfactor_noalloc(genfire_ctx *ctx, int32_t precision, const void *d_vol, int32_t n1,
+                                       int32_t n2, int32_t n3, int32_t num_proj, const double *angles,
+                                       const double *vectors, const double *d_measured, double *Rarr,
+                                       double *Rarr2, double *errR);
+
 /* ---- index and symmetry kernels (host pointers, FP64) -------------------- */
 
 /* CentroSymmetricity(obj, FS, n1, n_k1, n2)
