@@ -507,12 +507,6 @@ __global__ void k_iffshift(int s1, int s2, int s3, long long count, const long l
     }
 }
 
-__global__ void k_d2f(const double *__restrict__ in, float *__restrict__ out, long long n)
-{
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        out[i] = (float)in[i];
-}
-
 static unsigned grid_for(genfire_ctx *ctx, long long n, int threads)
 {
     long long b = (n + threads - 1) / threads;
@@ -585,31 +579,27 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     if (nk_out)
         for (int i = 0; i < P; ++i) nk_out[i] = sel.nk[i];
 
-    // DFT tiles: kDftJ consecutive points of one projection
-    std::vector<DftTile> tiles;
-    tiles.reserve((size_t)(sel.total / kDftJ + P));
-    for (int i = 0; i < P; ++i)
-        for (long long j = 0; j < sel.nk[i]; j += kDftJ)
-            tiles.push_back(DftTile{i, (int)std::min<long long>(kDftJ, sel.nk[i] - j), sel.off[i] + j});
     DevBuf F(sizeof(cplx<T>) * (size_t)std::max<long long>(sel.total, 1), st);
-    const T *d_projT;
-    DevBuf projF;
-    if (sizeof(T) == sizeof(double)) {
-        d_projT = reinterpret_cast<const T *>(d_proj);
+    if (sizeof(T) == sizeof(float)) {
+        // MIXED: split-BF16 tensor-core DFT (grid_mma.cu)
+        dft_tcgen05(ctx, d_proj, D1, D2, n1, n2, P, sel.nk, sel.off, sel.u.as<float>(), sel.v.as<float>(),
+                    reinterpret_cast<float2 *>(F.p));
     } else {
-        const long long np = (long long)D1 * D2 * P;
-        projF.alloc(sizeof(float) * np, st);
-        k_d2f<<<grid_for(ctx, np, 256), 256, 0, st>>>(d_proj, projF.as<float>(), np);
-        GF_CHECK_LAUNCH();
-        d_projT = reinterpret_cast<const T *>(projF.p);
-    }
-    if (!tiles.empty()) {
-        DevBuf dt(sizeof(DftTile) * tiles.size(), st);
-        GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(DftTile) * tiles.size(), cudaMemcpyHostToDevice, st));
-        k_dft<T><<<(unsigned)tiles.size(), 256, 0, st>>>(d_projT, D1, D2, n1, n2, dt.as<DftTile>(),
-                                                         sel.u.as<float>(), sel.v.as<float>(), F.as<cplx<T>>());
-        GF_CHECK_LAUNCH();
-        GF_CUDA(cudaStreamSynchronize(st));
+        // FP64: kDftJ consecutive points of one projection per CTA
+        std::vector<DftTile> tiles;
+        tiles.reserve((size_t)(sel.total / kDftJ + P));
+        for (int i = 0; i < P; ++i)
+            for (long long j = 0; j < sel.nk[i]; j += kDftJ)
+                tiles.push_back(DftTile{i, (int)std::min<long long>(kDftJ, sel.nk[i] - j), sel.off[i] + j});
+        if (!tiles.empty()) {
+            DevBuf dt(sizeof(DftTile) * tiles.size(), st);
+            GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(DftTile) * tiles.size(), cudaMemcpyHostToDevice, st));
+            k_dft<double><<<(unsigned)tiles.size(), 256, 0, st>>>(d_proj, D1, D2, n1, n2, dt.as<DftTile>(),
+                                                                   sel.u.as<float>(), sel.v.as<float>(),
+                                                                   reinterpret_cast<double2 *>(F.p));
+            GF_CHECK_LAUNCH();
+            GF_CUDA(cudaStreamSynchronize(st));
+        }
     }
 
     // weighted average in FP64, projection by projection

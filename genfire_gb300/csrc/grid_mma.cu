@@ -1,0 +1,456 @@
+// grid_mma.cu -- the MIXED-precision gridding DFT on the 5th-generation tensor
+// cores (tcgen05, sm_103a).
+//
+// For one projection P (D1 x D2) and a tile of 128 selected K-points j:
+//   Q(j, b) = sum_a E_u(j, a) P(a, b),  E_u(j, a) = exp(-2 pi i a u_j / n1)
+//   F_j     = sum_b Q(j, b) E_v(j, b),  E_v(j, b) = exp(-2 pi i b v_j / n2)
+// (fillInFourierGrid_DFT.m:243).  Q is a GEMM with M = 128 K-points, N = D2
+// (256-column chunks), K = D1 (32-wide chunks).  Operands are split into BF16
+// hi + lo parts and multiplied as hi*hi + hi*lo + lo*hi (FP32 accumulation),
+// which keeps ~16 significant bits of each operand:
+//   Re Q += Re(E_u)_hi P_hi + Re(E_u)_hi P_lo + Re(E_u)_lo P_hi   (TMEM cols   0..255)
+//   Im Q += Im(E_u)_hi P_hi + Im(E_u)_hi P_lo + Im(E_u)_lo P_hi   (TMEM cols 256..511)
+// * B (P, hi and lo) is pre-split once per projection into the canonical
+//   no-swizzle K-major layout and fed per K-chunk by cp.async.bulk (the TMA
+//   engine) into shared memory, completing on an mbarrier.
+// * A (E_u) is generated on the fly by the CTA's threads: per row, anchor
+//   phases are reduced exactly in FP64 (a*u is exact, the fractional part is
+//   taken before sincospi) and advanced by FP32 rotations within 16-element
+//   blocks, then split into BF16 hi/lo and stored in the same layout.
+// * One elected thread issues tcgen05.mma (M = 128, N = 256, K = 16) and
+//   tcgen05.commit; shared-memory stages are double buffered so the next
+//   chunk is generated while the tensor core works on the current one.
+// * The epilogue reads the accumulators with tcgen05.ld (one row per thread,
+//   two warps per 32-lane quadrant) and contracts them with E_v generated the
+//   same way.
+// Every mbarrier wait is bounded by a clock limit; on expiry the kernel records
+// an error flag, stops issuing work, waits (bounded) for its copies and MMAs,
+// frees its TMEM and returns.
+#include "internal.h"
+
+#include <cuda_bf16.h>
+
+namespace gf {
+
+namespace umma {
+
+constexpr int kThreads = 256;      // 8 warps
+constexpr int kM = 128;            // rows per tile
+constexpr int kKC = 32;            // K per chunk (two MMA k-steps of 16)
+constexpr int kNC = 256;           // N per chunk (columns of one accumulator)
+constexpr int kATile = kM * kKC;   // bf16 elements of one A array (8 KB)
+constexpr int kBTile = kNC * kKC;  // bf16 elements of one B array (16 KB)
+// stage: A re_hi, re_lo, im_hi, im_lo (4 x 8 KB) then B hi, lo (2 x 16 KB)
+constexpr int kStageBytes = 4 * kATile * 2 + 2 * kBTile * 2;  // 64 KB
+constexpr long long kWaitCycles = 4000000000LL;               // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Canonical no-swizzle K-major layout: core matrices of 8 rows x 8 bf16
+// (16 bytes per row, 128 bytes each); core matrices adjacent along K are 128 B
+// apart (leading byte offset), 8-row groups are 512 B apart (stride byte
+// offset) for a 32-wide K chunk.
+__device__ __forceinline__ int kmaj_index(int row, int k) { return (row >> 3) * 256 + (k >> 3) * 64 + (row & 7) * 8 + (k & 7); }
+constexpr uint32_t kLBO = 128, kSBO = 512;
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((kLBO >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((kSBO >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;  // descriptor version of the 5th-generation tensor core
+    return d;                // base offset 0, no swizzle
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; returns false on expiry
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    while (!mbar_try(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(dst)), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t accum)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(accum)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// exp(-2 pi i * a * w / n) for integer a and FP32 w, phase reduced in FP64
+__device__ __forceinline__ float2 phase_exact(int a, float w, double inv_n)
+{
+    double t = (double)a * (double)w * inv_n;
+    t -= rint(t);
+    float s, c;
+    sincospif((float)(-2.0 * t), &s, &c);
+    return make_float2(c, s);
+}
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem)
+{
+    __nv_bfloat162 t = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x = first (lower address)
+    return *reinterpret_cast<uint32_t *>(&t);
+}
+
+}  // namespace umma
+
+// One work item: a tile of up to 128 consecutive selected points of one projection.
+struct MmaTile {
+    int proj;
+    int nj;
+    long long j0;
+};
+
+struct MmaArgs {
+    const __nv_bfloat16 *B;   // pre-split projections: [proj][nchunk][kchunk][hi|lo][256 x 32]
+    const MmaTile *tiles;
+    int ntiles;
+    const float *u, *v;
+    float2 *F;
+    int D1, D2, n1, n2;
+    int nkc, nnc;             // K chunks (32 wide), N chunks (256 wide)
+    int npad_last;            // columns of the last N chunk, a multiple of 32
+    int *err;                 // set to 1 when a bounded wait expires
+};
+
+__global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
+{
+    using namespace umma;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // carve: [stage 0][stage 1] (64 KB each), then barriers and scratch
+    unsigned char *stage_base = smem_raw;
+    uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem_raw + 2 * kStageBytes);
+    uint64_t *bar_mma = bar_load + 2;
+    uint64_t *bar_done = bar_mma + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_done + 1);
+    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
+    float2 *red = reinterpret_cast<float2 *>(smem_raw + 2 * kStageBytes + 128);  // 128 partial F
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        mbar_init(&bar_load[0], 1);
+        mbar_init(&bar_load[1], 1);
+        mbar_init(&bar_mma[0], 1);
+        mbar_init(&bar_mma[1], 1);
+        mbar_init(bar_done, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    uint32_t n_load[2] = {0, 0}, n_mma[2] = {0, 0}, n_done = 0;  // completions issued per barrier
+    uint32_t w_load[2] = {0, 0}, w_mma[2] = {0, 0}, w_done = 0;  // completions waited per barrier
+    const double inv1 = 1.0 / (double)a.n1, inv2 = 1.0 / (double)a.n2;
+    const int amin = -(a.D1 / 2), bmin = -(a.D2 / 2);
+    const int r = tid & (kM - 1), h = tid >> 7;  // A generation: row r, half h of the 32-wide chunk
+    bool ok = true;
+
+    for (int item = blockIdx.x; item < a.ntiles && ok; item += gridDim.x) {
+        const MmaTile tl = a.tiles[item];
+        const bool row_ok = r < tl.nj;
+        const float uj = row_ok ? a.u[tl.j0 + r] : 0.f;
+        // epilogue row and column half
+        const int erow = (warp & 3) * 32 + lane, ehalf = warp >> 2;
+        const bool erow_ok = erow < tl.nj;
+        const float vj = erow_ok ? a.v[tl.j0 + erow] : 0.f;
+        float2 Fsum = make_float2(0.f, 0.f);
+
+        for (int nc = 0; nc < a.nnc && ok; ++nc) {
+            const int N = (nc == a.nnc - 1) ? a.npad_last : kNC;
+            const uint32_t idesc = idesc_bf16(kM, N);
+            // A anchors for this thread: S = E_u(amin + 16h), rotations by 1 and by 32
+            float2 S = row_ok ? phase_exact(amin + 16 * h, uj, inv1) : make_float2(0.f, 0.f);
+            const float2 w1 = phase_exact(1, uj, inv1), w32 = phase_exact(32, uj, inv1);
+            const __nv_bfloat16 *Bp = a.B + ((size_t)(tl.proj * a.nnc + nc) * a.nkc) * 2 * kBTile;
+            for (int kc = 0; kc < a.nkc; ++kc) {
+                const int s = kc & 1;
+                unsigned char *st = stage_base + s * kStageBytes;
+                __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(st);  // re_hi, re_lo, im_hi, im_lo
+                __nv_bfloat16 *Bs = Ah + 4 * kATile;                          // hi, lo
+                // the MMAs that last read this stage must be complete
+                if (w_mma[s] < n_mma[s]) {
+                    if (!mbar_wait(&bar_mma[s], w_mma[s] & 1)) { *abort_flag = 1; }
+                    ++w_mma[s];
+                }
+                __syncthreads();
+                if (*abort_flag) { ok = false; break; }
+                if (tid == 0) {
+                    mbar_expect_tx(&bar_load[s], 2 * kBTile * 2);
+                    const __nv_bfloat16 *src = Bp + (size_t)kc * 2 * kBTile;
+                    bulk_g2s(Bs, src, kBTile * 2, &bar_load[s]);
+                    bulk_g2s(Bs + kBTile, src + kBTile, kBTile * 2, &bar_load[s]);
+                }
+                ++n_load[s];
+                // A: 16 consecutive k for row r: k = 16h .. 16h+15 of this chunk
+                {
+                    float2 e = S;
+                    uint32_t rh[8], rl[8], ih[8], il[8];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        float2 e0 = e;
+                        e = cmulf(e, w1);
+                        float2 e1 = e;
+                        e = cmulf(e, w1);
+                        const float r0h = __bfloat162float(__float2bfloat16_rn(e0.x));
+                        const float r1h = __bfloat162float(__float2bfloat16_rn(e1.x));
+                        const float i0h = __bfloat162float(__float2bfloat16_rn(e0.y));
+                        const float i1h = __bfloat162float(__float2bfloat16_rn(e1.y));
+                        rh[q] = pack_bf16(r0h, r1h);
+                        rl[q] = pack_bf16(e0.x - r0h, e1.x - r1h);
+                        ih[q] = pack_bf16(i0h, i1h);
+                        il[q] = pack_bf16(e0.y - i0h, e1.y - i1h);
+                    }
+                    S = cmulf(S, w32);
+                    // two 16-byte core-matrix rows (k = 16h..16h+7 and 16h+8..16h+15) per array
+#pragma unroll
+                    for (int g = 0; g < 2; ++g) {
+                        const int idx = kmaj_index(r, 16 * h + 8 * g);
+                        *reinterpret_cast<uint4 *>(Ah + 0 * kATile + idx) = make_uint4(rh[4 * g], rh[4 * g + 1], rh[4 * g + 2], rh[4 * g + 3]);
+                        *reinterpret_cast<uint4 *>(Ah + 1 * kATile + idx) = make_uint4(rl[4 * g], rl[4 * g + 1], rl[4 * g + 2], rl[4 * g + 3]);
+                        *reinterpret_cast<uint4 *>(Ah + 2 * kATile + idx) = make_uint4(ih[4 * g], ih[4 * g + 1], ih[4 * g + 2], ih[4 * g + 3]);
+                        *reinterpret_cast<uint4 *>(Ah + 3 * kATile + idx) = make_uint4(il[4 * g], il[4 * g + 1], il[4 * g + 2], il[4 * g + 3]);
+                    }
+                }
+                fence_proxy_async();
+                __syncthreads();
+                if (!mbar_wait(&bar_load[s], w_load[s] & 1)) *abort_flag = 1;
+                ++w_load[s];
+                __syncthreads();
+                if (*abort_flag) { ok = false; break; }
+                if (tid == 0) {
+                    tc_fence_after();
+                    const uint32_t a_base = saddr(Ah), b_base = saddr(Bs);
+#pragma unroll
+                    for (int ks = 0; ks < 2; ++ks) {
+                        const uint32_t ko = ks * 16 * 16;  // 16 k = two core matrices = 256 bytes
+                        const uint64_t b_hi = sdesc(b_base + ko), b_lo = sdesc(b_base + kBTile * 2 + ko);
+                        const uint64_t a_rh = sdesc(a_base + ko), a_rl = sdesc(a_base + kATile * 2 + ko);
+                        const uint64_t a_ih = sdesc(a_base + 2 * kATile * 2 + ko), a_il = sdesc(a_base + 3 * kATile * 2 + ko);
+                        const uint32_t first = (kc == 0 && ks == 0) ? 0u : 1u;
+                        mma_bf16(tmem, a_rh, b_hi, idesc, first);
+                        mma_bf16(tmem, a_rh, b_lo, idesc, 1u);
+                        mma_bf16(tmem, a_rl, b_hi, idesc, 1u);
+                        mma_bf16(tmem + 256, a_ih, b_hi, idesc, first);
+                        mma_bf16(tmem + 256, a_ih, b_lo, idesc, 1u);
+                        mma_bf16(tmem + 256, a_il, b_hi, idesc, 1u);
+                    }
+                    mma_commit(&bar_mma[s]);
+                }
+                ++n_mma[s];
+            }
+            if (!ok) break;
+            // all MMAs of this N chunk done -> epilogue
+            if (tid == 0) mma_commit(bar_done);
+            ++n_done;
+            if (!mbar_wait(bar_done, w_done & 1)) *abort_flag = 1;
+            ++w_done;
+            tc_fence_after();
+            __syncthreads();
+            if (*abort_flag) { ok = false; break; }
+            {
+                const int half = N / 2;                  // columns per warp half (multiple of 16)
+                const int c0 = ehalf * half;
+                const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+                float2 Sv = erow_ok ? phase_exact(bmin + nc * kNC + c0, vj, inv2) : make_float2(0.f, 0.f);
+                const float2 v1 = phase_exact(1, vj, inv2);
+                for (int c = 0; c < half; c += 16) {
+                    uint32_t re[16], im[16];
+                    tmem_ld16(tmem + lane_base + (uint32_t)(c0 + c), re);
+                    tmem_ld16(tmem + lane_base + 256u + (uint32_t)(c0 + c), im);
+                    tmem_wait_ld();
+                    float2 e = Sv;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const float qr = __uint_as_float(re[i]), qi = __uint_as_float(im[i]);
+                        Fsum.x += qr * e.x - qi * e.y;
+                        Fsum.y += qr * e.y + qi * e.x;
+                        e = cmulf(e, v1);
+                    }
+                    Sv = erow_ok ? phase_exact(bmin + nc * kNC + c0 + c + 16, vj, inv2) : Sv;
+                }
+            }
+            tc_fence_before();
+            __syncthreads();  // TMEM reads finished before the next MMAs overwrite it
+        }
+        if (!ok) break;
+        // combine the two column halves of each row and store
+        if (ehalf == 1) red[erow] = Fsum;
+        __syncthreads();
+        if (ehalf == 0 && erow_ok) {
+            const float2 o = red[erow];
+            a.F[tl.j0 + erow] = make_float2(Fsum.x + o.x, Fsum.y + o.y);
+        }
+        __syncthreads();
+    }
+
+    if (!ok && tid == 0) atomicExch(a.err, 1);
+    // drain: bounded waits for copies and MMAs still in flight, then free TMEM
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            while (w_load[s] < n_load[s]) { mbar_wait(&bar_load[s], w_load[s] & 1); ++w_load[s]; }
+            while (w_mma[s] < n_mma[s]) { mbar_wait(&bar_mma[s], w_mma[s] & 1); ++w_mma[s]; }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+// Pre-split projections into BF16 hi/lo in the B layout (one 16 KB array per
+// (projection, N chunk, K chunk, hi|lo)); zero beyond D1 x D2.
+__global__ void k_split_projections(const double *__restrict__ proj, int D1, int D2, int P, int nkc, int nnc,
+                                    __nv_bfloat16 *__restrict__ B)
+{
+    using namespace umma;
+    const long long total = (long long)P * nnc * nkc * kBTile;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+        const int e = (int)(t % kBTile);
+        long long blk = t / kBTile;  // (p * nnc + nc) * nkc + kc
+        const int kc = (int)(blk % nkc);
+        blk /= nkc;
+        const int nc = (int)(blk % nnc);
+        const int p = (int)(blk / nnc);
+        // e is the linear position in the layout: invert kmaj_index
+        const int rg = e >> 8, kg = (e >> 6) & 3, rr = (e >> 3) & 7, kk = e & 7;
+        const int row = rg * 8 + rr, k = kg * 8 + kk;
+        const int b = nc * kNC + row, aa = kc * kKC + k;
+        double x = 0.0;
+        if (b < D2 && aa < D1) x = proj[(long long)p * D1 * D2 + aa + (long long)D1 * b];
+        const float xf = (float)x;
+        const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(xf - __bfloat162float(hi));
+        const long long base = (((long long)p * nnc + nc) * nkc + kc) * 2 * kBTile;
+        B[base + e] = hi;
+        B[base + kBTile + e] = lo;
+    }
+}
+
+// Host: F (float2, one per selected point) for all projections.
+void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
+                 const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
+                 const float *d_v, float2 *d_F)
+{
+    using namespace umma;
+    cudaStream_t st = ctx->stream;
+    const int nkc = (D1 + kKC - 1) / kKC;
+    const int nnc = (D2 + kNC - 1) / kNC;
+    const int last = D2 - (nnc - 1) * kNC;
+    const int npad_last = (last + 31) / 32 * 32;
+    const size_t nB = (size_t)P * nnc * nkc * 2 * kBTile;
+    DevBuf B(nB * sizeof(__nv_bfloat16), st);
+    {
+        const long long total = (long long)P * nnc * nkc * kBTile;
+        long long blocks = (total + 255) / 256;
+        if (blocks > (long long)ctx->sm_count * 16) blocks = (long long)ctx->sm_count * 16;
+        k_split_projections<<<(unsigned)blocks, 256, 0, st>>>(d_proj, D1, D2, P, nkc, nnc, B.as<__nv_bfloat16>());
+        GF_CHECK_LAUNCH();
+    }
+    std::vector<MmaTile> tiles;
+    for (int p = 0; p < P; ++p)
+        for (long long j = 0; j < nk[p]; j += kM)
+            tiles.push_back(MmaTile{p, (int)std::min<long long>(kM, nk[p] - j), off[p] + j});
+    if (tiles.empty()) return;
+    DevBuf dt(sizeof(MmaTile) * tiles.size(), st), derr(sizeof(int), st);
+    GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(MmaTile) * tiles.size(), cudaMemcpyHostToDevice, st));
+    GF_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), st));
+    MmaArgs a;
+    a.B = B.as<__nv_bfloat16>();
+    a.tiles = dt.as<MmaTile>();
+    a.ntiles = (int)tiles.size();
+    a.u = d_u;
+    a.v = d_v;
+    a.F = d_F;
+    a.D1 = D1; a.D2 = D2; a.n1 = n1; a.n2 = n2;
+    a.nkc = nkc; a.nnc = nnc; a.npad_last = npad_last;
+    a.err = derr.as<int>();
+    const size_t smem = 2 * (size_t)kStageBytes + 128 + 128 * sizeof(float2);
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_dft_tcgen05, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = (int)std::min<size_t>(tiles.size(), (size_t)ctx->sm_count);
+    k_dft_tcgen05<<<grid, kThreads, smem, st>>>(a);
+    GF_CHECK_LAUNCH();
+    int herr = 0;
+    GF_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GF_CUDA(cudaStreamSynchronize(st));
+    if (herr) fail(GENFIRE_ERR_TIMEOUT, "tensor-core gridding: a bounded wait for the tensor core or a bulk copy expired.");
+}
+
+}  // namespace gf

@@ -55,6 +55,12 @@ void check_params(const genfire_params &p, bool need_projs);
 void grid_dft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
               void *d_M, void *d_rec, int64_t *nk);
 
+// MIXED DFT of all selected points on the tensor cores (grid_mma.cu): F[j]
+// (complex64) for the points of every projection (counts nk, offsets off).
+void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
+                 const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
+                 const float *d_v, float2 *d_F);
+
 // Selection of one projection into host arrays (test entry point).
 long long select_one(genfire_ctx *ctx, const genfire_params &p, double phi, double theta, double psi,
                      long long cap, int64_t *ind, float *dist, float *u, float *v);
