@@ -1,8 +1,9 @@
 // grid.cu -- DFT gridding (fillInFourierGrid_DFT) and the index/symmetry kernels.
 //
 // Pipeline for P projections (all on the context stream):
-//   1. k_sel_count   every grid point x every projection, FP32 plane test;
-//                    one count per 4096-point chunk
+//   1. k_sel_count   per row (k2, k3) of the gridded space and projection: the
+//                    k1 interval near the plane, FP32 plane test of its points;
+//                    one count per 1024-row chunk
 //   2. k_sel_scan    per-projection exclusive scan of the chunk counts
 //   3. k_sel_write   ordered compaction: (index, D, u, v) in ascending index
 //                    order within each projection, i.e. the order of find()
@@ -155,25 +156,25 @@ void check_params(const genfire_params &p, bool need_projs)
 // ===========================================================================
 struct SelParams {
     int lo1, lo2, lo3, l1, l2;
-    int total;
-    int nchunks;
+    int nrows;    // l2 * l3 rows of the gridded index space
+    int nchunks;  // CTAs per projection
     double cutoff, half1, half2;
 };
 
+// Rows (k2, k3) of the gridded index space are the work units: the points of
+// a row that can lie within the cutoff of the plane form one interval of k1,
+// found with conservative FP32 bounds; only those candidates get the exact
+// test, and rows are taken in (k3, k2) order so the output keeps the
+// ascending linear order of find().
 constexpr int kSelThreads = 256;
-constexpr int kSelItems = 16;
-constexpr int kSelChunk = kSelThreads * kSelItems;
+constexpr int kSelItems = 4;
+constexpr int kSelChunk = kSelThreads * kSelItems;  // rows per CTA
 
-// FP32 plane test of grid point li (distancePointsPlane_YY, closestpoint,
-// R \ CP, box filter), with every rounding step explicit.
-__device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp, int li, float &D, float &u,
-                                         float &v)
+// FP32 plane test of grid point (K1, K2, K3) (distancePointsPlane_YY,
+// closestpoint, R \ CP, box filter), with every rounding step explicit.
+__device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp, float K1, float K2, float K3,
+                                         float &D, float &u, float &v)
 {
-    const int i1 = li % sp.l1;
-    const int r = li / sp.l1;
-    const int i2 = r % sp.l2;
-    const int i3 = r / sp.l2;
-    const float K1 = (float)(sp.lo1 + i1), K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
     D = fabsf(__fadd_rn(__fadd_rn(__fmul_rn(K1, g.h[0]), __fmul_rn(K2, g.h[1])), __fmul_rn(K3, g.h[2])));
     if (!((double)D < sp.cutoff)) return false;
     const float s = __fadd_rn(__fadd_rn(__fmul_rn(K1, g.nrm[0]), __fmul_rn(K2, g.nrm[1])), __fmul_rn(K3, g.nrm[2]));
@@ -200,6 +201,55 @@ __device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp,
     return fabs((double)b[0]) <= sp.half1 && fabs((double)b[1]) <= sp.half2;
 }
 
+// Candidate k1 range [k1a, k1b] of row (K2, K3): every k1 with
+// |k1 h1 + K2 h2 + K3 h3| below the cutoff, widened by a margin that covers the
+// FP32 rounding of D (|error| < 1e-3 for grids up to 2^16) and of the bounds.
+__device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp, float K2, float K3, int &k1a, int &k1b)
+{
+    const int lo = sp.lo1, hi = sp.lo1 + sp.l1 - 1;
+    const float x = -(K2 * g.h[1] + K3 * g.h[2]);
+    const float c = (float)sp.cutoff + 0.01f;
+    const float h1 = g.h[0];
+    k1a = lo;
+    k1b = hi;
+    if (fabsf(h1) >= 0.01f) {
+        float b0 = (x - c) / h1, b1 = (x + c) / h1;
+        if (b0 > b1) { const float t = b0; b0 = b1; b1 = t; }
+        b0 = fmaxf(b0, (float)lo - 4.f);
+        b1 = fminf(b1, (float)hi + 4.f);
+        k1a = max(lo, (int)floorf(b0) - 1);
+        k1b = min(hi, (int)ceilf(b1) + 1);
+    } else {
+        const float reach = fabsf(h1) * (float)max(-lo, hi);
+        if (fabsf(x) > c + reach) { k1a = 1; k1b = 0; }  // empty
+    }
+}
+
+// block-wide exclusive scan of one int per thread; *total receives the sum
+__device__ __forceinline__ int block_exclusive_scan(int x, int *total)
+{
+    __shared__ int wsum[kSelThreads / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    int woff = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < kSelThreads / 32; ++k) {
+        const int c = wsum[k];
+        woff += (k < w) ? c : 0;
+        tot += c;
+    }
+    __syncthreads();
+    *total = tot;
+    return woff + inc - x;
+}
+
 __global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__restrict__ geo, SelParams sp,
                                                           int *__restrict__ counts)
 {
@@ -207,10 +257,21 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__res
     const ProjGeom g = geo[p];
     int total = 0;
     for (int it = 0; it < kSelItems; ++it) {
-        const int li = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
-        float D, u, v;
-        const bool pred = li < sp.total && sel_test(g, sp, li, D, u, v);
-        total += __syncthreads_count(pred);
+        const int ri = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
+        int cnt = 0;
+        if (ri < sp.nrows) {
+            const int i2 = ri % sp.l2, i3 = ri / sp.l2;
+            const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
+            int a0, a1;
+            row_range(g, sp, K2, K3, a0, a1);
+            for (int k1 = a0; k1 <= a1; ++k1) {
+                float D, u, v;
+                cnt += sel_test(g, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
+            }
+        }
+        int tot;
+        block_exclusive_scan(cnt, &tot);
+        total += tot;
     }
     if (threadIdx.x == 0) counts[(long long)p * sp.nchunks + chunk] = total;
 }
@@ -242,34 +303,37 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__res
                                                           uint32_t *__restrict__ ind, float *__restrict__ dist,
                                                           float *__restrict__ uu, float *__restrict__ vv)
 {
-    __shared__ int wsum[kSelThreads / 32];
     const int p = blockIdx.y, chunk = blockIdx.x;
     const ProjGeom g = geo[p];
     long long base = proj_off[p] + chunk_off[(long long)p * sp.nchunks + chunk];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int it = 0; it < kSelItems; ++it) {
-        const int li = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
-        float D = 0, u = 0, v = 0;
-        const bool pred = li < sp.total && sel_test(g, sp, li, D, u, v);
-        const unsigned m = __ballot_sync(0xffffffffu, pred);
-        if (lane == 0) wsum[w] = __popc(m);
-        __syncthreads();
-        int woff = 0, tot = 0;
-#pragma unroll
-        for (int k = 0; k < kSelThreads / 32; ++k) {
-            const int c = wsum[k];
-            woff += (k < w) ? c : 0;
-            tot += c;
+        const int ri = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
+        int cnt = 0, a0 = 1, a1 = 0, i2 = 0, i3 = 0;
+        float K2 = 0.f, K3 = 0.f;
+        if (ri < sp.nrows) {
+            i2 = ri % sp.l2;
+            i3 = ri / sp.l2;
+            K2 = (float)(sp.lo2 + i2);
+            K3 = (float)(sp.lo3 + i3);
+            row_range(g, sp, K2, K3, a0, a1);
+            for (int k1 = a0; k1 <= a1; ++k1) {
+                float D, u, v;
+                cnt += sel_test(g, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
+            }
         }
-        if (pred) {
-            const long long o = base + woff + __popc(m & ((1u << lane) - 1u));
-            ind[o] = (uint32_t)li;
-            dist[o] = D;
-            uu[o] = u;
-            vv[o] = v;
+        int tot;
+        long long o = base + block_exclusive_scan(cnt, &tot);
+        for (int k1 = a0; k1 <= a1; ++k1) {
+            float D, u, v;
+            if (sel_test(g, sp, (float)k1, K2, K3, D, u, v)) {
+                ind[o] = (uint32_t)((k1 - sp.lo1) + sp.l1 * ri);
+                dist[o] = D;
+                uu[o] = u;
+                vv[o] = v;
+                ++o;
+            }
         }
         base += tot;
-        __syncthreads();
     }
 }
 
@@ -532,8 +596,8 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     const int P = (int)geo.size();
     SelParams sp;
     sp.lo1 = g.lo1; sp.lo2 = g.lo2; sp.lo3 = g.lo3; sp.l1 = g.l1; sp.l2 = g.l2;
-    sp.total = (int)g.total;
-    sp.nchunks = (int)cdiv(g.total, kSelChunk);
+    sp.nrows = g.l2 * g.l3;
+    sp.nchunks = (int)cdiv(sp.nrows, kSelChunk);
     sp.cutoff = cutoff; sp.half1 = n1 / 2.0; sp.half2 = n2 / 2.0;
     DevBuf dgeo(sizeof(ProjGeom) * P, st);
     GF_CUDA(cudaMemcpyAsync(dgeo.p, geo.data(), sizeof(ProjGeom) * P, cudaMemcpyHostToDevice, st));

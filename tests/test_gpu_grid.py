@@ -149,3 +149,18 @@ def test_grid_dft_rejects_bad_parameters(lib, ctx, field, value, status):
         ctx.grid_dft(p, projs, angles)
     assert e.value.status == status
     assert str(e.value).startswith("GENFIRE:")
+
+
+@pytest.mark.parametrize("D1,D2,P,os_,cut", [(64, 64, 12, 2.0, 0.125), (40, 300, 3, 2.0, 0.3), (100, 72, 4, 2.0, 0.2),
+                                             (128, 128, 3, 2.0, 0.125)])
+def test_grid_dft_mixed_tensor_core_shapes(lib, ctx, oracle, D1, D2, P, os_, cut):
+    """Split-BF16 tensor-core DFT: several 128-point tiles, K (D1) not a multiple of 32,
+    N (D2) above 256 (two accumulator chunks)."""
+    projs, angles = _random_case(D1 + D2 + P, D1, D2, P)
+    kw = dict(oversamplingRatio=os_, interpolationCutoffDistance=cut, vector3=(0, 0, 1))
+    M, rec, nk = ctx.grid_dft(params(lib, D1, D2, P, precision="mixed", **kw), projs, angles)
+    Mo, reco, nko = oracle.grid_dft(oracle.make_params(D1, D2, P, **kw), projs, angles)
+    assert np.array_equal(nk, nko)
+    assert np.array_equal(M != 0, Mo != 0)
+    assert rel(M, Mo) < MIXED_TOL
+    assert rel(rec, reco) < MIXED_TOL
