@@ -106,6 +106,13 @@ genfire_status genfire_create(int32_t device, genfire_ctx **out)
         GF_CUDA(cudaSetDevice(device));
         GF_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
         GF_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+        // keep memory freed by the library's stream-ordered allocations in the
+        // device's pool instead of returning it to the driver at each
+        // synchronisation, so repeated calls do not re-map gigabytes
+        cudaMemPool_t pool;
+        GF_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+        uint64_t keep = UINT64_MAX;
+        GF_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
     });
     if (st != GENFIRE_OK) {
         delete c;

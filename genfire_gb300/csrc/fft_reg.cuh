@@ -25,15 +25,21 @@ template <int N> struct P2Plan {
     static constexpr int ns(int s) { return s == 0 ? 1 : ns(s - 1) * radix(s - 1); }
 };
 
-// shared-memory layouts with one padding row every 8 rows (bank spreading)
+// shared-memory layouts with one padding row every 8 rows (bank spreading).
+// idx(i0 + k*S, c) = idx(i0, c) + k * stride(S) whenever S is a multiple of 8,
+// or S == 1 with i0 a multiple of 8 and k < 8 -- which covers every exchange
+// of the schedules below, so each exchange is one base address plus
+// compile-time offsets.
 template <int N, int W> struct ColLayout {   // the W columns interleaved, column fastest
     static constexpr int SIZE = (N + N / 8) * W;
     static __device__ __forceinline__ int idx(int i, int c) { return (i + (i >> 3)) * W + c; }
+    static constexpr int stride(int S) { return (S % 8 == 0 ? S + S / 8 : S) * W; }
 };
 template <int N, int W> struct RowLayout {   // each column contiguous
     static constexpr int PC = N + N / 8;
     static constexpr int SIZE = PC * W;
     static __device__ __forceinline__ int idx(int i, int c) { return c * PC + i + (i >> 3); }
+    static constexpr int stride(int S) { return S % 8 == 0 ? S + S / 8 : S; }
 };
 
 template <typename T, int N, int S>
@@ -76,20 +82,52 @@ template <int N> __device__ __forceinline__ int reg_final_index(int j, int k)
     return reg_out_index<N, P2Plan<N>::NST - 1>(j, k);
 }
 
+// Shared-memory positions of the registers after stage S: register
+// k = b + r*NB sits at out_base<S>(j, c, b) + r * Lay::stride(NS).
+template <int N, class Lay, int S> __device__ __forceinline__ int out_base(int j, int c, int b)
+{
+    constexpr int R = P2Plan<N>::radix(S);
+    constexpr int NS = P2Plan<N>::ns(S);
+    const int jp = j + b * (N / 8);
+    const int kk = jp & (NS - 1);
+    return Lay::idx((jp - kk) * R + kk, c);
+}
+
+template <typename T, int N, class Lay, int S>
+__device__ __forceinline__ void store_stage(cplx<T> *s, const cplx<T> (&v)[8], int j, int c)
+{
+    constexpr int R = P2Plan<N>::radix(S);
+    constexpr int NB = 8 / R;
+    constexpr int ST = Lay::stride(P2Plan<N>::ns(S));
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        cplx<T> *q = s + out_base<N, Lay, S>(j, c, b);
+#pragma unroll
+        for (int r = 0; r < R; ++r) q[r * ST] = v[b + r * NB];
+    }
+}
+
+// next stage's inputs: register k holds x[j + k*N/8]
+template <typename T, int N, class Lay>
+__device__ __forceinline__ void load_stage(const cplx<T> *s, cplx<T> (&v)[8], int in_base)
+{
+    constexpr int ST = Lay::stride(N / 8);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = s[in_base + k * ST];
+}
+
 template <typename T, int N, class Lay, int S = 0>
 __device__ __forceinline__ void reg_fft(cplx<T> (&v)[8], cplx<T> *sA, cplx<T> *sB, int &buf, int j, int c,
-                                        const cplx<T> *__restrict__ tw, bool inv)
+                                        int in_base, const cplx<T> *__restrict__ tw, bool inv)
 {
     reg_stage<T, N, S>(v, j, tw, inv);
     if constexpr (S + 1 < P2Plan<N>::NST) {
         cplx<T> *s = buf ? sB : sA;
         buf ^= 1;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) s[Lay::idx(reg_out_index<N, S>(j, k), c)] = v[k];
+        store_stage<T, N, Lay, S>(s, v, j, c);
         __syncthreads();
-#pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = s[Lay::idx(j + k * (N / 8), c)];
-        reg_fft<T, N, Lay, S + 1>(v, sA, sB, buf, j, c, tw, inv);
+        load_stage<T, N, Lay>(s, v, in_base);
+        reg_fft<T, N, Lay, S + 1>(v, sA, sB, buf, j, c, in_base, tw, inv);
     }
 }
 
@@ -163,44 +201,59 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_c
     const int col = tile * W + c;
     const bool valid = col < a.ncols;
     const cplx<T> zero = mk((T)0, (T)0);
+    const int in_base = Lay::idx(j, c);
     cplx<T> v[8];
     {
         const cplx<T> *in = a.in + (long long)other * a.in_other + (long long)col * a.col_stride;
         const unsigned idim = (unsigned)a.in_dim;
+        int e = j + a.in_c;
+        if (e >= N) e -= N;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            int e = j + k * (N / 8) + a.in_c;
-            if (e >= N) e -= N;
             v[k] = (valid && e < a.in_cnt) ? in[(unsigned)e * idim] : zero;
+            e += N / 8;
+            if (e >= N) e -= N;
         }
     }
     int buf = 0;
     float err = 0.f;
-    if (a.mode & 1) reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, false);
+    if (a.mode & 1) reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, false);
     if (a.mode & 2) {
         if (a.mode & 1) {
             cplx<T> *s = buf ? sB : sA;
             buf ^= 1;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) s[Lay::idx(reg_final_index<N>(j, k), c)] = v[k];
+            store_stage<T, N, Lay, NST - 1>(s, v, j, c);
             __syncthreads();
             if (a.mode & 4) {
                 err = apply_table<T, Lay>(s, a, tile, W, other);
                 __syncthreads();
             }
-#pragma unroll
-            for (int k = 0; k < 8; ++k) v[k] = s[Lay::idx(j + k * (N / 8), c)];
+            load_stage<T, N, Lay>(s, v, in_base);
         }
-        reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, true);
+        reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, true);
     }
-    (void)NST;
     cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
     const unsigned odim = (unsigned)a.out_dim;
+    {
+        constexpr int R = P2Plan<N>::radix(NST - 1);
+        constexpr int NB = 8 / R;
+        constexpr int NS = P2Plan<N>::ns(NST - 1);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        int e = reg_final_index<N>(j, k) + a.out_c;
-        if (e >= N) e -= N;
-        if (valid && e < a.out_cnt) out[(unsigned)e * odim] = mk(v[k].x * a.scale, v[k].y * a.scale);
+        for (int b = 0; b < NB; ++b) {
+            const int jp = j + b * (N / 8);
+            const int kk = jp & (NS - 1);
+            int e = (jp - kk) * R + kk + a.out_c;
+            if (e >= N) e -= N;
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                if (valid && e < a.out_cnt) {
+                    const cplx<T> x = v[b + r * NB];
+                    out[(unsigned)e * odim] = mk(x.x * a.scale, x.y * a.scale);
+                }
+                e += NS;
+                if (e >= N) e -= N;
+            }
+        }
     }
     if (a.mode & 4) block_partial(err, a.partial + (long long)other * gridDim.x + tile);
 }
@@ -241,10 +294,10 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
         v[k] = mk(va, vb);
     }
     int buf = 0;
-    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, false);
+    const int in_base = Lay::idx(j, c);
+    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, false);
     cplx<T> *s = buf ? sB : sA;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) s[Lay::idx(reg_final_index<N>(j, k), c)] = v[k];
+    store_stage<T, N, Lay, P2Plan<N>::NST - 1>(s, v, j, c);
     __syncthreads();
     const int rbase = blockIdx.x * W * 2;
     for (int idx = threadIdx.x; idx < W * a.h1; idx += blockDim.x) {
@@ -283,10 +336,10 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     }
     __syncthreads();
     cplx<T> v[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = sA[Lay::idx(j + k * TPC, c)];
+    const int in_base = Lay::idx(j, c);
+    load_stage<T, N, Lay>(sA, v, in_base);
     int buf = 1;
-    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, a.tw, true);
+    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, true);
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {

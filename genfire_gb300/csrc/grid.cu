@@ -472,6 +472,8 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
     return (long long)(k1 - g.lo1) + (long long)g.l1 * ((k2 - g.lo2) + (long long)g.l2 * (k3 - g.lo3));
 }
 
+// Most of the grid is untouched: the exact flag and the weight sum are read
+// first, the complex sums only where one of them is set.
 template <typename TO>
 __global__ void k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
                            const double2 *__restrict__ ex, const uint8_t *__restrict__ hx, GridSpec g, int n1,
@@ -484,12 +486,16 @@ __global__ void k_finalize(const double2 *__restrict__ num, const double *__rest
         const int c2 = (int)(r % n2), c3 = (int)(r / n2);
         bool cj;
         const long long li = src_index(g, n1, n2, centro, c1, c2, c3, cj);
-        double2 v;
-        if (hx[li]) v = ex[li];
-        else {
-            v = num[li];
+        double2 v = make_double2(0.0, 0.0);
+        if (hx[li]) {
+            v = ex[li];
+        } else {
             const double ws = wsum[li];
-            if (ws > 0) { v.x /= ws; v.y /= ws; }
+            if (ws > 0) {
+                v = num[li];
+                v.x /= ws;
+                v.y /= ws;
+            }
         }
         M[o] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
     }
