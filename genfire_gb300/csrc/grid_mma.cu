@@ -157,6 +157,44 @@ __device__ __forceinline__ float2 phase_exact(int a, float w, double inv_n)
 }
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
+// exp(-2 pi i * a * w / 2^t) with the phase reduced exactly in integer
+// arithmetic: w = m * 2^e (m the 24-bit significand), a * m is exact in 64
+// bits, and the fraction of a*m*2^(e-t) is its low (t-e) bits.  No FP64 (the
+// FP64 pipe issues 2 instructions per clock per SM on this part).
+__device__ __forceinline__ float2 phase_pow2(int a, float w, int t)
+{
+    const int bits = __float_as_int(w);
+    const int ex = (bits >> 23) & 0xFF;
+    float f;
+    if (ex == 0) {
+        f = 0.f;  // zero or subnormal: the phase is below 2^-100
+    } else {
+        long long m = (long long)((bits & 0x7FFFFF) | 0x800000);
+        if (bits < 0) m = -m;
+        const int sh = t - (ex - 150);  // a*w/2^t = (a*m) * 2^-sh
+        const long long P = (long long)a * m;
+        if (sh <= 0) {
+            f = 0.f;  // an integer number of turns
+        } else if (sh >= 62) {
+            f = (float)P * __int_as_float((127 - (sh > 125 ? 125 : sh)) << 23);
+            if (sh > 125) f = 0.f;
+        } else {
+            long long low = P & ((1LL << sh) - 1);
+            if (low >= (1LL << (sh - 1))) low -= (1LL << sh);  // to [-1/2, 1/2) turns
+            f = (float)low * __int_as_float((127 - sh) << 23);
+        }
+    }
+    float sv, cv;
+    sincospif(-2.f * f, &sv, &cv);
+    return make_float2(cv, sv);
+}
+
+// exact phase for any n: the power-of-two form when log2n >= 0, else FP64
+__device__ __forceinline__ float2 phase_any(int a, float w, int log2n, double inv_n)
+{
+    return log2n >= 0 ? phase_pow2(a, w, log2n) : phase_exact(a, w, inv_n);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem)
 {
     __nv_bfloat162 t = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x = first (lower address)
@@ -179,6 +217,7 @@ struct MmaArgs {
     const float *u, *v;
     float2 *F;
     int D1, D2, n1, n2;
+    int log2n1, log2n2;       // log2 of n1, n2 when powers of two, else -1
     int nkc, nnc;             // K chunks (32 wide), N chunks (256 wide)
     int npad_last;            // columns of the last N chunk, a multiple of 32
     int *err;                 // set to 1 when a bounded wait expires
@@ -237,8 +276,8 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
             const int N = (nc == a.nnc - 1) ? a.npad_last : kNC;
             const uint32_t idesc = idesc_bf16(kM, N);
             // A anchors for this thread: S = E_u(amin + 16h), rotations by 1 and by 32
-            float2 S = row_ok ? phase_exact(amin + 16 * h, uj, inv1) : make_float2(0.f, 0.f);
-            const float2 w1 = phase_exact(1, uj, inv1), w32 = phase_exact(32, uj, inv1);
+            float2 S = row_ok ? phase_any(amin + 16 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
+            const float2 w1 = phase_any(1, uj, a.log2n1, inv1), w32 = phase_any(32, uj, a.log2n1, inv1);
             const __nv_bfloat16 *Bp = a.B + ((size_t)(tl.proj * a.nnc + nc) * a.nkc) * 2 * kBTile;
             for (int kc = 0; kc < a.nkc; ++kc) {
                 const int s = kc & 1;
@@ -326,25 +365,28 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
             __syncthreads();
             if (*abort_flag) { ok = false; break; }
             {
+                // F_j += sum_b Q(j,b) E_v(j,b): per 16-column group g, Horner's rule in
+                // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g)
                 const int half = N / 2;                  // columns per warp half (multiple of 16)
                 const int c0 = ehalf * half;
                 const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-                float2 Sv = erow_ok ? phase_exact(bmin + nc * kNC + c0, vj, inv2) : make_float2(0.f, 0.f);
-                const float2 v1 = phase_exact(1, vj, inv2);
+                const float2 v1 = phase_any(1, vj, a.log2n2, inv2);
                 for (int c = 0; c < half; c += 16) {
                     uint32_t re[16], im[16];
                     tmem_ld16(tmem + lane_base + (uint32_t)(c0 + c), re);
                     tmem_ld16(tmem + lane_base + 256u + (uint32_t)(c0 + c), im);
+                    const float2 anchor = erow_ok ? phase_any(bmin + nc * kNC + c0 + c, vj, a.log2n2, inv2)
+                                                  : make_float2(0.f, 0.f);
                     tmem_wait_ld();
-                    float2 e = Sv;
+                    float2 hs = make_float2(__uint_as_float(re[15]), __uint_as_float(im[15]));
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) {
-                        const float qr = __uint_as_float(re[i]), qi = __uint_as_float(im[i]);
-                        Fsum.x += qr * e.x - qi * e.y;
-                        Fsum.y += qr * e.y + qi * e.x;
-                        e = cmulf(e, v1);
+                    for (int i = 14; i >= 0; --i) {
+                        const float2 t = cmulf(hs, v1);
+                        hs = make_float2(t.x + __uint_as_float(re[i]), t.y + __uint_as_float(im[i]));
                     }
-                    Sv = erow_ok ? phase_exact(bmin + nc * kNC + c0 + c + 16, vj, inv2) : Sv;
+                    const float2 contrib = cmulf(hs, anchor);
+                    Fsum.x += contrib.x;
+                    Fsum.y += contrib.y;
                 }
             }
             tc_fence_before();
@@ -440,6 +482,8 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     a.v = d_v;
     a.F = d_F;
     a.D1 = D1; a.D2 = D2; a.n1 = n1; a.n2 = n2;
+    auto lg = [](int n) { int t = 0; while ((1 << t) < n) ++t; return (1 << t) == n ? t : -1; };
+    a.log2n1 = lg(n1); a.log2n2 = lg(n2);
     a.nkc = nkc; a.nnc = nnc; a.npad_last = npad_last;
     a.err = derr.as<int>();
     const size_t smem = 2 * (size_t)kStageBytes + 128 + 128 * sizeof(float2);
