@@ -169,15 +169,14 @@ template <typename T>
 __global__ void k_half_from_centered(const cplx<T> *__restrict__ M, int n1, int n2, int h1, int ld1,
                                      cplx<T> *__restrict__ H)
 {
-    const long long N = (long long)h1 * n2 * n1;
-    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
-        const int q1 = (int)(o % h1);
-        const long long r = o / h1;
-        const int q2 = (int)(r % n2), q3 = (int)(r / n2);
-        const long long a = (long long)((q1 + n1 / 2) % n1) + (long long)n1 * (((q2 + n2 / 2) % n2) + (long long)n2 * ((q3 + n1 / 2) % n1));
-        const int m1 = (n1 - q1) % n1, m2 = (n2 - q2) % n2, m3 = (n1 - q3) % n1;
-        const long long b = (long long)((m1 + n1 / 2) % n1) + (long long)n1 * (((m2 + n2 / 2) % n2) + (long long)n2 * ((m3 + n1 / 2) % n1));
-        const cplx<T> x = M[a], y = M[b];
+    // grid: x over q1, y = q2, z = q3
+    const int q2 = blockIdx.y, q3 = blockIdx.z;
+    const int m2 = (n2 - q2) % n2, m3 = (n1 - q3) % n1;
+    const long long ra = (long long)n1 * (((q2 + n2 / 2) % n2) + (long long)n2 * ((q3 + n1 / 2) % n1));
+    const long long rb = (long long)n1 * (((m2 + n2 / 2) % n2) + (long long)n2 * ((m3 + n1 / 2) % n1));
+    for (int q1 = blockIdx.x * blockDim.x + threadIdx.x; q1 < h1; q1 += gridDim.x * blockDim.x) {
+        const int m1 = (n1 - q1) % n1;
+        const cplx<T> x = M[ra + (q1 + n1 / 2) % n1], y = M[rb + (m1 + n1 / 2) % n1];
         H[q1 + (long long)ld1 * (q2 + (long long)n2 * q3)] = mk((T)0.5 * (x.x + y.x), (T)0.5 * (x.y - y.y));
     }
 }
@@ -229,7 +228,7 @@ static void rec_ifft_t(genfire_ctx *ctx, const cplx<T> *d_M, int n1, int n2, int
     DevBuf H(sizeof(cplx<T>) * (size_t)c.ld1 * n2 * n1, st);
     DevBuf Y(sizeof(cplx<T>) * (size_t)c.ld1 * n2 * D1, st);
     DevBuf Z(sizeof(cplx<T>) * (size_t)c.ld1 * D2 * D1, st);
-    k_half_from_centered<T><<<grid_for(ctx, (long long)c.h1 * n2 * n1, 256), 256, 0, st>>>(d_M, n1, n2, c.h1, c.ld1, H.as<cplx<T>>());
+    k_half_from_centered<T><<<dim3(cdiv(c.h1, 256), n2, n1), 256, 0, st>>>(d_M, n1, n2, c.h1, c.ld1, H.as<cplx<T>>());
     GF_CHECK_LAUNCH();
     // dim 3 inverse: all n1 entries in, the D1 box entries out
     ColPassArgs<T> a = colargs<T>(c.pl3, c.tw3, c.W3, c.h1);
@@ -473,43 +472,41 @@ __global__ void __launch_bounds__(1024) k_scan_cols(const int *__restrict__ coun
 }
 
 // Object in box coordinates from an initial object (D1 x D2 x D1) or zeros.
+// grid: x over e1, y = e2, z = e3
 template <typename T>
 __global__ void k_place(const T *__restrict__ init, int D1, int D2, int B1, int B2, int B3, T *__restrict__ x)
 {
-    const long long N = (long long)B1 * B2 * B3;
     const int o1 = B1 / 2 - D1 / 2, o2 = B2 / 2 - D2 / 2, o3 = B3 / 2 - D1 / 2;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
-        const int e1 = (int)(i % B1);
-        const long long r = i / B1;
-        const int e2 = (int)(r % B2), e3 = (int)(r / B2);
-        const int a = e1 - o1, b = e2 - o2, c = e3 - o3;
-        T v = 0;
-        if (init && a >= 0 && a < D1 && b >= 0 && b < D2 && c >= 0 && c < D1) v = init[a + (long long)D1 * (b + (long long)D2 * c)];
-        x[i] = v;
+    const int e2 = blockIdx.y, e3 = blockIdx.z;
+    const int b = e2 - o2, c = e3 - o3;
+    const bool in23 = init && b >= 0 && b < D2 && c >= 0 && c < D1;
+    T *row = x + (long long)B1 * (e2 + (long long)B2 * e3);
+    for (int e1 = blockIdx.x * blockDim.x + threadIdx.x; e1 < B1; e1 += gridDim.x * blockDim.x) {
+        const int a = e1 - o1;
+        row[e1] = (in23 && a >= 0 && a < D1) ? init[a + (long long)D1 * (b + (long long)D2 * c)] : (T)0;
     }
 }
 
 // reconstruction = My_stripzero(fftshift(best), [D1 D2 D1]) with the best
 // object taken after positivity and support (reconstruct.m:126-131, 152, 192)
+// grid: x over a (dim 1), y = b, z = c
 template <typename T>
-__global__ void k_extract(const T *const *__restrict__ xs, const Ctl *__restrict__ c, const uint8_t *__restrict__ S,
+__global__ void k_extract(const T *const *__restrict__ xs, const Ctl *__restrict__ ctl, const uint8_t *__restrict__ S,
                           int positivity, int D1, int D2, int B1, int B2, int B3, T *__restrict__ out)
 {
-    const long long N = (long long)D1 * D2 * D1;
     const int o1 = B1 / 2 - D1 / 2, o2 = B2 / 2 - D2 / 2, o3 = B3 / 2 - D1 / 2;
-    const int sel = c->xbest;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const int sel = ctl->xbest;
+    const int b = blockIdx.y, c = blockIdx.z;
+    const long long rin = (long long)B1 * ((b + o2) + (long long)B2 * (c + o3)) + o1;
+    T *orow = out + (long long)D1 * (b + (long long)D2 * c);
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < D1; a += gridDim.x * blockDim.x) {
         T v = 0;
         if (sel >= 0) {
-            const int a = (int)(i % D1);
-            const long long r = i / D1;
-            const int b = (int)(r % D2), cc = (int)(r / D2);
-            const long long bi = (a + o1) + (long long)B1 * ((b + o2) + (long long)B2 * (cc + o3));
-            v = xs[sel][bi];
+            v = xs[sel][rin + a];
             if (positivity && v < (T)0) v = 0;
-            if (S) v = v * (T)S[bi];
+            if (S) v = v * (T)S[rin + a];
         }
-        out[i] = v;
+        orow[a] = v;
     }
 }
 
@@ -627,7 +624,7 @@ template <typename T> struct ReconT : ReconBase {
                     dinit = init.as<T>();
                 }
             }
-            k_place<T><<<grid_for(ctx, NB, 256), 256, 0, st>>>(dinit, D1, D2, B1, B2, B3, xbuf[0].as<T>());
+            k_place<T><<<dim3(cdiv(B1, 256), B2, B3), 256, 0, st>>>(dinit, D1, D2, B1, B2, B3, xbuf[0].as<T>());
             GF_CHECK_LAUNCH();
             GF_CUDA(cudaStreamSynchronize(st));
         }
@@ -844,7 +841,7 @@ template <typename T> struct ReconT : ReconBase {
         if (on_device) dout = static_cast<T *>(rec);
         else { out.alloc(sizeof(T) * nv, st); dout = out.as<T>(); }
         if (rec) {
-            k_extract<T><<<grid_for(ctx, (long long)nv, 256), 256, 0, st>>>(
+            k_extract<T><<<dim3(cdiv(D1, 256), D2, D1), 256, 0, st>>>(
                 xptrs.as<T *>(), ctl.as<Ctl>(), p.constraintSupport ? S.as<uint8_t>() : nullptr,
                 p.constraintPositivity, D1, D2, B1, B2, B3, dout);
             GF_CHECK_LAUNCH();

@@ -474,16 +474,17 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
 
 // Most of the grid is untouched: the exact flag and the weight sum are read
 // first, the complex sums only where one of them is set.
+// Grid: x over dim 1 (c1), y = c2, z = c3, so no index has to be decoded.
+// Most of the grid is untouched: the exact flag and the weight sum are read
+// first, the complex sums only where one of them is set.
 template <typename TO>
 __global__ void k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
                            const double2 *__restrict__ ex, const uint8_t *__restrict__ hx, GridSpec g, int n1,
                            int n2, int centro, cplx<TO> *__restrict__ M)
 {
-    const long long N = (long long)n1 * n2 * n1;
-    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
-        const int c1 = (int)(o % n1);
-        const long long r = o / n1;
-        const int c2 = (int)(r % n2), c3 = (int)(r / n2);
+    const int c2 = blockIdx.y, c3 = blockIdx.z;
+    const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
+    for (int c1 = blockIdx.x * blockDim.x + threadIdx.x; c1 < n1; c1 += gridDim.x * blockDim.x) {
         bool cj;
         const long long li = src_index(g, n1, n2, centro, c1, c2, c3, cj);
         double2 v = make_double2(0.0, 0.0);
@@ -497,21 +498,19 @@ __global__ void k_finalize(const double2 *__restrict__ num, const double *__rest
                 v.y /= ws;
             }
         }
-        M[o] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
+        M[row + c1] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
     }
 }
 
 __global__ void k_centro(const double2 *__restrict__ FS, GridSpec g, int n1, int n2, double2 *__restrict__ M)
 {
-    const long long N = (long long)n1 * n2 * n1;
-    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < N; o += (long long)gridDim.x * blockDim.x) {
-        const int c1 = (int)(o % n1);
-        const long long r = o / n1;
-        const int c2 = (int)(r % n2), c3 = (int)(r / n2);
+    const int c2 = blockIdx.y, c3 = blockIdx.z;
+    const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
+    for (int c1 = blockIdx.x * blockDim.x + threadIdx.x; c1 < n1; c1 += gridDim.x * blockDim.x) {
         bool cj;
         const long long li = src_index(g, n1, n2, 1, c1, c2, c3, cj);
         const double2 v = FS[li];
-        M[o] = make_double2(v.x, cj ? -v.y : v.y);
+        M[row + c1] = make_double2(v.x, cj ? -v.y : v.y);
     }
 }
 
@@ -685,10 +684,10 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
             num.as<double2>(), wsum.as<double>(), ex.as<double2>(), hx.as<uint8_t>());
         GF_CHECK_LAUNCH();
     }
-    const long long N = (long long)n1 * n2 * n1;
-    k_finalize<T><<<grid_for(ctx, N, 256), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(), ex.as<double2>(),
-                                                         hx.as<uint8_t>(), g, n1, n2, p.DFT_CentroSymmetricity,
-                                                         reinterpret_cast<cplx<T> *>(d_M));
+    k_finalize<T><<<dim3(cdiv(n1, 256), n2, n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
+                                                               ex.as<double2>(), hx.as<uint8_t>(), g, n1, n2,
+                                                               p.DFT_CentroSymmetricity,
+                                                               reinterpret_cast<cplx<T> *>(d_M));
     GF_CHECK_LAUNCH();
     if (d_rec) rec_ifft(ctx, p.precision, d_M, n1, n2, D1, D2, d_rec);
     GF_CUDA(cudaStreamSynchronize(st));
@@ -729,8 +728,7 @@ void centro_device(genfire_ctx *ctx, const double2 *d_FS, int n1, int n_k1, int 
 {
     (void)n_k1;
     const GridSpec g = make_grid(n1, n2, 1);
-    const long long N = (long long)n1 * n2 * n1;
-    k_centro<<<grid_for(ctx, N, 256), 256, 0, ctx->stream>>>(d_FS, g, n1, n2, d_M);
+    k_centro<<<dim3(cdiv(n1, 256), n2, n1), 256, 0, ctx->stream>>>(d_FS, g, n1, n2, d_M);
     GF_CHECK_LAUNCH();
 }
 
