@@ -450,12 +450,16 @@ __global__ void k_accum(const uint32_t *__restrict__ ind, const float *__restric
             ex[li] = make_double2((double)f.x, (double)f.y);
             hx[li] = 1;
         } else {
+            // num is not cleared beforehand: a zero weight sum marks a point
+            // no earlier projection touched (every weight is positive)
             const double wgt = 1.0 / d;
-            double2 a = num[li];
+            const double w0 = wsum[li];
+            double2 a = make_double2(0.0, 0.0);
+            if (w0 != 0.0) a = num[li];
             a.x += (double)f.x * wgt;
             a.y += (double)f.y * wgt;
             num[li] = a;
-            wsum[li] += wgt;
+            wsum[li] = w0 + wgt;
         }
     }
 }
@@ -472,33 +476,46 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
     return (long long)(k1 - g.lo1) + (long long)g.l1 * ((k2 - g.lo2) + (long long)g.l2 * (k3 - g.lo3));
 }
 
-// Most of the grid is untouched: the exact flag and the weight sum are read
-// first, the complex sums only where one of them is set.
-// Grid: x over dim 1 (c1), y = c2, z = c3, so no index has to be decoded.
-// Most of the grid is untouched: the exact flag and the weight sum are read
-// first, the complex sums only where one of them is set.
+// Grid: x over dim 1 (c1), y = c2, z = c3, one point per thread, so no index
+// has to be decoded.  Most of the grid is untouched: each thread reads the
+// exact flag and the weight sum of its point and writes zero if neither is
+// set; the touched points of the CTA are gathered into a shared list and then
+// averaged by consecutive threads, so the FP64 divisions (a slow pipe on this
+// part) run in full warps instead of one lane of many warps.
 template <typename TO>
-__global__ void k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
-                           const double2 *__restrict__ ex, const uint8_t *__restrict__ hx, GridSpec g, int n1,
-                           int n2, int centro, cplx<TO> *__restrict__ M)
+__global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
+                                                  const double2 *__restrict__ ex, const uint8_t *__restrict__ hx,
+                                                  GridSpec g, int n1, int n2, int centro, cplx<TO> *__restrict__ M)
 {
+    __shared__ int list[256];
+    __shared__ int cnt;
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
     const int c2 = blockIdx.y, c3 = blockIdx.z;
     const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
-    for (int c1 = blockIdx.x * blockDim.x + threadIdx.x; c1 < n1; c1 += gridDim.x * blockDim.x) {
+    const int c1 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c1 < n1) {
         bool cj;
         const long long li = src_index(g, n1, n2, centro, c1, c2, c3, cj);
-        double2 v = make_double2(0.0, 0.0);
+        if (hx[li] || wsum[li] > 0) list[atomicAdd(&cnt, 1)] = c1;
+        else M[row + c1] = mk((TO)0, cj ? -(TO)0 : (TO)0);
+    }
+    __syncthreads();
+    const int m = cnt;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int c = list[i];
+        bool cj;
+        const long long li = src_index(g, n1, n2, centro, c, c2, c3, cj);
+        double2 v;
         if (hx[li]) {
             v = ex[li];
         } else {
             const double ws = wsum[li];
-            if (ws > 0) {
-                v = num[li];
-                v.x /= ws;
-                v.y /= ws;
-            }
+            v = num[li];
+            v.x /= ws;
+            v.y /= ws;
         }
-        M[row + c1] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
+        M[row + c] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
     }
 }
 
@@ -674,8 +691,7 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     // weighted average in FP64, projection by projection
     const size_t G = (size_t)g.total;
     DevBuf num(sizeof(double2) * G, st), wsum(sizeof(double) * G, st), ex(sizeof(double2) * G, st), hx(G, st);
-    GF_CUDA(cudaMemsetAsync(num.p, 0, num.bytes, st));
-    GF_CUDA(cudaMemsetAsync(wsum.p, 0, wsum.bytes, st));
+    GF_CUDA(cudaMemsetAsync(wsum.p, 0, wsum.bytes, st));  // num and ex are read only where wsum / hx are set
     GF_CUDA(cudaMemsetAsync(hx.p, 0, hx.bytes, st));
     for (int i = 0; i < P; ++i) {
         if (sel.nk[i] == 0) continue;

@@ -20,9 +20,10 @@
 // * One elected thread issues tcgen05.mma (M = 128, N = 256, K = 16) and
 //   tcgen05.commit; shared-memory stages are double buffered so the next
 //   chunk is generated while the tensor core works on the current one.
-// * The epilogue reads the accumulators with tcgen05.ld (one row per thread,
-//   two warps per 32-lane quadrant) and contracts them with E_v generated the
-//   same way.
+// * 16 warps: each thread generates 8 consecutive k of one row of A per chunk;
+//   the epilogue reads the accumulators with tcgen05.ld (one row per thread,
+//   four warps per 32-lane quadrant, each a quarter of the columns) and
+//   contracts them with E_v, two 16-column groups at a time.
 // Every mbarrier wait is bounded by a clock limit; on expiry the kernel records
 // an error flag, stops issuing work, waits (bounded) for its copies and MMAs,
 // frees its TMEM and returns.
@@ -34,7 +35,7 @@ namespace gf {
 
 namespace umma {
 
-constexpr int kThreads = 256;      // 8 warps
+constexpr int kThreads = 512;      // 16 warps
 constexpr int kM = 128;            // rows per tile
 constexpr int kKC = 32;            // K per chunk (two MMA k-steps of 16)
 constexpr int kNC = 256;           // N per chunk (columns of one accumulator)
@@ -219,7 +220,7 @@ struct MmaArgs {
     int D1, D2, n1, n2;
     int log2n1, log2n2;       // log2 of n1, n2 when powers of two, else -1
     int nkc, nnc;             // K chunks (32 wide), N chunks (256 wide)
-    int npad_last;            // columns of the last N chunk, a multiple of 32
+    int npad_last;            // columns of the last N chunk, a multiple of 64
     int *err;                 // set to 1 when a bounded wait expires
 };
 
@@ -234,7 +235,7 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     uint64_t *bar_done = bar_mma + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_done + 1);
     int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
-    float2 *red = reinterpret_cast<float2 *>(smem_raw + 2 * kStageBytes + 128);  // 128 partial F
+    float2 *red = reinterpret_cast<float2 *>(smem_raw + 2 * kStageBytes + 128);  // 3 x 128 partial F
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
@@ -259,15 +260,15 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     uint32_t w_load[2] = {0, 0}, w_mma[2] = {0, 0}, w_done = 0;  // completions waited per barrier
     const double inv1 = 1.0 / (double)a.n1, inv2 = 1.0 / (double)a.n2;
     const int amin = -(a.D1 / 2), bmin = -(a.D2 / 2);
-    const int r = tid & (kM - 1), h = tid >> 7;  // A generation: row r, half h of the 32-wide chunk
+    const int r = tid & (kM - 1), h = tid >> 7;  // A generation: row r, quarter h of the 32-wide chunk
     bool ok = true;
 
     for (int item = blockIdx.x; item < a.ntiles && ok; item += gridDim.x) {
         const MmaTile tl = a.tiles[item];
         const bool row_ok = r < tl.nj;
         const float uj = row_ok ? a.u[tl.j0 + r] : 0.f;
-        // epilogue row and column half
-        const int erow = (warp & 3) * 32 + lane, ehalf = warp >> 2;
+        // epilogue row and column quarter
+        const int erow = (warp & 3) * 32 + lane, equart = warp >> 2;
         const bool erow_ok = erow < tl.nj;
         const float vj = erow_ok ? a.v[tl.j0 + erow] : 0.f;
         float2 Fsum = make_float2(0.f, 0.f);
@@ -275,8 +276,8 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
         for (int nc = 0; nc < a.nnc && ok; ++nc) {
             const int N = (nc == a.nnc - 1) ? a.npad_last : kNC;
             const uint32_t idesc = idesc_bf16(kM, N);
-            // A anchors for this thread: S = E_u(amin + 16h), rotations by 1 and by 32
-            float2 S = row_ok ? phase_any(amin + 16 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
+            // A anchors for this thread: S = E_u(amin + 8h), rotations by 1 and by 32
+            float2 S = row_ok ? phase_any(amin + 8 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
             const float2 w1 = phase_any(1, uj, a.log2n1, inv1), w32 = phase_any(32, uj, a.log2n1, inv1);
             const __nv_bfloat16 *Bp = a.B + ((size_t)(tl.proj * a.nnc + nc) * a.nkc) * 2 * kBTile;
             for (int kc = 0; kc < a.nkc; ++kc) {
@@ -298,12 +299,12 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                     bulk_g2s(Bs + kBTile, src + kBTile, kBTile * 2, &bar_load[s]);
                 }
                 ++n_load[s];
-                // A: 16 consecutive k for row r: k = 16h .. 16h+15 of this chunk
+                // A: 8 consecutive k for row r: k = 8h .. 8h+7 of this chunk
                 {
                     float2 e = S;
-                    uint32_t rh[8], rl[8], ih[8], il[8];
+                    uint32_t rh[4], rl[4], ih[4], il[4];
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) {
+                    for (int q = 0; q < 4; ++q) {
                         float2 e0 = e;
                         e = cmulf(e, w1);
                         float2 e1 = e;
@@ -318,15 +319,12 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                         il[q] = pack_bf16(e0.y - i0h, e1.y - i1h);
                     }
                     S = cmulf(S, w32);
-                    // two 16-byte core-matrix rows (k = 16h..16h+7 and 16h+8..16h+15) per array
-#pragma unroll
-                    for (int g = 0; g < 2; ++g) {
-                        const int idx = kmaj_index(r, 16 * h + 8 * g);
-                        *reinterpret_cast<uint4 *>(Ah + 0 * kATile + idx) = make_uint4(rh[4 * g], rh[4 * g + 1], rh[4 * g + 2], rh[4 * g + 3]);
-                        *reinterpret_cast<uint4 *>(Ah + 1 * kATile + idx) = make_uint4(rl[4 * g], rl[4 * g + 1], rl[4 * g + 2], rl[4 * g + 3]);
-                        *reinterpret_cast<uint4 *>(Ah + 2 * kATile + idx) = make_uint4(ih[4 * g], ih[4 * g + 1], ih[4 * g + 2], ih[4 * g + 3]);
-                        *reinterpret_cast<uint4 *>(Ah + 3 * kATile + idx) = make_uint4(il[4 * g], il[4 * g + 1], il[4 * g + 2], il[4 * g + 3]);
-                    }
+                    // one 16-byte core-matrix row (k = 8h..8h+7) per array
+                    const int idx = kmaj_index(r, 8 * h);
+                    *reinterpret_cast<uint4 *>(Ah + 0 * kATile + idx) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+                    *reinterpret_cast<uint4 *>(Ah + 1 * kATile + idx) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+                    *reinterpret_cast<uint4 *>(Ah + 2 * kATile + idx) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+                    *reinterpret_cast<uint4 *>(Ah + 3 * kATile + idx) = make_uint4(il[0], il[1], il[2], il[3]);
                 }
                 fence_proxy_async();
                 __syncthreads();
@@ -366,39 +364,58 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
             if (*abort_flag) { ok = false; break; }
             {
                 // F_j += sum_b Q(j,b) E_v(j,b): per 16-column group g, Horner's rule in
-                // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g)
-                const int half = N / 2;                  // columns per warp half (multiple of 16)
-                const int c0 = ehalf * half;
+                // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g);
+                // two groups per step (independent chains, one wait for both loads)
+                const int quarter = N / 4;               // columns per warp quarter (multiple of 16)
+                const int c0 = equart * quarter;
                 const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
                 const float2 v1 = phase_any(1, vj, a.log2n2, inv2);
-                for (int c = 0; c < half; c += 16) {
-                    uint32_t re[16], im[16];
-                    tmem_ld16(tmem + lane_base + (uint32_t)(c0 + c), re);
-                    tmem_ld16(tmem + lane_base + 256u + (uint32_t)(c0 + c), im);
-                    const float2 anchor = erow_ok ? phase_any(bmin + nc * kNC + c0 + c, vj, a.log2n2, inv2)
-                                                  : make_float2(0.f, 0.f);
+                for (int c = 0; c < quarter; c += 32) {
+                    const bool two = c + 16 < quarter;   // warp-uniform
+                    uint32_t re0[16], im0[16], re1[16], im1[16];
+                    const uint32_t col = (uint32_t)(c0 + c);
+                    tmem_ld16(tmem + lane_base + col, re0);
+                    tmem_ld16(tmem + lane_base + 256u + col, im0);
+                    if (two) {
+                        tmem_ld16(tmem + lane_base + col + 16u, re1);
+                        tmem_ld16(tmem + lane_base + 256u + col + 16u, im1);
+                    }
+                    const int b0 = bmin + nc * kNC + c0 + c;
+                    const float2 an0 = erow_ok ? phase_any(b0, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
+                    const float2 an1 = (erow_ok && two) ? phase_any(b0 + 16, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
                     tmem_wait_ld();
-                    float2 hs = make_float2(__uint_as_float(re[15]), __uint_as_float(im[15]));
+                    float2 h0 = make_float2(__uint_as_float(re0[15]), __uint_as_float(im0[15]));
 #pragma unroll
                     for (int i = 14; i >= 0; --i) {
-                        const float2 t = cmulf(hs, v1);
-                        hs = make_float2(t.x + __uint_as_float(re[i]), t.y + __uint_as_float(im[i]));
+                        const float2 t = cmulf(h0, v1);
+                        h0 = make_float2(t.x + __uint_as_float(re0[i]), t.y + __uint_as_float(im0[i]));
                     }
-                    const float2 contrib = cmulf(hs, anchor);
-                    Fsum.x += contrib.x;
-                    Fsum.y += contrib.y;
+                    const float2 p0 = cmulf(h0, an0);
+                    Fsum.x += p0.x;
+                    Fsum.y += p0.y;
+                    if (two) {
+                        float2 h1 = make_float2(__uint_as_float(re1[15]), __uint_as_float(im1[15]));
+#pragma unroll
+                        for (int i = 14; i >= 0; --i) {
+                            const float2 t = cmulf(h1, v1);
+                            h1 = make_float2(t.x + __uint_as_float(re1[i]), t.y + __uint_as_float(im1[i]));
+                        }
+                        const float2 p1 = cmulf(h1, an1);
+                        Fsum.x += p1.x;
+                        Fsum.y += p1.y;
+                    }
                 }
             }
             tc_fence_before();
             __syncthreads();  // TMEM reads finished before the next MMAs overwrite it
         }
         if (!ok) break;
-        // combine the two column halves of each row and store
-        if (ehalf == 1) red[erow] = Fsum;
+        // combine the four column quarters of each row and store
+        if (equart > 0) red[(equart - 1) * kM + erow] = Fsum;
         __syncthreads();
-        if (ehalf == 0 && erow_ok) {
-            const float2 o = red[erow];
-            a.F[tl.j0 + erow] = make_float2(Fsum.x + o.x, Fsum.y + o.y);
+        if (equart == 0 && erow_ok) {
+            const float2 o1 = red[erow], o2 = red[kM + erow], o3 = red[2 * kM + erow];
+            a.F[tl.j0 + erow] = make_float2(((Fsum.x + o1.x) + o2.x) + o3.x, ((Fsum.y + o1.y) + o2.y) + o3.y);
         }
         __syncthreads();
     }
@@ -456,7 +473,7 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     const int nkc = (D1 + kKC - 1) / kKC;
     const int nnc = (D2 + kNC - 1) / kNC;
     const int last = D2 - (nnc - 1) * kNC;
-    const int npad_last = (last + 31) / 32 * 32;
+    const int npad_last = (last + 63) / 64 * 64;  // four epilogue quarters of whole 16-column groups
     const size_t nB = (size_t)P * nnc * nkc * 2 * kBTile;
     DevBuf B(nB * sizeof(__nv_bfloat16), st);
     {
@@ -486,7 +503,7 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     a.log2n1 = lg(n1); a.log2n2 = lg(n2);
     a.nkc = nkc; a.nnc = nnc; a.npad_last = npad_last;
     a.err = derr.as<int>();
-    const size_t smem = 2 * (size_t)kStageBytes + 128 + 128 * sizeof(float2);
+    const size_t smem = 2 * (size_t)kStageBytes + 128 + 3 * kM * sizeof(float2);
     GF_CUDA(cudaFuncSetAttribute((const void *)k_dft_tcgen05, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<size_t>(tiles.size(), (size_t)ctx->sm_count);
     k_dft_tcgen05<<<grid, kThreads, smem, st>>>(a);
