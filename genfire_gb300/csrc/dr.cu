@@ -20,6 +20,7 @@
 #include "fft_reg.cuh"
 #include "internal.h"
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -29,7 +30,9 @@
 namespace gf {
 
 // ===========================================================================
-// twiddle tables, one per (device, n, precision), kept for the process
+// twiddle tables, one per (device, n, precision), kept for the process: the
+// n entries exp(-2 pi i t / n), then (power-of-two n) the packed per-stage
+// table of the register-resident passes (P2Plan::twoff), copied from them
 // ===========================================================================
 template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
 {
@@ -41,15 +44,32 @@ template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
     auto key = std::make_tuple(dev, n, (int)sizeof(T));
     auto it = cache.find(key);
     if (it != cache.end()) return static_cast<const cplx<T> *>(it->second);
-    std::vector<cplx<T>> h(n);
+    const int np = packed_twiddle_count(n);
+    std::vector<cplx<T>> h((size_t)n + np);
     const double pi = 3.14159265358979323846;
     for (int t = 0; t < n; ++t) {
         double a = -2.0 * pi * (double)t / (double)n;
         h[t] = mk((T)std::cos(a), (T)std::sin(a));
     }
+    if (np) {
+        int L = 0;
+        while ((1 << L) < n) ++L;
+        const int n8 = L / 3, rem = L % 3, nst = n8 + (rem ? 1 : 0);
+        size_t o = (size_t)n;
+        for (int st = 0, ns = 1; st < nst; ns *= (st < n8 ? 8 : (rem == 2 ? 4 : 2)), ++st) {
+            const int R = st < n8 ? 8 : (rem == 2 ? 4 : 2);
+            if (ns == 1) continue;
+            const int step = n / (ns * R);
+            for (int kk = 0; kk < ns; ++kk) {
+                for (int r = 1; r < R; ++r) h[o++] = h[(size_t)kk * r * step];
+                h[o++] = mk((T)1, (T)0);  // pad
+            }
+        }
+        if (o != h.size()) fail(GENFIRE_ERR_STATE, "internal: packed twiddle table size.");
+    }
     void *d = nullptr;
-    GF_CUDA(cudaMalloc(&d, sizeof(cplx<T>) * n));
-    GF_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(cplx<T>) * n, cudaMemcpyHostToDevice, s));
+    GF_CUDA(cudaMalloc(&d, sizeof(cplx<T>) * h.size()));
+    GF_CUDA(cudaMemcpyAsync(d, h.data(), sizeof(cplx<T>) * h.size(), cudaMemcpyHostToDevice, s));
     GF_CUDA(cudaStreamSynchronize(s));
     cache[key] = d;
     return static_cast<const cplx<T> *>(d);
@@ -70,9 +90,23 @@ static FftPlan plan_or_fail(int n)
 template <typename T, int N> static void set_reg_attrs()
 {
     const int sm = (int)reg_smem<T, N>();
-    GF_CUDA(cudaFuncSetAttribute((const void *)k_col_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    GF_CUDA(cudaFuncSetAttribute((const void *)k_col_reg<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    if constexpr (sizeof(T) == 4)
+        GF_CUDA(cudaFuncSetAttribute((const void *)k_col_reg<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     GF_CUDA(cudaFuncSetAttribute((const void *)k_row_r2c_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     GF_CUDA(cudaFuncSetAttribute((const void *)k_row_c2r_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+}
+
+// Two float columns per thread need unit column stride and 16-byte aligned
+// column pairs (even strides, aligned bases; tiles start at even columns).
+// They pay off in the fused forward + constraint + inverse pass (two
+// transforms per load); the single-transform passes keep one column per
+// thread and twice the resident warps.
+template <typename T> static bool pair_ok(const ColPassArgs<T> &a)
+{
+    auto al = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
+    return sizeof(T) == 4 && (a.mode & 3) == 3 && a.col_stride == 1 && al(a.in) && al(a.out) &&
+           a.in_dim % 2 == 0 && a.in_other % 2 == 0 && a.out_dim % 2 == 0 && a.out_other % 2 == 0;
 }
 
 // Register-resident passes for power-of-two lengths 64..1024.
@@ -81,7 +115,13 @@ template <typename T, int N> static void col_reg(const ColPassArgs<T> &a, int ot
     constexpr int W = reg_width<T>(N);
     if (a.W != W) fail(GENFIRE_ERR_STATE, "internal: column tile width mismatch.");
     dim3 grid(cdiv(a.ncols, W), other);
-    k_col_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
+    if constexpr (sizeof(T) == 4) {
+        if (pair_ok(a)) {
+            k_col_reg<T, N, 2><<<grid, col_threads<T, N, 2>(), reg_smem<T, N>(), st>>>(a);
+            return;
+        }
+    }
+    k_col_reg<T, N, 1><<<grid, col_threads<T, N, 1>(), reg_smem<T, N>(), st>>>(a);
 }
 template <typename T, int N> static void rows_reg(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
 {
@@ -93,6 +133,9 @@ template <typename T, int N> static void rows_reg(const RowPassArgs<T> &a, bool 
 }
 template <typename T> static bool try_col_reg(const ColPassArgs<T> &a, int other, cudaStream_t st)
 {
+    // element offsets along the transform are 32-bit in the register passes
+    const long long span = (long long)(a.pl.n - 1) * std::max(a.in_dim, a.out_dim) + 1;
+    if (span >= (1LL << 32)) return false;
     switch (a.pl.n) {
     case 64: col_reg<T, 64>(a, other, st); return true;
     case 128: col_reg<T, 128>(a, other, st); return true;

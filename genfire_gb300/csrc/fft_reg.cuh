@@ -23,6 +23,17 @@ template <int N> struct P2Plan {
     static constexpr int NST = N8 + (REM ? 1 : 0);
     static constexpr int radix(int s) { return s < N8 ? 8 : (REM == 2 ? 4 : 2); }
     static constexpr int ns(int s) { return s == 0 ? 1 : ns(s - 1) * radix(s - 1); }
+    // Packed twiddle table (stored right after the n-entry table tw[t] =
+    // exp(-2 pi i t / n)): for every stage s with ns(s) > 1 and every kk < ns(s),
+    // R = radix(s) entries tw[kk * r * n / (ns(s) * R)] for r = 1 .. R-1 and one
+    // pad, so a butterfly's twiddles are R/2 aligned 16-byte loads (float) from
+    // one base address.  twoff(s) is the offset of stage s.
+    static constexpr int twoff(int s)
+    {
+        int o = 0;
+        for (int t = 0; t < s; ++t) o += ns(t) > 1 ? ns(t) * radix(t) : 0;
+        return o;
+    }
 };
 
 // shared-memory layouts with one padding row every 8 rows (bank spreading).
@@ -42,27 +53,53 @@ template <int N, int W> struct RowLayout {   // each column contiguous
     static constexpr int stride(int S) { return S % 8 == 0 ? S + S / 8 : S; }
 };
 
-template <typename T, int N, int S>
-__device__ __forceinline__ void reg_stage(cplx<T> (&v)[8], int j, const cplx<T> *__restrict__ tw, bool inv)
+// w[1 .. R-1] of one butterfly from the packed table
+template <typename T, int R>
+__device__ __forceinline__ void load_tw(const cplx<T> *__restrict__ p, cplx<T> (&w)[R])
+{
+    if constexpr (sizeof(T) == 4) {
+        const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) {
+            const float4 t = __ldg(q + i);
+            w[2 * i + 1] = mk(t.x, t.y);
+            if (2 * i + 2 < R) w[2 * i + 2] = mk(t.z, t.w);
+        }
+    } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) w[r] = __ldg(p + r - 1);
+    }
+}
+
+// One stage on the NC columns a thread holds: register k of column c holds
+// x[j + k*N/8] of the stage's input.  The twiddles are loaded once and applied
+// to every column.
+template <typename T, int N, int S, bool INV, int NC>
+__device__ __forceinline__ void reg_stage(cplx<T> (&v)[NC][8], int j, const cplx<T> *__restrict__ twp)
 {
     constexpr int R = P2Plan<N>::radix(S);
     constexpr int NS = P2Plan<N>::ns(S);
     constexpr int NB = 8 / R;
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-        const int jp = j + b * (N / 8);
-        cplx<T> u[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) u[r] = v[b + r * NB];
-        if (NS > 1) {
-            const int kk = jp & (NS - 1);
-            constexpr int step = N / (NS * R);
-#pragma unroll
-            for (int r = 1; r < R; ++r) u[r] = ctw(u[r], __ldg(&tw[kk * r * step]), inv);
+        cplx<T> w[R];
+        if constexpr (NS > 1) {
+            const int kk = (j + b * (N / 8)) & (NS - 1);
+            load_tw<T, R>(twp + P2Plan<N>::twoff(S) + kk * R, w);
         }
-        Dft<R, T>::run(u, inv, tw, N);
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[b + r * NB] = u[r];
+        for (int c = 0; c < NC; ++c) {
+            cplx<T> u[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) u[r] = v[c][b + r * NB];
+            if constexpr (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) u[r] = ctw(u[r], w[r], INV);
+            }
+            Dft<R, T>::run(u, INV, nullptr, N);
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[c][b + r * NB] = u[r];
+        }
     }
 }
 
@@ -93,8 +130,31 @@ template <int N, class Lay, int S> __device__ __forceinline__ int out_base(int j
     return Lay::idx((jp - kk) * R + kk, c);
 }
 
-template <typename T, int N, class Lay, int S>
-__device__ __forceinline__ void store_stage(cplx<T> *s, const cplx<T> (&v)[8], int j, int c)
+// register k of the NC adjacent columns at q[0 .. NC-1] (one 16-byte access
+// for two float columns; ColLayout keeps adjacent columns adjacent)
+template <typename T, int NC> __device__ __forceinline__ void st_cols(cplx<T> *q, const cplx<T> (&v)[NC][8], int k)
+{
+    if constexpr (NC == 2 && sizeof(T) == 4) {
+        *reinterpret_cast<float4 *>(q) = make_float4(v[0][k].x, v[0][k].y, v[1][k].x, v[1][k].y);
+    } else {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) q[c] = v[c][k];
+    }
+}
+template <typename T, int NC> __device__ __forceinline__ void ld_cols(const cplx<T> *q, cplx<T> (&v)[NC][8], int k)
+{
+    if constexpr (NC == 2 && sizeof(T) == 4) {
+        const float4 t = *reinterpret_cast<const float4 *>(q);
+        v[0][k] = mk(t.x, t.y);
+        v[1][k] = mk(t.z, t.w);
+    } else {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) v[c][k] = q[c];
+    }
+}
+
+template <typename T, int N, class Lay, int S, int NC>
+__device__ __forceinline__ void store_stage(cplx<T> *s, const cplx<T> (&v)[NC][8], int j, int c)
 {
     constexpr int R = P2Plan<N>::radix(S);
     constexpr int NB = 8 / R;
@@ -103,31 +163,31 @@ __device__ __forceinline__ void store_stage(cplx<T> *s, const cplx<T> (&v)[8], i
     for (int b = 0; b < NB; ++b) {
         cplx<T> *q = s + out_base<N, Lay, S>(j, c, b);
 #pragma unroll
-        for (int r = 0; r < R; ++r) q[r * ST] = v[b + r * NB];
+        for (int r = 0; r < R; ++r) st_cols<T, NC>(q + r * ST, v, b + r * NB);
     }
 }
 
 // next stage's inputs: register k holds x[j + k*N/8]
-template <typename T, int N, class Lay>
-__device__ __forceinline__ void load_stage(const cplx<T> *s, cplx<T> (&v)[8], int in_base)
+template <typename T, int N, class Lay, int NC>
+__device__ __forceinline__ void load_stage(const cplx<T> *s, cplx<T> (&v)[NC][8], int in_base)
 {
     constexpr int ST = Lay::stride(N / 8);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = s[in_base + k * ST];
+    for (int k = 0; k < 8; ++k) ld_cols<T, NC>(s + in_base + k * ST, v, k);
 }
 
-template <typename T, int N, class Lay, int S = 0>
-__device__ __forceinline__ void reg_fft(cplx<T> (&v)[8], cplx<T> *sA, cplx<T> *sB, int &buf, int j, int c,
-                                        int in_base, const cplx<T> *__restrict__ tw, bool inv)
+template <typename T, int N, class Lay, bool INV, int NC, int S = 0>
+__device__ __forceinline__ void reg_fft(cplx<T> (&v)[NC][8], cplx<T> *sA, cplx<T> *sB, int &buf, int j, int c,
+                                        int in_base, const cplx<T> *__restrict__ twp)
 {
-    reg_stage<T, N, S>(v, j, tw, inv);
+    reg_stage<T, N, S, INV, NC>(v, j, twp);
     if constexpr (S + 1 < P2Plan<N>::NST) {
         cplx<T> *s = buf ? sB : sA;
         buf ^= 1;
-        store_stage<T, N, Lay, S>(s, v, j, c);
+        store_stage<T, N, Lay, S, NC>(s, v, j, c);
         __syncthreads();
-        load_stage<T, N, Lay>(s, v, in_base);
-        reg_fft<T, N, Lay, S + 1>(v, sA, sB, buf, j, c, in_base, tw, inv);
+        load_stage<T, N, Lay, NC>(s, v, in_base);
+        reg_fft<T, N, Lay, INV, NC, S + 1>(v, sA, sB, buf, j, c, in_base, twp);
     }
 }
 
@@ -186,23 +246,65 @@ template <typename T> constexpr int reg_width(int n)
     return sizeof(T) == 4 ? (n * 8 > 4096 ? 4096 / n : 8) : (n * 4 > 2048 ? 2048 / n : 4);
 }
 
-// Column pass (same contract as k_colpass) for N a power of two.
-template <typename T, int N>
-__global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_col_reg(ColPassArgs<T> a)
+// Columns per thread of the column pass: two adjacent float columns (16-byte
+// global and shared-memory accesses, twiddles and index arithmetic shared by
+// both) when the host has checked unit column stride and 16-byte alignment.
+template <typename T, int N, int NC> constexpr int col_threads() { return N / 8 * reg_width<T>(N) / NC; }
+
+// global element access for the NC columns of a thread: nv of them exist
+template <typename T, int NC>
+__device__ __forceinline__ void ld_global(const cplx<T> *p, cplx<T> (&v)[NC][8], int k, int nv)
+{
+    const cplx<T> zero = mk((T)0, (T)0);
+    if constexpr (NC == 2 && sizeof(T) == 4) {
+        if (nv == 2) {
+            const float4 t = *reinterpret_cast<const float4 *>(p);
+            v[0][k] = mk(t.x, t.y);
+            v[1][k] = mk(t.z, t.w);
+        } else {
+            v[0][k] = nv == 1 ? p[0] : zero;
+            v[1][k] = zero;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) v[c][k] = c < nv ? p[c] : zero;
+    }
+}
+template <typename T, int NC>
+__device__ __forceinline__ void st_global(cplx<T> *p, const cplx<T> (&v)[NC][8], int k, int nv, T scale)
+{
+    if constexpr (NC == 2 && sizeof(T) == 4) {
+        if (nv == 2)
+            *reinterpret_cast<float4 *>(p) =
+                make_float4(v[0][k].x * scale, v[0][k].y * scale, v[1][k].x * scale, v[1][k].y * scale);
+        else if (nv == 1)
+            p[0] = mk(v[0][k].x * scale, v[0][k].y * scale);
+    } else {
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+            if (c < nv) p[c] = mk(v[c][k].x * scale, v[c][k].y * scale);
+    }
+}
+
+// Column pass (same contract as k_colpass) for N a power of two; each thread
+// holds NC adjacent columns (NC = 2 requires col_stride 1).
+template <typename T, int N, int NC>
+__global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_col_reg(ColPassArgs<T> a)
 {
     constexpr int W = reg_width<T>(N);
+    constexpr int WT = W / NC;  // threads across the tile's columns
     using Lay = ColLayout<N, W>;
     constexpr int NST = P2Plan<N>::NST;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *sB = sA + Lay::SIZE;
-    const int c = threadIdx.x % W, j = threadIdx.x / W;
+    const cplx<T> *twp = a.tw + N;
+    const int c = (threadIdx.x % WT) * NC, j = threadIdx.x / WT;
     const int tile = blockIdx.x, other = blockIdx.y;
     const int col = tile * W + c;
-    const bool valid = col < a.ncols;
-    const cplx<T> zero = mk((T)0, (T)0);
+    const int nv = min(max(a.ncols - col, 0), NC);  // columns of this thread that exist
     const int in_base = Lay::idx(j, c);
-    cplx<T> v[8];
+    cplx<T> v[NC][8];
     {
         const cplx<T> *in = a.in + (long long)other * a.in_other + (long long)col * a.col_stride;
         const unsigned idim = (unsigned)a.in_dim;
@@ -210,27 +312,27 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_c
         if (e >= N) e -= N;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            v[k] = (valid && e < a.in_cnt) ? in[(unsigned)e * idim] : zero;
+            ld_global<T, NC>(in + (unsigned)e * idim, v, k, e < a.in_cnt ? nv : 0);
             e += N / 8;
             if (e >= N) e -= N;
         }
     }
     int buf = 0;
     float err = 0.f;
-    if (a.mode & 1) reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, false);
+    if (a.mode & 1) reg_fft<T, N, Lay, false, NC>(v, sA, sB, buf, j, c, in_base, twp);
     if (a.mode & 2) {
         if (a.mode & 1) {
             cplx<T> *s = buf ? sB : sA;
             buf ^= 1;
-            store_stage<T, N, Lay, NST - 1>(s, v, j, c);
+            store_stage<T, N, Lay, NST - 1, NC>(s, v, j, c);
             __syncthreads();
             if (a.mode & 4) {
                 err = apply_table<T, Lay>(s, a, tile, W, other);
                 __syncthreads();
             }
-            load_stage<T, N, Lay>(s, v, in_base);
+            load_stage<T, N, Lay, NC>(s, v, in_base);
         }
-        reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, true);
+        reg_fft<T, N, Lay, true, NC>(v, sA, sB, buf, j, c, in_base, twp);
     }
     cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
     const unsigned odim = (unsigned)a.out_dim;
@@ -246,10 +348,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_c
             if (e >= N) e -= N;
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-                if (valid && e < a.out_cnt) {
-                    const cplx<T> x = v[b + r * NB];
-                    out[(unsigned)e * odim] = mk(x.x * a.scale, x.y * a.scale);
-                }
+                if (e < a.out_cnt) st_global<T, NC>(out + (unsigned)e * odim, v, b + r * NB, nv, a.scale);
                 e += NS;
                 if (e >= N) e -= N;
             }
@@ -271,7 +370,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
-    cplx<T> v[8];
+    cplx<T> v[1][8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         int e = j + k * TPC + a.c1;
@@ -291,24 +390,25 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
                 if (a.support) vb = vb * (T)a.support[o];
             }
         }
-        v[k] = mk(va, vb);
+        v[0][k] = mk(va, vb);
     }
     int buf = 0;
     const int in_base = Lay::idx(j, c);
-    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, false);
+    reg_fft<T, N, Lay, false, 1>(v, sA, sB, buf, j, c, in_base, a.tw + N);
     cplx<T> *s = buf ? sB : sA;
-    store_stage<T, N, Lay, P2Plan<N>::NST - 1>(s, v, j, c);
+    store_stage<T, N, Lay, P2Plan<N>::NST - 1, 1>(s, v, j, c);
     __syncthreads();
-    const int rbase = blockIdx.x * W * 2;
-    for (int idx = threadIdx.x; idx < W * a.h1; idx += blockDim.x) {
-        const int cc = idx / a.h1, q = idx - cc * a.h1;
-        const int q0 = rbase + 2 * cc, q1 = q0 + 1;
-        const cplx<T> Z = s[Lay::idx(q, cc)];
-        const cplx<T> Zm = s[Lay::idx(q == 0 ? 0 : N - q, cc)];
-        const cplx<T> Xa = mk((T)0.5 * (Z.x + Zm.x), (T)0.5 * (Z.y - Zm.y));
-        const cplx<T> Xb = mk((T)0.5 * (Z.y + Zm.y), (T)0.5 * (Zm.x - Z.x));
-        if (q0 < a.nrows) a.Y[(long long)q0 * a.ld1 + q] = Xa;
-        if (q1 < a.nrows) a.Y[(long long)q1 * a.ld1 + q] = Xb;
+    // split the pair's spectrum: each thread takes q = j, j + N/8, ... of its own pair
+    {
+        cplx<T> *ya = a.Y + (long long)r0 * a.ld1, *yb = ya + a.ld1;
+        for (int q = j; q < a.h1; q += TPC) {
+            const cplx<T> Z = s[Lay::idx(q, c)];
+            const cplx<T> Zm = s[Lay::idx(q == 0 ? 0 : N - q, c)];
+            const cplx<T> Xa = mk((T)0.5 * (Z.x + Zm.x), (T)0.5 * (Z.y - Zm.y));
+            const cplx<T> Xb = mk((T)0.5 * (Z.y + Zm.y), (T)0.5 * (Zm.x - Z.x));
+            if (r0 < a.nrows) ya[q] = Xa;
+            if (r1 < a.nrows) yb[q] = Xb;
+        }
     }
 }
 
@@ -323,31 +423,32 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     cplx<T> *sB = sA + Lay::SIZE;
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
     T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
-    const int rbase = blockIdx.x * W * 2;
-    for (int idx = threadIdx.x; idx < W * a.h1; idx += blockDim.x) {
-        const int cc = idx / a.h1, q = idx - cc * a.h1;
-        const int q0 = rbase + 2 * cc, q1 = q0 + 1;
-        cplx<T> ha = mk((T)0, (T)0), hb = ha;
-        if (q0 < a.nrows) ha = a.Y[(long long)q0 * a.ld1 + q];
-        if (q1 < a.nrows) hb = a.Y[(long long)q1 * a.ld1 + q];
-        if (q == 0 || 2 * q == N) { ha.y = 0; hb.y = 0; }
-        sA[Lay::idx(q, cc)] = mk(ha.x - hb.y, ha.y + hb.x);
-        if (q != 0 && N - q >= a.h1) sA[Lay::idx(N - q, cc)] = mk(ha.x + hb.y, hb.x - ha.y);
+    const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
+    // pack the two half spectra of the pair: each thread takes q = j, j + N/8, ...
+    {
+        const cplx<T> *ya = a.Y + (long long)r0 * a.ld1, *yb = ya + a.ld1;
+        for (int q = j; q < a.h1; q += TPC) {
+            cplx<T> ha = mk((T)0, (T)0), hb = ha;
+            if (r0 < a.nrows) ha = ya[q];
+            if (r1 < a.nrows) hb = yb[q];
+            if (q == 0 || 2 * q == N) { ha.y = 0; hb.y = 0; }
+            sA[Lay::idx(q, c)] = mk(ha.x - hb.y, ha.y + hb.x);
+            if (q != 0 && N - q >= a.h1) sA[Lay::idx(N - q, c)] = mk(ha.x + hb.y, hb.x - ha.y);
+        }
     }
     __syncthreads();
-    cplx<T> v[8];
+    cplx<T> v[1][8];
     const int in_base = Lay::idx(j, c);
-    load_stage<T, N, Lay>(sA, v, in_base);
+    load_stage<T, N, Lay, 1>(sA, v, in_base);
     int buf = 1;
-    reg_fft<T, N, Lay>(v, sA, sB, buf, j, c, in_base, a.tw, true);
-    const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
+    reg_fft<T, N, Lay, true, 1>(v, sA, sB, buf, j, c, in_base, a.tw + N);
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         int e = reg_final_index<N>(j, k) + a.c1;
         if (e >= N) e -= N;
         if (e < a.B1) {
-            if (r0 < a.nrows) x[(long long)r0 * a.B1 + e] = v[k].x * a.scale;
-            if (r1 < a.nrows) x[(long long)r1 * a.B1 + e] = v[k].y * a.scale;
+            if (r0 < a.nrows) x[(long long)r0 * a.B1 + e] = v[0][k].x * a.scale;
+            if (r1 < a.nrows) x[(long long)r1 * a.B1 + e] = v[0][k].y * a.scale;
         }
     }
 }
@@ -355,6 +456,24 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
 template <typename T, int N> constexpr size_t reg_smem()
 {
     return 2 * (size_t)ColLayout<N, reg_width<T>(N)>::SIZE * sizeof(cplx<T>);
+}
+
+// Size of the packed table appended to the n-entry twiddle table (0 when n
+// is not a power of two of at least 8); the host fills it in the order of
+// P2Plan::twoff.
+inline int packed_twiddle_count(int n)
+{
+    if (n < 8 || (n & (n - 1))) return 0;
+    int L = 0;
+    while ((1 << L) < n) ++L;
+    const int n8 = L / 3, rem = L % 3, nst = n8 + (rem ? 1 : 0);
+    int o = 0, ns = 1;
+    for (int s = 0; s < nst; ++s) {
+        const int R = s < n8 ? 8 : (rem == 2 ? 4 : 2);
+        if (ns > 1) o += ns * R;
+        ns *= R;
+    }
+    return o;
 }
 
 }  // namespace gf
