@@ -28,7 +28,7 @@ PREC_MIXED = 1
 EXPORTS = [
     "genfire_abi_version", "genfire_status_string", "genfire_params_init", "genfire_grid_size",
     "genfire_create", "genfire_destroy", "genfire_last_error", "genfire_stream",
-    "genfire_grid_dft", "genfire_grid_dft_device",
+    "genfire_grid_dft", "genfire_grid_dft_device", "genfire_grid_fft", "genfire_grid_fft_device",
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
     "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc",
@@ -55,7 +55,8 @@ class Params(C.Structure):
         ("numIterations", C.c_int32), ("constraintEnforcementMode", C.c_int32),
         ("constraintPositivity", C.c_int32), ("constraintSupport", C.c_int32),
         ("monitor_R", C.c_int32), ("monitorR_loopLength", C.c_int32),
-        ("precision", C.c_int32), ("reserved", C.c_int32 * 9),
+        ("precision", C.c_int32), ("griddingMethod", C.c_int32), ("allowMultipleGridMatches", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 
@@ -84,6 +85,8 @@ def load():
         "genfire_stream": (C.c_void_p, [vp]),
         "genfire_grid_dft": (C.c_int, [vp, pp, dp, dp, vp, vp, i64p]),
         "genfire_grid_dft_device": (C.c_int, [vp, pp, vp, dp, vp, vp, i64p]),
+        "genfire_grid_fft": (C.c_int, [vp, pp, dp, dp, vp, vp, i64p]),
+        "genfire_grid_fft_device": (C.c_int, [vp, pp, vp, dp, vp, vp, i64p]),
         "genfire_reconstruct": (C.c_int, [vp, pp, vp, up, up, vp, dp, dp, vp, dp, dp, dp, dp]),
         "genfire_recon_create": (C.c_int, [vp, pp, vp, vp, vp, vp, vp, vp, C.c_int32, C.POINTER(C.c_void_p)]),
         "genfire_recon_iterate": (C.c_int, [vp, C.c_int32]),
@@ -181,7 +184,7 @@ class Context:
         prec = p.precision
         cdt = np.complex128 if prec == PREC_FP64 else np.complex64
         rdt = np.float64 if prec == PREC_FP64 else np.float32
-        n1, n2 = grid_size(p)
+        n1, n2 = grid_size(p, method=2)
         P = fortran(projections, np.float64)
         A = fortran(angles, np.float64)
         M = np.zeros((n1, n2, n1), dtype=cdt, order="F")
@@ -200,8 +203,32 @@ class Context:
                                                   ptr(nk, C.c_int64)))
         return nk
 
+    def grid_fft(self, p, projections, angles, want_rec=True):
+        """fillInFourierGrid (griddingMethod 1): (measuredK m^3, recIFFT or None, gridded pairs)."""
+        L = load()
+        prec = p.precision
+        cdt = np.complex128 if prec == PREC_FP64 else np.complex64
+        rdt = np.float64 if prec == PREC_FP64 else np.float32
+        m, _ = grid_size(p, method=1)
+        P = fortran(projections, np.float64)
+        A = fortran(angles, np.float64)
+        M = np.zeros((m, m, m), dtype=cdt, order="F")
+        rec = np.zeros((p.Dim1, p.Dim2, p.Dim1), dtype=rdt, order="F") if want_rec else None
+        n = C.c_int64()
+        self.check(L.genfire_grid_fft(self._h, C.byref(p), ptr(P, C.c_double), ptr(A, C.c_double), ptr(M),
+                                      ptr(rec), C.byref(n)))
+        return M, rec, n.value
+
+    def grid_fft_device(self, p, d_proj_ptr, angles, d_M_ptr, d_rec_ptr=None):
+        A = fortran(angles, np.float64)
+        n = C.c_int64()
+        self.check(load().genfire_grid_fft_device(self._h, C.byref(p), C.c_void_p(d_proj_ptr), ptr(A, C.c_double),
+                                                  C.c_void_p(d_M_ptr),
+                                                  C.c_void_p(d_rec_ptr) if d_rec_ptr else None, C.byref(n)))
+        return n.value
+
     def select(self, p, phi, theta, psi):
-        n1, n2 = grid_size(p)
+        n1, n2 = grid_size(p, method=2)
         if p.DFT_CentroSymmetricity:
             cap = (n1 // 2 + 1) * (2 * (n2 // 2) + 1) * (2 * (n1 // 2) + 1)
         else:
@@ -387,10 +414,19 @@ class Recon:
             pass
 
 
-def grid_size(p):
+def grid_size(p, method=None):
+    """(n1, n2) of measuredK for p's griddingMethod, or for `method` (1 FFT, 2 DFT) if given."""
+    q = p
+    if method is not None:
+        q = Params()
+        C.pointer(q)[0] = p
+        q.griddingMethod = method
     n1 = C.c_int32()
     n2 = C.c_int32()
-    load().genfire_grid_size(C.byref(p), C.byref(n1), C.byref(n2))
+    st = load().genfire_grid_size(C.byref(q), C.byref(n1), C.byref(n2))
+    if st != GENFIRE_OK:
+        raise GenfireError(st, "GENFIRE: FFT gridding: Dim2 * oversamplingRatio (1 + (Dim2-1) * "
+                               "oversamplingRatio for odd Dim2) must be an integer.")
     return n1.value, n2.value
 
 

@@ -82,12 +82,20 @@ genfire_status genfire_params_init(genfire_params *p)
     p->monitor_R = 0;
     p->monitorR_loopLength = 10;
     p->precision = GENFIRE_PREC_FP64;
+    p->griddingMethod = 2;            // the C entry points name their method; sizes default to DFT
+    p->allowMultipleGridMatches = 1;  // GENFIRE_Reconstructor.m:46
     return GENFIRE_OK;
 }
 
 genfire_status genfire_grid_size(const genfire_params *p, int32_t *n1, int32_t *n2)
 {
     if (!p || !n1 || !n2) return GENFIRE_ERR_ARG;
+    if (p->griddingMethod == 1) {
+        const int m = gf::fft_grid_size(p->Dim2, p->oversamplingRatio);
+        if (m < 0) return GENFIRE_ERR_ARG;
+        *n1 = *n2 = m;
+        return GENFIRE_OK;
+    }
     *n1 = gf::oversampled(p->Dim1, p->oversamplingRatio);
     *n2 = gf::oversampled(p->Dim2, p->oversamplingRatio);
     return GENFIRE_OK;
@@ -173,6 +181,48 @@ genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p, const
         if (recIFFT) dR.alloc(nR, st);
         GF_CUDA(cudaMemcpyAsync(dp.p, projections, sizeof(double) * npj, cudaMemcpyHostToDevice, st));
         gf::grid_dft(ctx, *p, dp.as<double>(), angles, dM.p, recIFFT ? dR.p : nullptr, nk);
+        GF_CUDA(cudaMemcpyAsync(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st));
+        if (recIFFT) GF_CUDA(cudaMemcpyAsync(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+genfire_status genfire_grid_fft_device(genfire_ctx *ctx, const genfire_params *p, const double *d_projections,
+                                       const double *angles, void *d_measuredK, void *d_recIFFT, int64_t *npairs)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        need(d_projections, "projections");
+        need(angles, "angles");
+        need(d_measuredK, "measuredK");
+        gf::check_params(*p, true);
+        gf::grid_fft(ctx, *p, d_projections, angles, d_measuredK, d_recIFFT, npairs);
+    });
+}
+
+genfire_status genfire_grid_fft(genfire_ctx *ctx, const genfire_params *p, const double *projections,
+                                const double *angles, void *measuredK, void *recIFFT, int64_t *npairs)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        need(projections, "projections");
+        need(angles, "angles");
+        need(measuredK, "measuredK");
+        gf::check_params(*p, true);
+        const int m = gf::fft_grid_size(p->Dim2, p->oversamplingRatio);
+        if (m < 0)
+            gf::fail(GENFIRE_ERR_ARG, "FFT gridding: Dim2 * oversamplingRatio (1 + (Dim2-1) * oversamplingRatio "
+                                      "for odd Dim2) must be an integer.");
+        cudaStream_t st = ctx->stream;
+        const size_t npj = (size_t)p->Dim1 * p->Dim2 * p->NumProjs;
+        const size_t nM = (size_t)m * m * m * 2 * real_size(p->precision);
+        const size_t nR = (size_t)p->Dim1 * p->Dim2 * p->Dim1 * real_size(p->precision);
+        DevBuf dp(sizeof(double) * npj, st), dM(nM, st), dR;
+        if (recIFFT) dR.alloc(nR, st);
+        GF_CUDA(cudaMemcpyAsync(dp.p, projections, sizeof(double) * npj, cudaMemcpyHostToDevice, st));
+        gf::grid_fft(ctx, *p, dp.as<double>(), angles, dM.p, recIFFT ? dR.p : nullptr, npairs);
         GF_CUDA(cudaMemcpyAsync(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st));
         if (recIFFT) GF_CUDA(cudaMemcpyAsync(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st));
         GF_CUDA(cudaStreamSynchronize(st));

@@ -303,20 +303,24 @@ void rec_ifft(genfire_ctx *ctx, int precision, const void *d_M, int n1, int n2, 
 }
 
 // ===========================================================================
-// plain 3-D FFT (fftn / ifftn) on a full complex array
+// plain 3-D FFT (fftn / ifftn) on a full complex array, along the dimensions
+// set in axes (bit 0 = dim 1, ...); the inverse scales by 1 / (product of the
+// transformed lengths)
 // ===========================================================================
-template <typename T> static void fftn_t(genfire_ctx *ctx, cplx<T> *d, int n1, int n2, int n3, bool inv)
+template <typename T>
+static void fftn_t(genfire_ctx *ctx, cplx<T> *d, int n1, int n2, int n3, bool inv, int axes = 7)
 {
     cudaStream_t st = ctx->stream;
     ensure_smem_attrs<T>();
     const int dims[3] = {n1, n2, n3};
     int last = -1;
+    double prod = 1.0;
     for (int ax = 0; ax < 3; ++ax)
-        if (dims[ax] > 1) last = ax;
-    const T sc = inv ? (T)(1.0 / ((double)n1 * n2 * n3)) : (T)1;
+        if (dims[ax] > 1 && ((axes >> ax) & 1)) { last = ax; prod *= dims[ax]; }
+    const T sc = inv ? (T)(1.0 / prod) : (T)1;
     for (int ax = 0; ax < 3; ++ax) {
         const int n = dims[ax];
-        if (n == 1) continue;
+        if (n == 1 || !((axes >> ax) & 1)) continue;
         ColPassArgs<T> a = colargs<T>(plan_or_fail(n), twiddles<T>(n, st), tile_width<T>(n), 0);
         a.mode = inv ? 2 : 1;
         a.in = d; a.out = d; a.in_cnt = a.out_cnt = n; a.in_c = a.out_c = 0;
@@ -333,10 +337,10 @@ template <typename T> static void fftn_t(genfire_ctx *ctx, cplx<T> *d, int n1, i
     }
 }
 
-void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, int n3, bool inverse)
+void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, int n3, bool inverse, int axes)
 {
-    if (precision == GENFIRE_PREC_FP64) fftn_t<double>(ctx, (double2 *)d_data, n1, n2, n3, inverse);
-    else fftn_t<float>(ctx, (float2 *)d_data, n1, n2, n3, inverse);
+    if (precision == GENFIRE_PREC_FP64) fftn_t<double>(ctx, (double2 *)d_data, n1, n2, n3, inverse, axes);
+    else fftn_t<float>(ctx, (float2 *)d_data, n1, n2, n3, inverse, axes);
 }
 
 // ===========================================================================
@@ -585,8 +589,7 @@ template <typename T> struct ReconT : ReconBase {
         cudaStream_t st = ctx->stream;
         const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
         D1 = p.Dim1; D2 = p.Dim2;
-        n1 = oversampled(D1, p.oversamplingRatio);
-        n2 = oversampled(D2, p.oversamplingRatio);
+        grid_dims(p, n1, n2);
         if (n1 < D1 || n2 < D2) fail(GENFIRE_ERR_ARG, "oversampled size smaller than the projection size.");
         h1 = n1 / 2 + 1;
         ld1 = round_up(h1, 8);

@@ -55,6 +55,20 @@ void check_params(const genfire_params &p, bool need_projs);
 void grid_dft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
               void *d_M, void *d_rec, int64_t *nk);
 
+// Grid sizes of measuredK for the params' gridding method: DFT (griddingMethod
+// != 1) n1 x n2 x n1 with n = round(Dim * ratio); FFT (griddingMethod 1,
+// fillInFourierGrid.m:38-42) an m x m x m cube from Dim2 (n1 = n2 = m).
+void grid_dims(const genfire_params &p, int &n1, int &n2);
+// Cube size of fillInFourierGrid, -1 when Dim2 * ratio (or 1 + (Dim2-1) * ratio
+// for odd Dim2) is not an integer.
+int fft_grid_size(int Dim2, double ratio);
+
+// fillInFourierGrid (griddingMethod 1) on device buffers: d_proj (D1 x D2 x P
+// double), angles on the host, d_M (m x m x m centred, complex128 / complex64),
+// d_rec optional (D1 x D2 x D1); *npairs (optional) = gridded (voxel, value) pairs.
+void grid_fft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
+              void *d_M, void *d_rec, int64_t *npairs);
+
 // MIXED DFT of all selected points on the tensor cores (grid_mma.cu): F[j]
 // (complex64) for the points of every projection (counts nk, offsets off).
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
@@ -77,8 +91,9 @@ void iffshift_device(genfire_ctx *ctx, const int sz[3], long long count, const l
 // (the recIFFT of fillInFourierGrid_DFT.m:304).
 void rec_ifft(genfire_ctx *ctx, int precision, const void *d_M, int n1, int n2, int D1, int D2, void *d_rec);
 
-// In-place 3-D FFT (fftn/ifftn semantics) of an n1 x n2 x n3 complex array.
-void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, int n3, bool inverse);
+// In-place 3-D FFT (fftn/ifftn semantics) of an n1 x n2 x n3 complex array
+// along the dimensions set in axes (bit 0 = dim 1; 7 = all three).
+void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, int n3, bool inverse, int axes = 7);
 
 // The staged iteration behind genfire_recon_* (dr.cu).
 genfire_recon *recon_create(genfire_ctx *ctx, const genfire_params &p, const void *M, const uint8_t *mask,

@@ -109,6 +109,8 @@ class GENFIRE_Reconstructor:
         p.monitor_R = int(self.monitor_R)
         p.monitorR_loopLength = int(self.monitorR_loopLength)
         p.precision = self._prec()
+        p.griddingMethod = int(self.griddingMethod)
+        p.allowMultipleGridMatches = int(bool(self.allowMultipleGridMatches))
         return p
 
     # ------------------------------------------------------------------ GENFIRE_Reconstructor.m:82-112
@@ -182,14 +184,23 @@ class GENFIRE_Reconstructor:
     def runGridding(self):
         print("GENFIRE: Assembling Fourier grid...\n")
         if self.griddingMethod == 1:
-            raise GenfireError(_lib.GENFIRE_ERR_UNSUPPORTED,
-                               "GENFIRE: FFT gridding (griddingMethod = 1) is not in this build; use griddingMethod = 2.")
+            self.fillInFourierGrid()
         if self.griddingMethod == 2:
             self.fillInFourierGrid_DFT()
         if self._prec() == PREC_MIXED:
             self.measuredK = np.asfortranarray(self.measuredK, dtype=np.complex64)
         self.measuredK_mask = self.measuredK != 0
         self.Vol_ind = _lib.volumn_index(self.measuredK.shape, [self.Dim1, self.Dim2, self.Dim1])
+        return self
+
+    def fillInFourierGrid(self):
+        """@GENFIRE_Reconstructor/fillInFourierGrid.m:27-168 (griddingMethod 1) on the GPU."""
+        p = self.params()
+        M, rec, n = self._ctx().grid_fft(p, self.InputProjections, self.InputAngles, want_rec=True)
+        self.measuredK = M
+        self.recIFFT = rec
+        self.gridded_points = n
+        print("GENFIRE: Fourier grid assembled.\n")
         return self
 
     def fillInFourierGrid_DFT(self):
@@ -213,6 +224,18 @@ class GENFIRE_Reconstructor:
     # ------------------------------------------------------------------ reconstruct.m:28-194
     def reconstruct(self):
         p = self.params()
+        # reconstruct.m works on size(measuredK): pick the grid convention that matches it
+        shape = tuple(np.shape(self.measuredK))
+        for method in (int(self.griddingMethod), 2, 1):
+            try:
+                n1, n2 = _lib.grid_size(p, method=method)
+            except GenfireError:
+                continue
+            if shape == (n1, n2, n1):
+                p.griddingMethod = method
+                break
+        else:
+            raise GenfireError(_lib.GENFIRE_ERR_ARG, "GENFIRE: measuredK size does not match the projections.")
         if self.calculate_Rfree == 1:
             raise GenfireError(_lib.GENFIRE_ERR_UNSUPPORTED, "GENFIRE: calculate_Rfree is not in this build.")
         print("GENFIRE: Reconstructing... \n")

@@ -72,7 +72,13 @@ typedef struct genfire_params {
     int32_t monitor_R;                    /* R-factor every monitorR_loopLength */
     int32_t monitorR_loopLength;
     int32_t precision;                    /* genfire_precision */
-    int32_t reserved[9];                  /* zero */
+    int32_t griddingMethod;               /* 1: FFT gridding grid sizes (an m x m x m cube,
+                                             fillInFourierGrid.m:38-42) for genfire_grid_size
+                                             and the iteration; else DFT sizes n1 x n2 x n1.
+                                             genfire_params_init sets 2 (zero also means DFT) */
+    int32_t allowMultipleGridMatches;     /* FFT gridding: also grid to the voxels within
+                                             round(cutoff) of the nearest one (class default 1) */
+    int32_t reserved[7];                  /* zero */
 } genfire_params;
 
 typedef struct genfire_ctx genfire_ctx;
@@ -86,8 +92,10 @@ const char *genfire_status_string(genfire_status s);
 /* Class defaults (GENFIRE_Reconstructor.m:30-70) with precision = FP64. */
 genfire_status genfire_params_init(genfire_params *p);
 
-/* Oversampled grid size n1 = round(Dim1*ratio), n2 = round(Dim2*ratio)
- * (CheckPrepareData, GENFIRE_Reconstructor.m:168-169). */
+/* Size of measuredK: n1 x n2 x n1 with n1 = round(Dim1*ratio), n2 =
+ * round(Dim2*ratio) (CheckPrepareData, GENFIRE_Reconstructor.m:168-169), or,
+ * with griddingMethod = 1, the FFT-gridding cube n1 = n2 = m
+ * (fillInFourierGrid.m:38-42). */
 genfire_status genfire_grid_size(const genfire_params *p, int32_t *n1, int32_t *n2);
 
 /* ---- context ----------------------------------------------------------- */
@@ -119,6 +127,33 @@ genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p,
 genfire_status genfire_grid_dft_device(genfire_ctx *ctx, const genfire_params *p,
                                        const double *d_projections, const double *angles,
                                        void *d_measuredK, void *d_recIFFT, int64_t *nk);
+
+/* ---- gridding: fillInFourierGrid (griddingMethod = 1) -------------------
+ * Replaces obj = fillInFourierGrid(obj)
+ * (@GENFIRE_Reconstructor/fillInFourierGrid.m:27-168), the class's default
+ * gridding method in runGridding (GENFIRE_Reconstructor.m:175-177).
+ *   projections  Dim1 x Dim2 x NumProjs, double
+ *   angles       NumProjs x 3 (phi, theta, psi in degrees; the
+ *                GENFIRE/RELION convention of fillInFourierGrid.m:80-82 --
+ *                vector1..3 are not used), double
+ *   measuredK    m x m x m complex, centred; m = Dim2 * oversamplingRatio for
+ *                even Dim2, 1 + (Dim2-1) * oversamplingRatio for odd Dim2 (must
+ *                be an integer, and at least Dim1 and Dim2); complex128 for
+ *                FP64, complex64 for MIXED.  The values after the weighted
+ *                average (w = 1/(d + 1e-5) over the voxels within
+ *                interpolationCutoffDistance of each rotated FFT sample) and
+ *                hermitianSymmetrize.
+ *   recIFFT      Dim1 x Dim2 x Dim1 = My_stripzero(real(my_ifft(measuredK)))
+ *                (:165); double / float; NULL to skip
+ *   npairs       number of (voxel, value) pairs gridded; NULL ok
+ * allowMultipleGridMatches selects the shift search of :108-139.  The sums
+ * are FP64 atomic adds (order-independent up to FP64 rounding). */
+genfire_status genfire_grid_fft(genfire_ctx *ctx, const genfire_params *p,
+                                const double *projections, const double *angles,
+                                void *measuredK, void *recIFFT, int64_t *npairs);
+genfire_status genfire_grid_fft_device(genfire_ctx *ctx, const genfire_params *p,
+                                       const double *d_projections, const double *angles,
+                                       void *d_measuredK, void *d_recIFFT, int64_t *npairs);
 
 /* ---- iteration: reconstruct ---------------------------------------------
  * Replaces obj = reconstruct(obj) (@GENFIRE_Reconstructor/reconstruct.m:28-194).

@@ -666,6 +666,128 @@ int64_t orc_grid_dft(const orc_params *prm, const double *projs, const double *a
 }
 
 /* ------------------------------------------------------------------------ */
+/* FFT gridding: fillInFourierGrid (griddingMethod = 1)                       */
+/* ------------------------------------------------------------------------ */
+
+/* Cube size of fillInFourierGrid.m:38-42 (particleWindowSize = Dim2,
+ * GENFIRE_Reconstructor.m:121): Dim2*ratio for even Dim2, else
+ * 1 + (Dim2-1)*ratio; -1 when that is not an integer (MATLAB's zeros() would
+ * reject it). */
+int orc_fft_grid_size(int Dim2, double ratio)
+{
+    double m = (Dim2 % 2 == 0) ? (double)Dim2 * ratio : 1.0 + (double)(Dim2 - 1) * ratio;
+    double r = mround(m);
+    if (fabs(m - r) > 1e-9 || r < 1) return -1;
+    return (int)r;
+}
+
+/* fillInFourierGrid.m:27-168 in FP64 (the reference FFTs single-precision
+ * padded projections and sums single-precision products; this restatement
+ * keeps every value in double except the FP32 geometry and weights):
+ *   kMeasured(:,:,p) = my_fft(My_paddzero(proj_p, [m m])) (:59-61), my_fft =
+ *     fftshift(fftn(ifftshift(.))) (src/my_fft.m);
+ *   slice coordinates kx = i - nc (dim 1), ky = j - nc (dim 2), nc = floor(m/2)+1
+ *     (:47-54, meshgrid order);
+ *   rotkCoords = R' [kx; ky; 0] (:80-89) in FP32 with R of :80-82 (= the ZYZ
+ *     matrix of the projector transposed), products left to right without
+ *     FMA, the kz = 0 column dropped;
+ *   values exactly -999 are dropped (:97-101);
+ *   for Yshift, Xshift, Zshift in [-s, s] (outer to inner; s = round(cutoff)
+ *     when allowMultipleGridMatches, else 0, :108-139): voxel round(coords) +
+ *     shift (half away from zero), FP32 distance sqrt(dx^2 + dy^2 + dz^2),
+ *     kept when inside the m^3 cube and distance <= cutoff (compared in double);
+ *   weight 1/(d + 1e-5) in FP32 (:155-157); sums of w*F and w in FP64 in the
+ *     list order (shift, projection, pixel), FS = sum(wF)/sum(w) where
+ *     sum(w) > 0 (:159-161); measuredK = hermitianSymmetrize(FS) (:163);
+ *   recIFFT = My_stripzero(real(my_ifft(measuredK)), [Dim1 Dim2 Dim1]) (:165).
+ * measuredK: 2*m^3 doubles (centred, complex interleaved); rec (optional):
+ * Dim1*Dim2*Dim1.  Returns the number of (voxel, value) pairs gridded, or -1
+ * when m is not an integer or smaller than Dim1/Dim2. */
+int64_t orc_grid_fft(const orc_params *prm, int allowMultipleGridMatches, const double *projs,
+                     const double *angles, double *measuredK, double *rec)
+{
+    const int D1 = prm->Dim1, D2 = prm->Dim2, P = prm->NumProjs;
+    const int m = orc_fft_grid_size(D2, prm->oversamplingRatio);
+    if (m < 0 || m < D1 || m < D2) return -1;
+    const size_t mm = (size_t)m * m, N = mm * m;
+    const int h = m / 2;
+    /* per-projection centred spectra */
+    double *K = (double *)calloc(2 * mm * (size_t)P, sizeof(double));
+    double *buf = (double *)malloc(sizeof(double) * 2 * mm);
+    for (int p = 0; p < P; ++p) {
+        memset(buf, 0, sizeof(double) * 2 * mm);
+        /* padded position x + (h - D1/2), then ifftshift: index (x - D1/2) mod m */
+        for (int y = 0; y < D2; ++y)
+            for (int x = 0; x < D1; ++x) {
+                size_t d = (size_t)imod(x - D1 / 2, m) + (size_t)m * imod(y - D2 / 2, m);
+                buf[2 * d] = projs[(size_t)p * D1 * D2 + x + (size_t)D1 * y];
+            }
+        orc_fftn(buf, m, m, 1, 0);
+        double *kp = K + 2 * mm * (size_t)p;
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i < m; ++i) { /* fftshift: centred (i, j) <- FFT index (i - h, j - h) mod m */
+                size_t s = (size_t)imod(i - h, m) + (size_t)m * imod(j - h, m);
+                size_t d = (size_t)i + (size_t)m * j;
+                kp[2 * d] = buf[2 * s];
+                kp[2 * d + 1] = buf[2 * s + 1];
+            }
+    }
+    free(buf);
+    /* rotated slice coordinates, FP32 */
+    float *cx = (float *)malloc(sizeof(float) * mm * (size_t)P);
+    float *cy = (float *)malloc(sizeof(float) * mm * (size_t)P);
+    float *cz = (float *)malloc(sizeof(float) * mm * (size_t)P);
+    for (int p = 0; p < P; ++p) {
+        double R[9];
+        orc_rot_zyz(angles[p], angles[p + P], angles[p + 2 * P], R);
+        /* rotkCoords = R_fft' k = R_zyz k: X = R[0] kx + R[3] ky, Y = R[1] kx + R[4] ky, Z = R[2] kx + R[5] ky */
+        const float a0 = (float)R[0], a3 = (float)R[3], a1 = (float)R[1], a4 = (float)R[4];
+        const float a2 = (float)R[2], a5 = (float)R[5];
+        for (int j = 0; j < m; ++j)
+            for (int i = 0; i < m; ++i) {
+                const float kx = (float)(i - h), ky = (float)(j - h);
+                const size_t o = (size_t)p * mm + i + (size_t)m * j;
+                cx[o] = a0 * kx + a3 * ky;
+                cy[o] = a1 * kx + a4 * ky;
+                cz[o] = a2 * kx + a5 * ky;
+            }
+    }
+    const int s = allowMultipleGridMatches ? (int)mround(prm->interpolationCutoffDistance) : 0;
+    const double cut = prm->interpolationCutoffDistance;
+    double *num = (double *)calloc(2 * N, sizeof(double));
+    double *ws = (double *)calloc(N, sizeof(double));
+    int64_t pairs = 0;
+    for (int ys = -s; ys <= s; ++ys)
+        for (int xs = -s; xs <= s; ++xs)
+            for (int zs = -s; zs <= s; ++zs)
+                for (size_t o = 0; o < mm * (size_t)P; ++o) {
+                    const double vr = K[2 * o], vi = K[2 * o + 1];
+                    if (vr == -999.0 && vi == 0.0) continue;
+                    const float tx = roundf(cx[o]) + (float)xs, ty = roundf(cy[o]) + (float)ys,
+                                tz = roundf(cz[o]) + (float)zs;
+                    const float dx = cx[o] - tx, dy = cy[o] - ty, dz = cz[o] - tz;
+                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    const int ix = (int)tx + h, iy = (int)ty + h, iz = (int)tz + h;
+                    if (ix < 0 || ix >= m || iy < 0 || iy >= m || iz < 0 || iz >= m) continue;
+                    if (!((double)d <= cut)) continue;
+                    const float w = 1.0f / (d + 1e-5f);
+                    const size_t v = (size_t)ix + (size_t)m * (iy + (size_t)m * iz);
+                    num[2 * v] += vr * (double)w;
+                    num[2 * v + 1] += vi * (double)w;
+                    ws[v] += (double)w;
+                    ++pairs;
+                }
+    free(cx); free(cy); free(cz); free(K);
+    for (size_t v = 0; v < N; ++v)
+        if (ws[v] > 0) { num[2 * v] /= ws[v]; num[2 * v + 1] /= ws[v]; }
+    free(ws);
+    orc_hermitian_symmetrize(num, m, m, m, measuredK);
+    free(num);
+    if (rec) orc_rec_ifft(measuredK, m, m, D1, D2, rec);
+    return pairs;
+}
+
+/* ------------------------------------------------------------------------ */
 /* real-space projector (calculate3Dprojection_RealSpaceinterp(_general).m)  */
 /* interpolation is trilinear; out-of-volume samples are 0                    */
 /* ------------------------------------------------------------------------ */

@@ -254,3 +254,79 @@ def project(vol, R):
     c1 = c01 * (1 - fy) + c11 * fy
     val = np.where(inside, c0 * (1 - fz) + c1 * fz, 0.0)
     return val.reshape(n1, n2, n3).sum(axis=2)
+
+
+def _sincosd(x):
+    """sind/cosd exact at multiples of 90 degrees (MATLAB's sind/cosd)."""
+    r = np.remainder(x + 180.0, 360.0) - 180.0
+    q = np.round(r / 90.0)
+    t = np.deg2rad(r - 90.0 * q)
+    s, c = np.sin(t), np.cos(t)
+    qi = int(q) % 4
+    return [(s, c), (c, -s), (-s, -c), (-c, s)][qi]
+
+
+def fill_in_fourier_grid(projs, angles, ratio, cutoff, allow_multiple=True):
+    """fillInFourierGrid.m:27-168 statement by statement (FP64 values, FP32
+    coordinates and weights, accumarray as an ordered np.add.at)."""
+    D1, D2, P = projs.shape
+    m = D2 * ratio if D2 % 2 == 0 else 1 + (D2 - 1) * ratio
+    m = int(round(m))
+    nc = np.float32(mround((m + 1) / 2))
+    a = (np.arange(1, m + 1) - nc).astype(np.float32)
+    ky, kx = np.meshgrid(a, a)            # kx along dim 1, ky along dim 2
+    kx = kx.reshape(-1, order="F")
+    ky = ky.reshape(-1, order="F")
+    kz = np.zeros_like(kx)
+    kM = np.zeros((m, m, P), dtype=np.complex128)
+    for p in range(P):
+        pad = paddzero(projs[:, :, p], (m, m))
+        kM[:, :, p] = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(pad)))
+    mX = np.zeros((m * m, P), dtype=np.float32)
+    mY = np.zeros_like(mX)
+    mZ = np.zeros_like(mX)
+    for p in range(P):
+        sf, cf = _sincosd(angles[p, 0])
+        st, ct = _sincosd(angles[p, 1])
+        sp, cp = _sincosd(angles[p, 2])
+        R = np.array([[cp * ct * cf - sp * sf, cp * ct * sf + sp * cf, -cp * st],
+                      [-sp * ct * cf - cp * sf, -sp * ct * sf + cp * cf, sp * st],
+                      [st * cf, st * sf, ct]])
+        Rt = R.T.astype(np.float32)
+        mX[:, p] = Rt[0, 0] * kx + Rt[0, 1] * ky + Rt[0, 2] * kz
+        mY[:, p] = Rt[1, 0] * kx + Rt[1, 1] * ky + Rt[1, 2] * kz
+        mZ[:, p] = Rt[2, 0] * kx + Rt[2, 1] * ky + Rt[2, 2] * kz
+    mX = mX.reshape(-1, order="F"); mY = mY.reshape(-1, order="F"); mZ = mZ.reshape(-1, order="F")
+    kv = kM.reshape(-1, order="F")
+    good = kv != -999
+    mX, mY, mZ, kv = mX[good], mY[good], mZ[good], kv[good]
+    s = int(mround(cutoff)) if allow_multiple else 0
+    inds, vals, dists = [], [], []
+    for ys in range(-s, s + 1):
+        for xs in range(-s, s + 1):
+            for zs in range(-s, s + 1):
+                tX = (np.sign(mX) * np.floor(np.abs(mX) + np.float32(0.5))).astype(np.float32) + np.float32(xs)
+                tY = (np.sign(mY) * np.floor(np.abs(mY) + np.float32(0.5))).astype(np.float32) + np.float32(ys)
+                tZ = (np.sign(mZ) * np.floor(np.abs(mZ) + np.float32(0.5))).astype(np.float32) + np.float32(zs)
+                dx, dy, dz = mX - tX, mY - tY, mZ - tZ
+                d = np.sqrt(dx * dx + dy * dy + dz * dz).astype(np.float32)
+                tY1, tZ1, tX1 = tY + nc, tZ + nc, tX + nc
+                ok = ~((tX1 > m) | (tX1 < 1) | (tY1 > m) | (tY1 < 1) | (tZ1 > m) | (tZ1 < 1)) & (d.astype(np.float64) <= cutoff)
+                ix = tX1[ok].astype(np.int64) - 1
+                iy = tY1[ok].astype(np.int64) - 1
+                iz = tZ1[ok].astype(np.int64) - 1
+                inds.append(ix + m * (iy + m * iz))
+                vals.append(kv[ok])
+                dists.append(d[ok])
+    ind = np.concatenate(inds)
+    val = np.concatenate(vals)
+    w = np.float32(1.0) / (np.concatenate(dists) + np.float32(1e-5))
+    num = np.zeros(m ** 3, dtype=np.complex128)
+    ws = np.zeros(m ** 3, dtype=np.float64)
+    np.add.at(num, ind, val * w.astype(np.float64))
+    np.add.at(ws, ind, w.astype(np.float64))
+    pos = ws > 0
+    num[pos] = num[pos] / ws[pos]
+    K = hermitian_symmetrize(num.reshape((m, m, m), order="F"))
+    rec = stripzero(np.real(np.fft.fftshift(np.fft.ifftn(np.fft.ifftshift(K)))), (D1, D2, D1))
+    return K, rec, ind.size

@@ -64,6 +64,10 @@ def lib():
         L.orc_grid_dft.restype = C.c_int64
         L.orc_grid_dft.argtypes = [C.POINTER(OrcParams), dp, dp, dp, dp, lp]
         L.orc_rec_ifft.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_int, dp]
+        L.orc_fft_grid_size.restype = C.c_int
+        L.orc_fft_grid_size.argtypes = [C.c_int, C.c_double]
+        L.orc_grid_fft.restype = C.c_int64
+        L.orc_grid_fft.argtypes = [C.POINTER(OrcParams), C.c_int, dp, dp, dp, dp]
         L.orc_project_R.argtypes = [dp, C.c_int, C.c_int, C.c_int, dp, dp]
         L.orc_project.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]
         L.orc_rfactor.argtypes = [dp, dp, C.c_int64, dp, dp]
@@ -255,6 +259,27 @@ def grid_dft(prm, projs, angles, want_rec=True):
                        _p(M.reshape(-1, order="F").view(np.float64), C.c_double),
                        _p(rec, C.c_double), _p(nk, C.c_int64))
     return M, rec, nk
+
+
+def fft_grid_size(Dim2, ratio):
+    """Cube size m of fillInFourierGrid (-1 when not an integer)."""
+    return lib().orc_fft_grid_size(int(Dim2), float(ratio))
+
+
+def grid_fft(prm, projs, angles, allow_multiple=1, want_rec=True):
+    """fillInFourierGrid (griddingMethod 1): (measuredK m^3 centred complex128,
+    recIFFT or None, number of gridded pairs)."""
+    P = _f64(projs); A = _f64(angles)
+    m = fft_grid_size(prm.Dim2, prm.oversamplingRatio)
+    if m < 0:
+        raise ValueError("fillInFourierGrid: Dim2 * oversamplingRatio is not an integer")
+    M = np.zeros((m, m, m), dtype=np.complex128, order="F")
+    rec = np.zeros((prm.Dim1, prm.Dim2, prm.Dim1), dtype=np.float64, order="F") if want_rec else None
+    n = lib().orc_grid_fft(C.byref(prm), int(allow_multiple), _p(P, C.c_double), _p(A, C.c_double),
+                           _p(M.reshape(-1, order="F").view(np.float64), C.c_double), _p(rec, C.c_double))
+    if n < 0:
+        raise ValueError("fillInFourierGrid: grid smaller than the projections")
+    return M, rec, n
 
 
 def rec_ifft(M, D1, D2):
