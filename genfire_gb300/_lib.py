@@ -24,6 +24,9 @@ GENFIRE_ERR_STATE = 6
 PREC_FP64 = 0
 PREC_MIXED = 1
 
+INTERP_TRILINEAR = 0
+INTERP_CUBIC = 1
+
 # every entry point of include/genfire.h
 EXPORTS = [
     "genfire_abi_version", "genfire_status_string", "genfire_params_init", "genfire_grid_size",
@@ -31,7 +34,8 @@ EXPORTS = [
     "genfire_grid_dft", "genfire_grid_dft_device", "genfire_grid_fft", "genfire_grid_fft_device",
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
-    "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc",
+    "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc", "genfire_set_projector_interpolation",
+    "genfire_rfactor_realspace",
     "genfire_centro_symmetricity", "genfire_hermitian_symmetrize", "genfire_make_kspace_indices",
     "genfire_volumn_index", "genfire_iffshift3_ind", "genfire_select", "genfire_fftn",
 ]
@@ -99,6 +103,9 @@ def load():
                                       dp, dp, dp]),
         "genfire_rfactor_noalloc": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp,
                                               dp, vp, dp, dp, dp]),
+        "genfire_set_projector_interpolation": (C.c_int, [vp, C.c_int32]),
+        "genfire_rfactor_realspace": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, dp, C.c_int32,
+                                                C.c_int32, C.c_int32, dp, dp, dp, fp]),
         "genfire_centro_symmetricity": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32, dp]),
         "genfire_hermitian_symmetrize": (C.c_int, [vp, dp, C.c_int32, C.c_int32, C.c_int32, dp]),
         "genfire_make_kspace_indices": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32, dp]),
@@ -301,6 +308,26 @@ class Context:
                                           ptr(vec, C.c_double), ptr(Mj, C.c_double), ptr(R1, C.c_double),
                                           ptr(R2, C.c_double), C.byref(eR)))
         return eR.value, R1, R2
+
+    def set_projector_interpolation(self, interp):
+        """INTERP_TRILINEAR (default) or INTERP_CUBIC for every projector use of this context."""
+        self.check(load().genfire_set_projector_interpolation(self._h, int(interp)))
+
+    def rfactor_realspace(self, model, projs, angles, precision=PREC_FP64):
+        """Tian_calc_Rfactor_realspace: (Rtotal, Rarr, simuProjs float32)."""
+        rdt = np.float64 if precision == PREC_FP64 else np.float32
+        V = fortran(model, rdt)
+        Pj = fortran(projs if np.ndim(projs) == 3 else np.asarray(projs)[:, :, None], np.float64)
+        A = fortran(np.atleast_2d(angles), np.float64)
+        m1, m2, m3 = V.shape
+        p1, p2, P = Pj.shape
+        R = np.zeros(P)
+        tot = C.c_double()
+        simu = np.zeros((p1, p2, P), dtype=np.float32, order="F")
+        self.check(load().genfire_rfactor_realspace(self._h, precision, ptr(V), m1, m2, m3, ptr(Pj, C.c_double),
+                                                    p1, p2, P, ptr(A, C.c_double), ptr(R, C.c_double),
+                                                    C.byref(tot), ptr(simu, C.c_float)))
+        return tot.value, R, simu
 
     # ---------------------------------------------------------------- index / symmetry
     def centro_symmetricity(self, FS, n1, n_k1, n2):

@@ -374,6 +374,46 @@ genfire_status genfire_rfactor(genfire_ctx *ctx, int32_t precision, const void *
     });
 }
 
+genfire_status genfire_set_projector_interpolation(genfire_ctx *ctx, int32_t interp)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    if (interp != GENFIRE_INTERP_TRILINEAR && interp != GENFIRE_INTERP_CUBIC) {
+        ctx->last_error = "GENFIRE: interpolation must be GENFIRE_INTERP_TRILINEAR or GENFIRE_INTERP_CUBIC.";
+        return GENFIRE_ERR_ARG;
+    }
+    ctx->interp = interp;
+    return GENFIRE_OK;
+}
+
+genfire_status genfire_rfactor_realspace(genfire_ctx *ctx, int32_t precision, const void *model, int32_t m1,
+                                         int32_t m2, int32_t m3, const double *projs, int32_t p1, int32_t p2,
+                                         int32_t num_proj, const double *angles, double *Rarr, double *Rtotal,
+                                         float *simuProjs)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(model, "model");
+        need(projs, "projs");
+        need(angles, "angles");
+        if (precision != GENFIRE_PREC_FP64 && precision != GENFIRE_PREC_MIXED) gf::fail(GENFIRE_ERR_ARG, "bad precision.");
+        if (num_proj < 1) gf::fail(GENFIRE_ERR_ARG, "num_proj must be positive.");
+        if (p1 < 1 || p2 < 1) gf::fail(GENFIRE_ERR_ARG, "projection sizes must be positive.");
+        cudaStream_t st = ctx->stream;
+        const size_t es = real_size(precision);
+        const size_t nv = (size_t)m1 * m2 * m3, np = (size_t)p1 * p2 * num_proj;
+        DevBuf dv(es * nv, st), dp(sizeof(double) * np, st), ds;
+        if (simuProjs) ds.alloc(sizeof(float) * np, st);
+        GF_CUDA(cudaMemcpyAsync(dv.p, model, es * nv, cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemcpyAsync(dp.p, projs, sizeof(double) * np, cudaMemcpyHostToDevice, st));
+        gf::rfactor_realspace(ctx, precision, dv.p, m1, m2, m3, num_proj, angles, dp.as<double>(), p1, p2, Rarr,
+                              Rtotal, simuProjs ? ds.as<float>() : nullptr);
+        if (simuProjs) {
+            GF_CUDA(cudaMemcpyAsync(simuProjs, ds.p, sizeof(float) * np, cudaMemcpyDeviceToHost, st));
+            GF_CUDA(cudaStreamSynchronize(st));
+        }
+    });
+}
+
 // Allocation-free: no std::function wrapper, no heap buffers; errors are
 // caught here directly.
 genfire_status genfire_rfactor_noalloc(genfire_ctx *ctx, int32_t precision, const void *d_vol, int32_t n1,

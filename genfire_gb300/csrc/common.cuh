@@ -106,5 +106,6 @@ struct genfire_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
+    int interp = GENFIRE_INTERP_TRILINEAR;  // projector interpolation (genfire_set_projector_interpolation)
     std::string last_error;
 };

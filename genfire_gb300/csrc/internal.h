@@ -115,6 +115,13 @@ void project_batch(genfire_ctx *ctx, int precision, const void *d_vol, int n1, i
                    long long vs1, long long vs2, int P, const double *d_R, void *d_proj,
                    const double *d_measured, double *d_sums, cudaStream_t stream);
 
+// Tian_calc_Rfactor_realspace on device buffers: d_model (m1 x m2 x m3),
+// d_projs (p1 x p2 x P double), host angles; Rarr (P) and Rtotal on the host,
+// d_simu (p1 x p2 x P float, optional) on the device.
+void rfactor_realspace(genfire_ctx *ctx, int precision, const void *d_model, int m1, int m2, int m3, int P,
+                       const double *angles, const double *d_projs, int p1, int p2, double *Rarr, double *Rtotal,
+                       float *d_simu);
+
 // R-factors with the scratch in a static device array (no allocation); host
 // angles/vectors and outputs as genfire_rfactor.
 size_t rfactor_noalloc_bytes(int n1, int n2, int P);

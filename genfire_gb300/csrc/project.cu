@@ -4,7 +4,8 @@
 // grid by R, samples the volume there and sums along dimension 3
 // (src/calculate3Dprojection_RealSpaceinterp.m:17-55).  Here one thread owns
 // one output pixel and walks the rotated line through the volume with
-// trilinear interpolation (0 outside the volume); the volume of a 256^3
+// trilinear interpolation (the default) or the cubic convolution of interp3
+// 'cubic' (:45), both 0 outside the volume; the volume of a 256^3
 // reconstruction (67 MB in FP32) stays resident in the 129 MB L2.  The
 // R-factor sums of reconstruct.m:176-177 are fused into the same kernel
 // and reduced with warp shuffles, per projection, in a fixed order.
@@ -57,9 +58,71 @@ __device__ __forceinline__ T trilinear(const T *__restrict__ V, int n1, int n2, 
     return c0 * ((T)1 - fz) + c1 * fz;
 }
 
-constexpr int kProjThreads = 256;
+// interp3(..., 'cubic', 0) on a uniform grid: separable cubic convolution
+// with Keys' kernel (a = -1/2) and Keys' boundary rule f(-1) = 3 f(0) - 3 f(1)
+// + f(2) (and its mirror at the far end), 0 outside [0, n-1] in any
+// dimension.  MATLAB's own implementation is closed; this is the published
+// method it names (cubic convolution), restated.  Needs n >= 4 per dimension.
+// Per dimension: the 4 consecutive indices from s and their weights, with the
+// boundary rule folded in.
+template <typename T> __device__ __forceinline__ void keys_taps(T x, int n, int &s, T (&e)[4])
+{
+    int i = (int)floor(x);
+    i = min(max(i, 0), n - 2);
+    const T t = x - (T)i, t2 = t * t, t3 = t2 * t;
+    const T wm = (T)0.5 * (-t3 + (T)2 * t2 - t);            // index i - 1
+    const T w0 = (T)0.5 * ((T)3 * t3 - (T)5 * t2 + (T)2);   // i
+    const T w1 = (T)0.5 * ((T)-3 * t3 + (T)4 * t2 + t);     // i + 1
+    const T w2 = (T)0.5 * (t3 - t2);                        // i + 2
+    if (i == 0) {            // f(-1) = 3 f(0) - 3 f(1) + f(2)
+        s = 0;
+        e[0] = w0 + (T)3 * wm; e[1] = w1 - (T)3 * wm; e[2] = w2 + wm; e[3] = (T)0;
+    } else if (i == n - 2) { // f(n) = 3 f(n-1) - 3 f(n-2) + f(n-3)
+        s = n - 4;
+        e[0] = (T)0; e[1] = wm + w2; e[2] = w0 - (T)3 * w2; e[3] = w1 + (T)3 * w2;
+    } else {
+        s = i - 1;
+        e[0] = wm; e[1] = w0; e[2] = w1; e[3] = w2;
+    }
+}
 
 template <typename T>
+__device__ __forceinline__ T tricubic(const T *__restrict__ V, int n1, int n2, int n3, long long vs1, long long vs2,
+                                      T x, T y, T z)
+{
+    if (!(x >= (T)0 && y >= (T)0 && z >= (T)0 && x <= (T)(n1 - 1) && y <= (T)(n2 - 1) && z <= (T)(n3 - 1)))
+        return (T)0;
+    int si, sj, sk;
+    T ex[4], ey[4], ez[4];
+    keys_taps<T>(x, n1, si, ex);
+    keys_taps<T>(y, n2, sj, ey);
+    keys_taps<T>(z, n3, sk, ez);
+    T acc = (T)0;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        T accy = (T)0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const T *row = V + si + (long long)(sj + b) * vs1 + (long long)(sk + c) * vs2;
+            const T ax = ex[0] * row[0] + ex[1] * row[1] + ex[2] * row[2] + ex[3] * row[3];
+            accy += ey[b] * ax;
+        }
+        acc += ez[c] * accy;
+    }
+    return acc;
+}
+
+template <typename T, bool CUBIC>
+__device__ __forceinline__ T sample(const T *__restrict__ V, int n1, int n2, int n3, long long vs1, long long vs2,
+                                    T x, T y, T z)
+{
+    if constexpr (CUBIC) return tricubic<T>(V, n1, n2, n3, vs1, vs2, x, y, z);
+    else return trilinear<T>(V, n1, n2, n3, vs1, vs2, x, y, z);
+}
+
+constexpr int kProjThreads = 256;
+
+template <typename T, bool CUBIC>
 __global__ void __launch_bounds__(kProjThreads)
     k_project(const T *__restrict__ vol, int n1, int n2, int n3, long long vs1, long long vs2,
               const double *__restrict__ Rs, T *__restrict__ proj, const double *__restrict__ measured,
@@ -81,7 +144,7 @@ __global__ void __launch_bounds__(kProjThreads)
             const T rx = Coord<T>::lin(R[0], X, R[3], Y, R[6], Z);
             const T ry = Coord<T>::lin(R[1], X, R[4], Y, R[7], Z);
             const T rz = Coord<T>::lin(R[2], X, R[5], Y, R[8], Z);
-            part_acc += trilinear<T>(vol, n1, n2, n3, vs1, vs2, rx + (T)c1, ry + (T)c2, rz + (T)c3);
+            part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, rx + (T)c1, ry + (T)c2, rz + (T)c3);
             if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
         }
         acc += (double)part_acc;
@@ -127,13 +190,17 @@ static void project_t(genfire_ctx *ctx, const T *vol, int n1, int n2, int n3, lo
     DevBuf part;
     if (d_meas) part.alloc(sizeof(double) * 4 * (size_t)nblk * P, st);
     dim3 grid(nblk, P);
-    k_project<T><<<grid, kProjThreads, 0, st>>>(vol, n1, n2, n3, vs1, vs2, d_R, d_proj, d_meas, part.as<double>());
+    if (ctx->interp == GENFIRE_INTERP_CUBIC)
+        k_project<T, true><<<grid, kProjThreads, 0, st>>>(vol, n1, n2, n3, vs1, vs2, d_R, d_proj, d_meas,
+                                                          part.as<double>());
+    else
+        k_project<T, false><<<grid, kProjThreads, 0, st>>>(vol, n1, n2, n3, vs1, vs2, d_R, d_proj, d_meas,
+                                                           part.as<double>());
     GF_CHECK_LAUNCH();
     if (d_meas) {
         k_project_sums<<<P, 32, 0, st>>>(part.as<double>(), (int)nblk, d_sums);
         GF_CHECK_LAUNCH();
     }
-    (void)ctx;
 }
 
 void project_batch(genfire_ctx *ctx, int precision, const void *d_vol, int n1, int n2, int n3, long long vs1,
@@ -141,12 +208,94 @@ void project_batch(genfire_ctx *ctx, int precision, const void *d_vol, int n1, i
                    cudaStream_t stream)
 {
     if (n1 < 2 || n2 < 2 || n3 < 2) fail(GENFIRE_ERR_ARG, "projector: every volume dimension must be at least 2.");
+    if (ctx->interp == GENFIRE_INTERP_CUBIC && (n1 < 4 || n2 < 4 || n3 < 4))
+        fail(GENFIRE_ERR_ARG, "projector: cubic interpolation needs at least 4 samples in every dimension.");
     if (precision == GENFIRE_PREC_FP64)
         project_t<double>(ctx, (const double *)d_vol, n1, n2, n3, vs1, vs2, P, d_R, (double *)d_proj, d_measured,
                           d_sums, stream);
     else
         project_t<float>(ctx, (const float *)d_vol, n1, n2, n3, vs1, vs2, P, d_R, (float *)d_proj, d_measured,
                          d_sums, stream);
+}
+
+// ===========================================================================
+// Tian_calc_Rfactor_realspace (src/Tian_calc_Rfactor_realspace.m:1-24): the
+// ZYX projections of a model, cropped to the measured size (My_stripzero),
+// Rarr = sum| |bp| - |pj| | / sum|pj| per projection, their mean, and the
+// simulated projections in single precision.
+// ===========================================================================
+template <typename T>
+__global__ void __launch_bounds__(256) k_rfactor_rs(const T *__restrict__ bp, int m1, int m2, int o1, int o2,
+                                                    const double *__restrict__ pj, int p1, int p2,
+                                                    float *__restrict__ simu, double *__restrict__ sums)
+{
+    const int p = blockIdx.x;
+    const T *b = bp + (size_t)p * m1 * m2;
+    const double *q = pj + (size_t)p * p1 * p2;
+    double s0 = 0, s1 = 0;
+    for (int t = threadIdx.x; t < p1 * p2; t += blockDim.x) {
+        const int i = t % p1, j = t / p1;
+        const T v = b[(o1 + i) + (size_t)m1 * (o2 + j)];
+        const double x = q[t];
+        s0 += fabs(fabs((double)v) - fabs(x));
+        s1 += fabs(x);
+        if (simu) simu[(size_t)p * p1 * p2 + t] = (float)v;
+    }
+    __shared__ double red[2][8];
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = s0; red[1][threadIdx.x >> 5] = s1; }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double v = 0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) v += red[threadIdx.x][w];
+        sums[2 * p + threadIdx.x] = v;
+    }
+}
+
+// My_stripzero's crop start along a dimension of size big kept to size ori
+static int strip_start(int big, int ori)
+{
+    if (big % 2 == 0) return ori % 2 == 0 ? (big - ori) / 2 : (big - ori + 1) / 2;
+    return ori % 2 == 0 ? (big - ori - 1) / 2 : (big - ori) / 2;
+}
+
+void rfactor_realspace(genfire_ctx *ctx, int precision, const void *d_model, int m1, int m2, int m3, int P,
+                       const double *angles, const double *d_projs, int p1, int p2, double *Rarr, double *Rtotal,
+                       float *d_simu)
+{
+    if (p1 > m1 || p2 > m2) fail(GENFIRE_ERR_ARG, "rfactor_realspace: the projections are larger than the model.");
+    cudaStream_t st = ctx->stream;
+    // calculate3Dprojection_RealSpaceinterpZYX: the general projector with the
+    // axes Z, Y, X for phi, theta, psi
+    const double v[9] = {0, 0, 1, 0, 1, 0, 1, 0, 0};
+    std::vector<double> Rs(9 * (size_t)P);
+    for (int q = 0; q < P; ++q) euler_rot(v, v + 3, v + 6, angles[q], angles[q + P], angles[q + 2 * P], &Rs[9 * (size_t)q]);
+    const size_t es = precision == GENFIRE_PREC_FP64 ? sizeof(double) : sizeof(float);
+    DevBuf dR(sizeof(double) * Rs.size(), st), bp(es * (size_t)m1 * m2 * P, st), sums(sizeof(double) * 2 * P, st);
+    GF_CUDA(cudaMemcpyAsync(dR.p, Rs.data(), sizeof(double) * Rs.size(), cudaMemcpyHostToDevice, st));
+    project_batch(ctx, precision, d_model, m1, m2, m3, m1, (long long)m1 * m2, P, dR.as<double>(), bp.p, nullptr,
+                  nullptr, st);
+    const int o1 = strip_start(m1, p1), o2 = strip_start(m2, p2);
+    if (precision == GENFIRE_PREC_FP64)
+        k_rfactor_rs<double><<<P, 256, 0, st>>>(bp.as<double>(), m1, m2, o1, o2, d_projs, p1, p2, d_simu,
+                                                sums.as<double>());
+    else
+        k_rfactor_rs<float><<<P, 256, 0, st>>>(bp.as<float>(), m1, m2, o1, o2, d_projs, p1, p2, d_simu,
+                                               sums.as<double>());
+    GF_CHECK_LAUNCH();
+    std::vector<double> hs(2 * (size_t)P);
+    GF_CUDA(cudaMemcpyAsync(hs.data(), sums.p, sizeof(double) * hs.size(), cudaMemcpyDeviceToHost, st));
+    GF_CUDA(cudaStreamSynchronize(st));
+    double tot = 0;
+    for (int q = 0; q < P; ++q) {
+        const double r = hs[2 * q] / hs[2 * q + 1];
+        if (Rarr) Rarr[q] = r;
+        tot += r;
+    }
+    if (Rtotal) *Rtotal = tot / P;
 }
 
 // ===========================================================================
@@ -221,12 +370,19 @@ void rfactor_noalloc(genfire_ctx *ctx, int precision, const void *d_vol, int n1,
         GF_CUDA(cudaMemcpyAsync(dR + 9 * (size_t)c0, chunk, sizeof(double) * 9 * cn, cudaMemcpyHostToDevice, st));
     }
     dim3 grid(nblk, P);
-    if (precision == GENFIRE_PREC_FP64)
-        k_project<double><<<grid, kProjThreads, 0, st>>>((const double *)d_vol, n1, n2, n3, n1, (long long)n1 * n2,
-                                                        dR, nullptr, d_measured, part);
-    else
-        k_project<float><<<grid, kProjThreads, 0, st>>>((const float *)d_vol, n1, n2, n3, n1, (long long)n1 * n2,
-                                                       dR, nullptr, d_measured, part);
+    const bool cub = ctx->interp == GENFIRE_INTERP_CUBIC;
+    if (cub && (n1 < 4 || n2 < 4 || n3 < 4))
+        fail(GENFIRE_ERR_ARG, "projector: cubic interpolation needs at least 4 samples in every dimension.");
+    const long long s1 = n1, s2 = (long long)n1 * n2;
+    if (precision == GENFIRE_PREC_FP64) {
+        const double *v = (const double *)d_vol;
+        if (cub) k_project<double, true><<<grid, kProjThreads, 0, st>>>(v, n1, n2, n3, s1, s2, dR, nullptr, d_measured, part);
+        else k_project<double, false><<<grid, kProjThreads, 0, st>>>(v, n1, n2, n3, s1, s2, dR, nullptr, d_measured, part);
+    } else {
+        const float *v = (const float *)d_vol;
+        if (cub) k_project<float, true><<<grid, kProjThreads, 0, st>>>(v, n1, n2, n3, s1, s2, dR, nullptr, d_measured, part);
+        else k_project<float, false><<<grid, kProjThreads, 0, st>>>(v, n1, n2, n3, s1, s2, dR, nullptr, d_measured, part);
+    }
     GF_CHECK_LAUNCH();
     k_project_sums<<<P, 32, 0, st>>>(part, (int)nblk, dsum);
     GF_CHECK_LAUNCH();

@@ -211,14 +211,43 @@ const char *genfire_profile_kernel_name(int32_t k);
  * closed-form ZYZ matrix of :13-15) and
  * calculate3Dprojection_RealSpaceinterp_general(Vol,phi,theta,psi,v1,v2,v3)
  * (src/calculate3Dprojection_RealSpaceinterp_general.m:1-49; vectors = the 9
- * values v1, v2, v3).  Interpolation is trilinear, samples outside the volume
- * are 0.  Vol is n1 x n2 x n3; each projection is n1 x n2.  NumProj angle
+ * values v1, v2, v3).  Interpolation is trilinear (or cubic, see
+ * genfire_set_projector_interpolation), samples outside the volume are 0.  Vol is n1 x n2 x n3; each projection is n1 x n2.  NumProj angle
  * rows (NumProj x 3, column-major like InputAngles).  vol/projs are double
  * for FP64 and float for MIXED. */
 genfire_status genfire_project(genfire_ctx *ctx, int32_t precision,
                                const void *vol, int32_t n1, int32_t n2, int32_t n3,
                                int32_t num_proj, const double *angles, const double *vectors,
                                void *projs);
+/* Interpolation of the projector (genfire_project, genfire_rfactor,
+ * genfire_rfactor_noalloc, genfire_rfactor_realspace and the R-factor monitor
+ * of the iteration) for this context.  TRILINEAR (the default) is the
+ * projector the benchmark and its R-factors are defined with; CUBIC is the
+ * reference's interp3(..., 'cubic', 0) (calculate3Dprojection_RealSpaceinterp.m:45):
+ * separable cubic convolution with Keys' kernel (a = -1/2) and Keys' boundary
+ * rule, 0 outside the volume; it needs at least 4 samples per dimension.
+ * MATLAB's interp3 is closed source, so cubic parity with MATLAB is unpinned. */
+#define GENFIRE_INTERP_TRILINEAR 0
+#define GENFIRE_INTERP_CUBIC 1
+genfire_status genfire_set_projector_interpolation(genfire_ctx *ctx, int32_t interp);
+
+/* Replaces [Rtotal, Rarr, simuProjs] = Tian_calc_Rfactor_realspace(model, Projs,
+ * Angles) (src/Tian_calc_Rfactor_realspace.m:1-24).  Its projector,
+ * calculate3Dprojection_RealSpaceinterpZYX, is not in the reference tree; it is
+ * taken as the general projector with the axes Z, Y, X ([0 0 1], [0 1 0],
+ * [1 0 0]) for phi, theta, psi.  Each m1 x m2 projection of the m1 x m2 x m3
+ * model is cropped to p1 x p2 (My_stripzero) and compared with the measured
+ * projection: Rarr(i) = sum| |bp| - |pj| | / sum|pj|, Rtotal = mean(Rarr).
+ *   model      m1 x m2 x m3, double (FP64) / float (MIXED)
+ *   projs      p1 x p2 x num_proj double (p1 <= m1, p2 <= m2)
+ *   angles     num_proj x 3 double
+ *   simuProjs  p1 x p2 x num_proj float (single, as the reference returns
+ *              it); NULL to skip */
+genfire_status genfire_rfactor_realspace(genfire_ctx *ctx, int32_t precision, const void *model, int32_t m1,
+                                         int32_t m2, int32_t m3, const double *projs, int32_t p1, int32_t p2,
+                                         int32_t num_proj, const double *angles, double *Rarr, double *Rtotal,
+                                         float *simuProjs);
+
 /* R-factors of reconstruct.m:168-185: per projection
  * Rarr = sum|bp - pj| / sum|pj| and Rarr2 = ||bp - pj||_F / ||pj||_F of the
  * projection bp of vol against the measured pj; errR = mean(Rarr).

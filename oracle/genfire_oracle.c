@@ -815,9 +815,48 @@ static inline double tri(const double *V, int n1, int n2, int n3, double x, doub
     return c0 * (1 - fz) + c1 * fz;
 }
 
+/* interp3(..., 'cubic', 0) restated as the published method it names:
+ * cubic convolution with Keys' kernel (a = -1/2), samples beyond the grid
+ * taken from Keys' boundary rule f(-1) = 3 f(0) - 3 f(1) + f(2) (mirrored at
+ * the far end), 0 outside [0, n-1] in any dimension.  MATLAB's own code is
+ * closed, so parity with it is unpinned.  Needs n >= 4 per dimension. */
+static double keys_w(double s)
+{
+    s = fabs(s);
+    if (s <= 1.0) return 1.5 * s * s * s - 2.5 * s * s + 1.0;
+    if (s < 2.0) return -0.5 * s * s * s + 2.5 * s * s - 4.0 * s + 2.0;
+    return 0.0;
+}
+static double keys_ext(const double *V, int n1, int n2, int n3, int a, int b, int c)
+{
+    if (a < 0) return 3 * keys_ext(V, n1, n2, n3, 0, b, c) - 3 * keys_ext(V, n1, n2, n3, 1, b, c) + keys_ext(V, n1, n2, n3, 2, b, c);
+    if (a > n1 - 1) return 3 * keys_ext(V, n1, n2, n3, n1 - 1, b, c) - 3 * keys_ext(V, n1, n2, n3, n1 - 2, b, c) + keys_ext(V, n1, n2, n3, n1 - 3, b, c);
+    if (b < 0) return 3 * keys_ext(V, n1, n2, n3, a, 0, c) - 3 * keys_ext(V, n1, n2, n3, a, 1, c) + keys_ext(V, n1, n2, n3, a, 2, c);
+    if (b > n2 - 1) return 3 * keys_ext(V, n1, n2, n3, a, n2 - 1, c) - 3 * keys_ext(V, n1, n2, n3, a, n2 - 2, c) + keys_ext(V, n1, n2, n3, a, n2 - 3, c);
+    if (c < 0) return 3 * keys_ext(V, n1, n2, n3, a, b, 0) - 3 * keys_ext(V, n1, n2, n3, a, b, 1) + keys_ext(V, n1, n2, n3, a, b, 2);
+    if (c > n3 - 1) return 3 * keys_ext(V, n1, n2, n3, a, b, n3 - 1) - 3 * keys_ext(V, n1, n2, n3, a, b, n3 - 2) + keys_ext(V, n1, n2, n3, a, b, n3 - 3);
+    return V[(size_t)a + (size_t)n1 * (b + (size_t)n2 * c)];
+}
+static int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+static double cub(const double *V, int n1, int n2, int n3, double x, double y, double z)
+{
+    if (!(x >= 0 && y >= 0 && z >= 0 && x <= n1 - 1 && y <= n2 - 1 && z <= n3 - 1)) return 0.0;
+    const int i = clampi((int)floor(x), 0, n1 - 2), j = clampi((int)floor(y), 0, n2 - 2), k = clampi((int)floor(z), 0, n3 - 2);
+    double s = 0.0;
+    for (int c = k - 1; c <= k + 2; ++c) {
+        const double wz = keys_w(z - c);
+        for (int b = j - 1; b <= j + 2; ++b) {
+            const double wy = keys_w(y - b);
+            for (int a = i - 1; a <= i + 2; ++a) s += keys_w(x - a) * wy * wz * keys_ext(V, n1, n2, n3, a, b, c);
+        }
+    }
+    return s;
+}
+
 /* Proj(i,j) = sum_k Vol(R * [X_i; Y_j; Z_k]) with centred coordinates
- * -ceil((n-1)/2)..floor((n-1)/2) (…RealSpaceinterp.m:17-31, 55). */
-void orc_project_R(const double *vol, int n1, int n2, int n3, const double R[9], double *proj)
+ * -ceil((n-1)/2)..floor((n-1)/2) (…RealSpaceinterp.m:17-31, 55); interp 0
+ * trilinear, 1 cubic. */
+static void project_R_interp(const double *vol, int n1, int n2, int n3, const double R[9], int interp, double *proj)
 {
     int c1 = n1 / 2, c2 = n2 / 2, c3 = n3 / 2;
 #pragma omp parallel for collapse(2) schedule(static)
@@ -829,10 +868,16 @@ void orc_project_R(const double *vol, int n1, int n2, int n3, const double R[9],
                 double rx = R[0] * X + R[3] * Y + R[6] * Z;
                 double ry = R[1] * X + R[4] * Y + R[7] * Z;
                 double rz = R[2] * X + R[5] * Y + R[8] * Z;
-                s += tri(vol, n1, n2, n3, rx + c1, ry + c2, rz + c3);
+                s += interp ? cub(vol, n1, n2, n3, rx + c1, ry + c2, rz + c3)
+                            : tri(vol, n1, n2, n3, rx + c1, ry + c2, rz + c3);
             }
             proj[(size_t)i + (size_t)n1 * j] = s;
         }
+}
+
+void orc_project_R(const double *vol, int n1, int n2, int n3, const double R[9], double *proj)
+{
+    project_R_interp(vol, n1, n2, n3, R, 0, proj);
 }
 
 /* vecs == NULL: the ZYZ closed form of calculate3Dprojection_RealSpaceinterp;
@@ -843,7 +888,48 @@ void orc_project(const double *vol, int n1, int n2, int n3, double phi, double t
     double R[9];
     if (vecs) orc_euler_rot(vecs, vecs + 3, vecs + 6, phi, theta, psi, R);
     else orc_rot_zyz(phi, theta, psi, R);
-    orc_project_R(vol, n1, n2, n3, R, proj);
+    project_R_interp(vol, n1, n2, n3, R, 0, proj);
+}
+
+void orc_project_interp(const double *vol, int n1, int n2, int n3, double phi, double theta, double psi,
+                        const double *vecs, int interp, double *proj)
+{
+    double R[9];
+    if (vecs) orc_euler_rot(vecs, vecs + 3, vecs + 6, phi, theta, psi, R);
+    else orc_rot_zyz(phi, theta, psi, R);
+    project_R_interp(vol, n1, n2, n3, R, interp, proj);
+}
+
+/* Tian_calc_Rfactor_realspace.m:1-24: projections with the Z, Y, X axes
+ * (calculate3Dprojection_RealSpaceinterpZYX, absent from the reference tree,
+ * taken as the general projector with vectors [0 0 1], [0 1 0], [1 0 0]),
+ * cropped to p1 x p2 by My_stripzero, Rarr = sum| |bp| - |pj| | / sum|pj|,
+ * returns mean(Rarr); simu (p1*p2*P, optional) receives the cropped
+ * projections. */
+double orc_rfactor_realspace(const double *model, int m1, int m2, int m3, const double *projs, int p1, int p2,
+                             int P, const double *angles, int interp, double *Rarr, double *simu)
+{
+    const double v[9] = {0, 0, 1, 0, 1, 0, 1, 0, 0};
+    double *bp = (double *)malloc(sizeof(double) * (size_t)m1 * m2);
+    double *cr = (double *)malloc(sizeof(double) * (size_t)p1 * p2);
+    int ps[3] = {m1, m2, 1}, os[3] = {p1, p2, 1};
+    double tot = 0.0;
+    for (int q = 0; q < P; ++q) {
+        orc_project_interp(model, m1, m2, m3, angles[q], angles[q + P], angles[q + 2 * P], v, interp, bp);
+        orc_stripzero(bp, ps, os, cr);
+        const double *pj = projs + (size_t)q * p1 * p2;
+        double a = 0.0, b = 0.0;
+        for (size_t t = 0; t < (size_t)p1 * p2; ++t) {
+            a += fabs(fabs(cr[t]) - fabs(pj[t]));
+            b += fabs(pj[t]);
+        }
+        Rarr[q] = a / b;
+        tot += Rarr[q];
+        if (simu) memcpy(simu + (size_t)q * p1 * p2, cr, sizeof(double) * (size_t)p1 * p2);
+    }
+    free(bp);
+    free(cr);
+    return tot / P;
 }
 
 /* R-factors of reconstruct.m:176-177: sum|bp-pj|/sum|pj| and the Frobenius ratio. */

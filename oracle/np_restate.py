@@ -330,3 +330,44 @@ def fill_in_fourier_grid(projs, angles, ratio, cutoff, allow_multiple=True):
     K = hermitian_symmetrize(num.reshape((m, m, m), order="F"))
     rec = stripzero(np.real(np.fft.fftshift(np.fft.ifftn(np.fft.ifftshift(K)))), (D1, D2, D1))
     return K, rec, ind.size
+
+
+def _keys_dense(x, n):
+    """Dense length-n weights of Keys' cubic convolution (a = -1/2) at x, with
+    the boundary samples f(-1) = 3f(0) - 3f(1) + f(2) and f(n) = 3f(n-1) -
+    3f(n-2) + f(n-3) folded in; None outside [0, n-1]."""
+    if not (0 <= x <= n - 1):
+        return None
+    i = min(max(int(np.floor(x)), 0), n - 2)
+    w = np.zeros(n)
+    for a in range(i - 1, i + 3):
+        s = abs(x - a)
+        k = 1.5 * s ** 3 - 2.5 * s ** 2 + 1 if s <= 1 else (-0.5 * s ** 3 + 2.5 * s ** 2 - 4 * s + 2 if s < 2 else 0.0)
+        if a < 0:
+            w[0] += 3 * k; w[1] -= 3 * k; w[2] += k
+        elif a > n - 1:
+            w[n - 1] += 3 * k; w[n - 2] -= 3 * k; w[n - 3] += k
+        else:
+            w[a] += k
+    return w
+
+
+def project_cubic(vol, R):
+    """calculate3Dprojection_RealSpaceinterp with interp3 'cubic' read as Keys
+    cubic convolution: each rotated sample as a tensor product of dense 1-D
+    weight vectors."""
+    n1, n2, n3 = vol.shape
+    c = (n1 // 2, n2 // 2, n3 // 2)
+    out = np.zeros((n1, n2))
+    for i in range(n1):
+        for j in range(n2):
+            s = 0.0
+            for k in range(n3):
+                X = np.array([i - c[0], j - c[1], k - c[2]], dtype=np.float64)
+                r = R @ X + np.array(c)
+                w1, w2, w3 = _keys_dense(r[0], n1), _keys_dense(r[1], n2), _keys_dense(r[2], n3)
+                if w1 is None or w2 is None or w3 is None:
+                    continue
+                s += np.einsum("a,b,c,abc->", w1, w2, w3, vol)
+            out[i, j] = s
+    return out

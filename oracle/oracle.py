@@ -71,6 +71,11 @@ def lib():
         L.orc_project_R.argtypes = [dp, C.c_int, C.c_int, C.c_int, dp, dp]
         L.orc_project.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]
         L.orc_rfactor.argtypes = [dp, dp, C.c_int64, dp, dp]
+        L.orc_project_interp.argtypes = [dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, dp,
+                                         C.c_int, dp]
+        L.orc_rfactor_realspace.restype = C.c_double
+        L.orc_rfactor_realspace.argtypes = [dp, C.c_int, C.c_int, C.c_int, dp, C.c_int, C.c_int, C.c_int, dp,
+                                            C.c_int, dp, dp]
         L.orc_delay_indicators.restype = C.c_int
         L.orc_delay_indicators.argtypes = [C.c_int, dp]
         L.orc_change_points.argtypes = [C.c_int, C.c_int, ip]
@@ -288,6 +293,30 @@ def rec_ifft(M, D1, D2):
     rec = np.zeros((D1, D2, D1), dtype=np.float64, order="F")
     lib().orc_rec_ifft(_p(Mv, C.c_double), n1, n2, D1, D2, _p(rec, C.c_double))
     return rec
+
+
+def project_interp(vol, phi, theta, psi, vectors=None, cubic=False):
+    """Projector with trilinear (cubic=False) or Keys cubic-convolution (cubic=True) sampling."""
+    V = _f64(vol); n1, n2, n3 = V.shape
+    out = np.zeros((n1, n2), dtype=np.float64, order="F")
+    vec = None
+    if vectors is not None:
+        vec = np.ascontiguousarray(np.asarray(vectors, dtype=np.float64).reshape(9))
+    lib().orc_project_interp(_p(V, C.c_double), n1, n2, n3, phi, theta, psi, _p(vec, C.c_double), int(cubic),
+                             _p(out, C.c_double))
+    return out
+
+
+def rfactor_realspace(model, projs, angles, cubic=False):
+    """Tian_calc_Rfactor_realspace: (Rtotal, Rarr, simuProjs)."""
+    V = _f64(model); m1, m2, m3 = V.shape
+    Pj = _f64(projs); p1, p2, P = Pj.shape
+    A = _f64(np.atleast_2d(angles))
+    R = np.zeros(P)
+    simu = np.zeros((p1, p2, P), dtype=np.float64, order="F")
+    tot = lib().orc_rfactor_realspace(_p(V, C.c_double), m1, m2, m3, _p(Pj, C.c_double), p1, p2, P,
+                                      _p(A, C.c_double), int(cubic), _p(R, C.c_double), _p(simu, C.c_double))
+    return tot, R, simu
 
 
 def project(vol, phi, theta, psi, vectors=None):
