@@ -34,6 +34,7 @@ EXPORTS = [
     "genfire_grid_dft", "genfire_grid_dft_device", "genfire_grid_fft", "genfire_grid_fft_device",
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
+    "genfire_recon_batch_create", "genfire_recon_batch_iterate", "genfire_recon_batch_destroy",
     "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc", "genfire_set_projector_interpolation",
     "genfire_rfactor_realspace",
     "genfire_centro_symmetricity", "genfire_hermitian_symmetrize", "genfire_make_kspace_indices",
@@ -96,6 +97,9 @@ def load():
         "genfire_recon_iterate": (C.c_int, [vp, C.c_int32]),
         "genfire_recon_result": (C.c_int, [vp, vp, vp, dp, dp, dp, C.c_int32]),
         "genfire_recon_destroy": (C.c_int, [vp]),
+        "genfire_recon_batch_create": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "genfire_recon_batch_iterate": (C.c_int, [vp, C.c_int32]),
+        "genfire_recon_batch_destroy": (C.c_int, [vp]),
         "genfire_recon_profile": (C.c_int, [vp, C.c_int32, dp, dp]),
         "genfire_profile_kernel_name": (C.c_char_p, [C.c_int32]),
         "genfire_project": (C.c_int, [vp, C.c_int32, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp, dp, vp]),
@@ -432,6 +436,34 @@ class Recon:
     def close(self):
         if getattr(self, "_h", None):
             load().genfire_recon_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ReconBatch:
+    """A genfire_recon_batch: one graph launch iterates every member Recon concurrently."""
+
+    def __init__(self, ctx, members):
+        self.ctx = ctx
+        self.members = list(members)
+        arr = (C.c_void_p * len(self.members))(*[m._h.value for m in self.members])
+        h = C.c_void_p()
+        ctx.check(load().genfire_recon_batch_create(ctx.handle, len(self.members), arr, C.byref(h)))
+        self._h = h
+
+    def iterate(self, count):
+        self.ctx.check(load().genfire_recon_batch_iterate(self._h, count))
+        for m in self.members:
+            m.done += count
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().genfire_recon_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

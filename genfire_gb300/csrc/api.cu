@@ -266,6 +266,30 @@ genfire_status genfire_recon_destroy(genfire_recon *r)
     return guarded(ctx, [&] { gf::recon_destroy(r); });
 }
 
+genfire_status genfire_recon_batch_create(genfire_ctx *ctx, int32_t count, genfire_recon *const *members,
+                                          genfire_recon_batch **out)
+{
+    if (!ctx || !out) return GENFIRE_ERR_ARG;
+    *out = nullptr;
+    return guarded(ctx, [&] {
+        need(members, "members");
+        *out = gf::recon_batch_create(ctx, members, count);
+    });
+}
+
+genfire_status genfire_recon_batch_iterate(genfire_recon_batch *b, int32_t count)
+{
+    if (!b) return GENFIRE_ERR_ARG;
+    return guarded(b->ctx, [&] { gf::recon_batch_iterate(b, count); });
+}
+
+genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b)
+{
+    if (!b) return GENFIRE_OK;
+    genfire_ctx *ctx = b->ctx;
+    return guarded(ctx, [&] { gf::recon_batch_destroy(b); });
+}
+
 genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes)
 {
     if (!r) return GENFIRE_ERR_ARG;

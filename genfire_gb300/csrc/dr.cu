@@ -21,6 +21,7 @@
 #include "internal.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -97,26 +98,28 @@ template <typename T, int N> static void set_reg_attrs()
     GF_CUDA(cudaFuncSetAttribute((const void *)k_row_c2r_reg<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
 }
 
-// Two float columns per thread need unit column stride and 16-byte aligned
-// column pairs (even strides, aligned bases; tiles start at even columns).
-// They pay off in the fused forward + constraint + inverse pass (two
-// transforms per load); the single-transform passes keep one column per
-// thread and twice the resident warps.
-template <typename T> static bool pair_ok(const ColPassArgs<T> &a)
+// Launch variants of a column pass: the generic shared-memory engine, the
+// register-resident engine with one column per thread, or with two adjacent
+// float columns per thread.  The last needs unit column stride and 16-byte
+// aligned column pairs (even strides, aligned bases; tiles start at even
+// columns).
+enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2 };
+
+template <typename T> static bool pair_capable(const ColPassArgs<T> &a)
 {
     auto al = [](const void *p) { return ((uintptr_t)p & 15u) == 0; };
-    return sizeof(T) == 4 && (a.mode & 3) == 3 && a.col_stride == 1 && al(a.in) && al(a.out) &&
-           a.in_dim % 2 == 0 && a.in_other % 2 == 0 && a.out_dim % 2 == 0 && a.out_other % 2 == 0;
+    return sizeof(T) == 4 && a.col_stride == 1 && al(a.in) && al(a.out) && a.in_dim % 2 == 0 &&
+           a.in_other % 2 == 0 && a.out_dim % 2 == 0 && a.out_other % 2 == 0;
 }
 
 // Register-resident passes for power-of-two lengths 64..1024.
-template <typename T, int N> static void col_reg(const ColPassArgs<T> &a, int other, cudaStream_t st)
+template <typename T, int N> static void col_reg(const ColPassArgs<T> &a, int other, cudaStream_t st, int nc)
 {
     constexpr int W = reg_width<T>(N);
     if (a.W != W) fail(GENFIRE_ERR_STATE, "internal: column tile width mismatch.");
     dim3 grid(cdiv(a.ncols, W), other);
     if constexpr (sizeof(T) == 4) {
-        if (pair_ok(a)) {
+        if (nc == 2) {
             k_col_reg<T, N, 2><<<grid, col_threads<T, N, 2>(), reg_smem<T, N>(), st>>>(a);
             return;
         }
@@ -131,18 +134,21 @@ template <typename T, int N> static void rows_reg(const RowPassArgs<T> &a, bool 
     if (forward) k_row_r2c_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
     else k_row_c2r_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
 }
-template <typename T> static bool try_col_reg(const ColPassArgs<T> &a, int other, cudaStream_t st)
+template <typename T> static bool reg_capable(const ColPassArgs<T> &a)
 {
     // element offsets along the transform are 32-bit in the register passes
     const long long span = (long long)(a.pl.n - 1) * std::max(a.in_dim, a.out_dim) + 1;
-    if (span >= (1LL << 32)) return false;
+    const int n = a.pl.n;
+    return span < (1LL << 32) && (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024);
+}
+template <typename T> static void col_reg_any(const ColPassArgs<T> &a, int other, cudaStream_t st, int nc)
+{
     switch (a.pl.n) {
-    case 64: col_reg<T, 64>(a, other, st); return true;
-    case 128: col_reg<T, 128>(a, other, st); return true;
-    case 256: col_reg<T, 256>(a, other, st); return true;
-    case 512: col_reg<T, 512>(a, other, st); return true;
-    case 1024: col_reg<T, 1024>(a, other, st); return true;
-    default: return false;
+    case 64: col_reg<T, 64>(a, other, st, nc); break;
+    case 128: col_reg<T, 128>(a, other, st, nc); break;
+    case 256: col_reg<T, 256>(a, other, st, nc); break;
+    case 512: col_reg<T, 512>(a, other, st, nc); break;
+    default: col_reg<T, 1024>(a, other, st, nc); break;
     }
 }
 template <typename T> static bool try_rows_reg(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
@@ -179,16 +185,75 @@ template <typename T> static void ensure_smem_attrs()
     done.insert(dev);
 }
 
-// Column pass launcher
-template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st)
+template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
+{
+    if (v == kColGeneric) return true;
+    if (!reg_capable(a)) return false;
+    return v == kColReg1 || (v == kColReg2 && pair_capable(a));
+}
+
+// Column pass launcher.  Without a tuned variant: two columns per thread in
+// the fused forward + constraint + inverse pass (two transforms per load),
+// one column per thread in the single-transform passes (twice the resident
+// warps), the generic engine for other lengths.
+template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st, int variant = kColAuto)
 {
     a.P = a.W + 1;
-    if (!try_col_reg<T>(a, other, st)) {
+    if (variant == kColAuto || !col_variant_ok(a, variant)) {
+        if (!reg_capable(a)) variant = kColGeneric;
+        else variant = ((a.mode & 3) == 3 && pair_capable(a)) ? kColReg2 : kColReg1;
+    }
+    if (variant == kColGeneric) {
         const size_t sm = tile_smem<T>(a.pl.n, a.W);
         dim3 grid(cdiv(a.ncols, a.W), other);
         k_colpass<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
+    } else {
+        col_reg_any<T>(a, other, st, variant == kColReg2 ? 2 : 1);
     }
     GF_CHECK_LAUNCH();
+}
+
+// Autotuner of the column passes: every valid variant is timed on the
+// caller's own buffers (one warm-up launch, then the mean of 3 launches
+// bracketed by CUDA events) and the fastest is kept for the process, keyed by
+// the device, the precision and the pass geometry.  Runs at setup, outside
+// any stream capture; the timed launches only write the pass's output buffer
+// and its errK partials, which the first real iteration overwrites.
+template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, cudaStream_t st)
+{
+    static std::mutex mu;
+    static std::map<std::vector<long long>, int> cache;
+    ensure_smem_attrs<T>();
+    int dev = 0;
+    GF_CUDA(cudaGetDevice(&dev));
+    const std::vector<long long> key = {dev, (long long)sizeof(T), a.pl.n, a.mode, a.ncols, other, a.in_cnt,
+                                        a.in_c, a.out_cnt, a.out_c, a.in_dim, a.in_other, a.out_dim, a.out_other};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    cudaEvent_t e0, e1;
+    GF_CUDA(cudaEventCreate(&e0));
+    GF_CUDA(cudaEventCreate(&e1));
+    int best = kColAuto;
+    float best_ms = 0;
+    for (int v : {kColGeneric, kColReg1, kColReg2}) {
+        if (!col_variant_ok(a, v)) continue;
+        launch_colpass<T>(a, other, st, v);
+        GF_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < 3; ++r) launch_colpass<T>(a, other, st, v);
+        GF_CUDA(cudaEventRecord(e1, st));
+        GF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        GF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (best == kColAuto || ms < best_ms) { best = v; best_ms = ms; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = best;
+    return best;
 }
 
 template <typename T> static void launch_rows(RowPassArgs<T> a, bool forward, cudaStream_t st)
@@ -560,6 +625,11 @@ __global__ void k_extract(const T *const *__restrict__ xs, const Ctl *__restrict
 struct ReconBase {
     virtual ~ReconBase() {}
     virtual void iterate(int count) = 0;
+    // one iteration as a (not instantiated) graph, for batches
+    virtual cudaGraph_t capture_iteration() = 0;
+    // iterations still allowed, and the bookkeeping after one batched iteration
+    virtual int remaining() const = 0;
+    virtual void advance() = 0;
     virtual void profile(int count, double *ms, double *bytes) = 0;
     virtual void result(void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device) = 0;
 };
@@ -574,6 +644,7 @@ template <typename T> struct ReconT : ReconBase {
     int m = 0, nparts = 0, tiles1 = 0, ntab = 0;
     double denom = 0;
     int it_done = 0;
+    int vF2 = kColAuto, vF3 = kColAuto, vI2 = kColAuto;  // column-pass variants (autotuned)
     cudaGraphExec_t exec = nullptr;
     std::vector<double> errR, Rarr, Rarr2;
 
@@ -715,7 +786,52 @@ template <typename T> struct ReconT : ReconBase {
             dsums.alloc(sizeof(double) * 4 * P, st);
         }
         GF_CUDA(cudaStreamSynchronize(st));
+        autotune();
         build_graph();
+    }
+
+    // F2: dim 2 forward, box rows in, all n2 frequencies out
+    ColPassArgs<T> f2_args()
+    {
+        ColPassArgs<T> a = colargs<T>(pl2, tw2, W2, h1);
+        a.in = Y1.as<cplx<T>>(); a.in_dim = ld1; a.in_other = (long long)ld1 * B2; a.in_cnt = B2; a.in_c = B2 / 2;
+        a.out = Y2.as<cplx<T>>(); a.out_dim = ld1; a.out_other = (long long)ld1 * n2; a.out_cnt = n2; a.out_c = 0;
+        a.mode = 1;
+        return a;
+    }
+    // F3: dim 3 forward, constraint, dim 3 inverse (in place)
+    ColPassArgs<T> f3_args()
+    {
+        Ctl *c = ctl.as<Ctl>();
+        ColPassArgs<T> b = colargs<T>(pl1, tw1, W3, h1);
+        b.in = Y2.as<cplx<T>>(); b.in_dim = (long long)ld1 * n2; b.in_other = ld1; b.in_cnt = B3; b.in_c = B3 / 2;
+        b.out = Y2.as<cplx<T>>(); b.out_dim = (long long)ld1 * n2; b.out_other = ld1; b.out_cnt = B3; b.out_c = B3 / 2;
+        b.mode = 1 | 2 | 4;
+        b.tab_off = taboff.as<int>(); b.tab = tab.as<TabEntry<T>>(); b.h1 = h1; b.partial = partial.as<double>();
+        b.cidx = &c->cidx;
+        return b;
+    }
+    // I2: dim 2 inverse, box rows out
+    ColPassArgs<T> i2_args()
+    {
+        ColPassArgs<T> d = colargs<T>(pl2, tw2, W2, h1);
+        d.in = Y2.as<cplx<T>>(); d.in_dim = ld1; d.in_other = (long long)ld1 * n2; d.in_cnt = n2; d.in_c = 0;
+        d.out = Y1.as<cplx<T>>(); d.out_dim = ld1; d.out_other = (long long)ld1 * B2; d.out_cnt = B2; d.out_c = B2 / 2;
+        d.mode = 2;
+        return d;
+    }
+
+    // Column-pass variants by measurement on this problem's buffers (the
+    // environment variable GENFIRE_AUTOTUNE=0 keeps the default choices).
+    void autotune()
+    {
+        const char *env = std::getenv("GENFIRE_AUTOTUNE");
+        if (env && env[0] == '0') return;
+        cudaStream_t st = ctx->stream;
+        vF2 = autotune_colpass<T>(f2_args(), B3, st);
+        vF3 = autotune_colpass<T>(f3_args(), n2, st);
+        vI2 = autotune_colpass<T>(i2_args(), B3, st);
+        GF_CUDA(cudaStreamSynchronize(st));
     }
 
     // ev (optional) receives an event before each of the 7 kernels and one after
@@ -739,31 +855,14 @@ template <typename T> struct ReconT : ReconBase {
         r.scale = (T)1;
         launch_rows<T>(r, true, st);
         mark();
-        // F2: dim 2 forward, box rows in, all n2 frequencies out
-        ColPassArgs<T> a = colargs<T>(pl2, tw2, W2, h1);
-        a.in = Y1.as<cplx<T>>(); a.in_dim = ld1; a.in_other = (long long)ld1 * B2; a.in_cnt = B2; a.in_c = B2 / 2;
-        a.out = Y2.as<cplx<T>>(); a.out_dim = ld1; a.out_other = (long long)ld1 * n2; a.out_cnt = n2; a.out_c = 0;
-        a.mode = 1;
-        launch_colpass<T>(a, B3, st);
+        launch_colpass<T>(f2_args(), B3, st, vF2);
         mark();
-        // F3: dim 3 forward, constraint, dim 3 inverse (in place)
-        ColPassArgs<T> b = colargs<T>(pl1, tw1, W3, h1);
-        b.in = Y2.as<cplx<T>>(); b.in_dim = (long long)ld1 * n2; b.in_other = ld1; b.in_cnt = B3; b.in_c = B3 / 2;
-        b.out = Y2.as<cplx<T>>(); b.out_dim = (long long)ld1 * n2; b.out_other = ld1; b.out_cnt = B3; b.out_c = B3 / 2;
-        b.mode = 1 | 2 | 4;
-        b.tab_off = taboff.as<int>(); b.tab = tab.as<TabEntry<T>>(); b.h1 = h1; b.partial = partial.as<double>();
-        b.cidx = &c->cidx;
-        launch_colpass<T>(b, n2, st);
+        launch_colpass<T>(f3_args(), n2, st, vF3);
         mark();
         k_ctl_mid<<<1, 1024, 0, st>>>(c, partial.as<double>(), nparts, denom, hist.as<double>());
         GF_CHECK_LAUNCH();
         mark();
-        // I2: dim 2 inverse, box rows out
-        ColPassArgs<T> d = colargs<T>(pl2, tw2, W2, h1);
-        d.in = Y2.as<cplx<T>>(); d.in_dim = ld1; d.in_other = (long long)ld1 * n2; d.in_cnt = n2; d.in_c = 0;
-        d.out = Y1.as<cplx<T>>(); d.out_dim = ld1; d.out_other = (long long)ld1 * B2; d.out_cnt = B2; d.out_c = B2 / 2;
-        d.mode = 2;
-        launch_colpass<T>(d, B3, st);
+        launch_colpass<T>(i2_args(), B3, st, vI2);
         mark();
         // I1: rows half spectrum -> real box, 1/N
         RowPassArgs<T> q = r;
@@ -820,7 +919,7 @@ template <typename T> struct ReconT : ReconBase {
         if (bytes) kernel_bytes(bytes);
     }
 
-    void build_graph()
+    cudaGraph_t capture_iteration() override
     {
         cudaStream_t st = ctx->stream;
         ensure_smem_attrs<T>();  // kernel attributes are set outside the capture
@@ -834,9 +933,22 @@ template <typename T> struct ReconT : ReconBase {
             throw;
         }
         GF_CUDA(cudaStreamEndCapture(st, &graph));
+        return graph;
+    }
+
+    void build_graph()
+    {
+        cudaGraph_t graph = capture_iteration();
         cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         GF_CUDA(e);
+    }
+
+    int remaining() const override { return p.numIterations - it_done; }
+    void advance() override
+    {
+        ++it_done;
+        if (p.monitor_R == 1 && it_done % p.monitorR_loopLength == 0) monitor();
     }
 
     void monitor()
@@ -937,6 +1049,64 @@ void recon_destroy(genfire_recon *r)
 {
     delete r->impl;
     delete r;
+}
+
+// ===========================================================================
+// batches: one graph holds one iteration of every member problem as
+// independent child graphs, so one launch runs them all concurrently
+// ===========================================================================
+genfire_recon_batch *recon_batch_create(genfire_ctx *ctx, genfire_recon *const *members, int count)
+{
+    if (count < 1) fail(GENFIRE_ERR_ARG, "batch: at least one reconstruction.");
+    for (int i = 0; i < count; ++i) {
+        if (!members[i]) fail(GENFIRE_ERR_ARG, "batch: NULL reconstruction.");
+        if (members[i]->ctx != ctx) fail(GENFIRE_ERR_ARG, "batch: every reconstruction must belong to the batch's context.");
+        for (int j = 0; j < i; ++j)
+            if (members[j] == members[i]) fail(GENFIRE_ERR_ARG, "batch: a reconstruction appears twice.");
+    }
+    cudaGraph_t parent = nullptr;
+    GF_CUDA(cudaGraphCreate(&parent, 0));
+    cudaGraphExec_t exec = nullptr;
+    try {
+        for (int i = 0; i < count; ++i) {
+            cudaGraph_t g = members[i]->impl->capture_iteration();
+            cudaGraphNode_t node;
+            const cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, g);  // copies g
+            cudaGraphDestroy(g);
+            GF_CUDA(e);
+        }
+        GF_CUDA(cudaGraphInstantiate(&exec, parent, 0));
+    } catch (...) {
+        cudaGraphDestroy(parent);
+        throw;
+    }
+    cudaGraphDestroy(parent);
+    auto *b = new genfire_recon_batch();
+    b->ctx = ctx;
+    b->members.assign(members, members + count);
+    b->exec = exec;
+    return b;
+}
+
+void recon_batch_iterate(genfire_recon_batch *b, int count)
+{
+    if (count < 0) fail(GENFIRE_ERR_ARG, "batch: negative iteration count.");
+    for (genfire_recon *r : b->members)
+        if (r->impl->remaining() < count)
+            fail(GENFIRE_ERR_STATE, "batch: more iterations requested than a member's numIterations allows.");
+    cudaStream_t st = b->ctx->stream;
+    for (int i = 0; i < count; ++i) {
+        GF_CUDA(cudaGraphLaunch(b->exec, st));
+        for (genfire_recon *r : b->members) r->impl->advance();
+    }
+    GF_CUDA(cudaStreamSynchronize(st));
+}
+
+void recon_batch_destroy(genfire_recon_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    cudaStreamSynchronize(b->ctx->stream);
+    delete b;
 }
 
 }  // namespace gf

@@ -17,6 +17,8 @@
 //   phases are reduced exactly in FP64 (a*u is exact, the fractional part is
 //   taken before sincospi) and advanced by FP32 rotations within 16-element
 //   blocks, then split into BF16 hi/lo and stored in the same layout.
+// * Persistent: one CTA per SM drains the tiles of all projections from a
+//   device work queue (an atomic counter).
 // * One elected thread issues tcgen05.mma (M = 128, N = 256, K = 16) and
 //   tcgen05.commit; shared-memory stages are double buffered so the next
 //   chunk is generated while the tensor core works on the current one.
@@ -222,6 +224,7 @@ struct MmaArgs {
     int nkc, nnc;             // K chunks (32 wide), N chunks (256 wide)
     int npad_last;            // columns of the last N chunk, a multiple of 64
     int *err;                 // set to 1 when a bounded wait expires
+    int *queue;               // next tile to take (starts at 0)
 };
 
 __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
@@ -263,7 +266,15 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     const int r = tid & (kM - 1), h = tid >> 7;  // A generation: row r, quarter h of the 32-wide chunk
     bool ok = true;
 
-    for (int item = blockIdx.x; item < a.ntiles && ok; item += gridDim.x) {
+    // tiles are drained from a device work queue: each CTA takes the next
+    // unclaimed tile when it finishes one
+    __shared__ int s_item;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(a.queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= a.ntiles) break;
         const MmaTile tl = a.tiles[item];
         const bool row_ok = r < tl.nj;
         const float uj = row_ok ? a.u[tl.j0 + r] : 0.f;
@@ -488,9 +499,9 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
         for (long long j = 0; j < nk[p]; j += kM)
             tiles.push_back(MmaTile{p, (int)std::min<long long>(kM, nk[p] - j), off[p] + j});
     if (tiles.empty()) return;
-    DevBuf dt(sizeof(MmaTile) * tiles.size(), st), derr(sizeof(int), st);
+    DevBuf dt(sizeof(MmaTile) * tiles.size(), st), derr(2 * sizeof(int), st);
     GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(MmaTile) * tiles.size(), cudaMemcpyHostToDevice, st));
-    GF_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), st));
+    GF_CUDA(cudaMemsetAsync(derr.p, 0, 2 * sizeof(int), st));
     MmaArgs a;
     a.B = B.as<__nv_bfloat16>();
     a.tiles = dt.as<MmaTile>();
@@ -503,6 +514,7 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     a.log2n1 = lg(n1); a.log2n2 = lg(n2);
     a.nkc = nkc; a.nnc = nnc; a.npad_last = npad_last;
     a.err = derr.as<int>();
+    a.queue = derr.as<int>() + 1;
     const size_t smem = 2 * (size_t)kStageBytes + 128 + 3 * kM * sizeof(float2);
     GF_CUDA(cudaFuncSetAttribute((const void *)k_dft_tcgen05, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<size_t>(tiles.size(), (size_t)ctx->sm_count);

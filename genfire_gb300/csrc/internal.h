@@ -13,6 +13,14 @@ struct genfire_recon {
     gf::ReconBase *impl;
 };
 
+// The handle behind genfire_recon_batch: member reconstructions (not owned)
+// and the instantiated graph of one iteration of all of them.
+struct genfire_recon_batch {
+    genfire_ctx *ctx;
+    std::vector<genfire_recon *> members;
+    cudaGraphExec_t exec = nullptr;
+};
+
 namespace gf {
 
 // ---------------------------------------------------------------- geometry
@@ -103,6 +111,9 @@ void recon_iterate(genfire_recon *r, int count);
 void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, double *Rarr, double *Rarr2,
                   bool on_device);
 void recon_destroy(genfire_recon *r);
+genfire_recon_batch *recon_batch_create(genfire_ctx *ctx, genfire_recon *const *members, int count);
+void recon_batch_iterate(genfire_recon_batch *b, int count);
+void recon_batch_destroy(genfire_recon_batch *b);
 void recon_profile(genfire_recon *r, int iterations, double *ms, double *bytes);
 
 // ---------------------------------------------------------------- projector

@@ -83,6 +83,7 @@ typedef struct genfire_params {
 
 typedef struct genfire_ctx genfire_ctx;
 typedef struct genfire_recon genfire_recon;
+typedef struct genfire_recon_batch genfire_recon_batch;
 
 /* ---- library ----------------------------------------------------------- */
 
@@ -193,6 +194,21 @@ genfire_status genfire_recon_result(genfire_recon *r, void *reconstruction, doub
                                     double *errR, double *Rarr, double *Rarr2,
                                     int32_t on_device);
 genfire_status genfire_recon_destroy(genfire_recon *r);
+
+/* Batches of independent reconstructions (problems of different sizes,
+ * precisions and projection counts) iterated together: one CUDA graph holds
+ * one iteration of every member as independent child graphs, so each launch
+ * runs all members' iterations concurrently on the device.  No counterpart in
+ * the reference, which reconstructs one object per call.  Every member must
+ * have been created on ctx; the batch does not own them: destroy the batch
+ * before any member, and do not iterate a member on its own while it is in a
+ * live batch.  genfire_recon_batch_iterate advances every member by count
+ * iterations (each member's total may not exceed its numIterations); results
+ * are read per member with genfire_recon_result. */
+genfire_status genfire_recon_batch_create(genfire_ctx *ctx, int32_t count, genfire_recon *const *members,
+                                          genfire_recon_batch **out);
+genfire_status genfire_recon_batch_iterate(genfire_recon_batch *b, int32_t count);
+genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b);
 
 /* Per-kernel timing of the iteration (tracing; the reference only prints
  * wall times, reconstruct.m:74,188-190).  Runs `iterations` further
