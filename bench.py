@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--rfactor-iters", type=int, default=50, help="iterations for the equal-R-factor comparison")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-problems leg")
+    ap.add_argument("--batch-steps", type=int, default=300, help="iterations per problem in the batched leg")
     ap.add_argument("--quick", action="store_true", help="small workload (for checking the script)")
     return ap.parse_args()
 
@@ -268,6 +270,20 @@ def run_ours(args, ws, rank, local, pg):
                "note": "one genfire_reconstruct call of %d iterations from host buffers: measuredK and support "
                        "copied in, reconstruction and errK copied out, setup included" % K}
 
+    # ---- FFT gridding (fillInFourierGrid, griddingMethod 1) on the same projections
+    pfm = params_for(G, w, G.PREC_MIXED, 1)
+    pfm.griddingMethod = 1
+    pfm.allowMultipleGridMatches = 1
+    ctx.grid_fft_device(pfm, d_proj.data_ptr(), angles, d_M32.data_ptr())             # warm-up
+    npairs, t_fft_grid = time_call(lambda: ctx.grid_fft_device(pfm, d_proj.data_ptr(), angles, d_M32.data_ptr()))
+    fft_grid = {"ms": t_fft_grid * 1e3, "pairs": int(npairs), "precision": "mixed",
+                "interpolationCutoffDistance": 0.125, "allowMultipleGridMatches": 1}
+
+    # ---- batched problems: one graph launch per iteration of all problems
+    batch = None
+    if not args.no_batch and rank == 0 and ws == 1:
+        batch = batch_leg(G, ctx, args.batch_steps, args.quick)
+
     # ---- roofline of the dominant kernel (live CUDA events per kernel)
     peak, peak_kind = measured_peaks()
     k = int(np.argmax(ms))
@@ -307,6 +323,8 @@ def run_ours(args, ws, rank, local, pg):
                     "volume_rel_l2_mixed_vs_fp64": vol_err, "volume_rel_l2_vs_ground_truth": gt_err},
         "gridded_points": int(np.sum(nk)),
         "e2e": e2e,
+        "fft_gridding": fft_grid,
+        "batch": batch,
         "roofline": roof,
         "cpu_baseline": cpu,
         "clocks": clk,
@@ -314,6 +332,44 @@ def run_ours(args, ws, rank, local, pg):
     }
     ctx.close()
     return res
+
+
+def batch_leg(G, ctx, K, quick):
+    """Independent problems of different sizes (the batched workload of
+    genfire_gb300.synth) iterated K times each: all problems per graph launch
+    (genfire_recon_batch) against the same problems iterated one after the
+    other; aggregate problem-iterations per second for both."""
+    from genfire_gb300 import synth
+
+    def proj(vol, angles, vectors):
+        return ctx.project(vol.astype(np.float64), angles, vectors=np.asarray(vectors, float).reshape(-1))
+    probs = synth.make_batch_workload(proj, count=4 if quick else 24, sizes=(48, 64) if quick else synth.BATCH_SIZES,
+                                      iters=K)
+    W = 3
+    recons = []
+    for w in probs:
+        p = params_for(G, w, G.PREC_MIXED, W + 2 * K)
+        M, _, _ = ctx.grid_dft(p, w["projections"], w["angles_in"], want_rec=False)
+        recons.append(ctx.recon(p, M, support=w["support"]))
+    b = G.ReconBatch(ctx, recons)
+    b.iterate(W)
+    t0 = time.perf_counter()
+    b.iterate(K)
+    t_batch = time.perf_counter() - t0
+    b.close()
+    t0 = time.perf_counter()
+    for r in recons:
+        r.iterate(K)
+    t_seq = time.perf_counter() - t0
+    for r in recons:
+        r.close()
+    n = len(probs)
+    return {"problems": n, "sizes": [w["D"] for w in probs], "projections": [int(w["projections"].shape[2]) for w in probs],
+            "iterations_per_problem": K, "precision": "mixed",
+            "batched_problem_iters_per_s": n * K / t_batch, "sequential_problem_iters_per_s": n * K / t_seq,
+            "batched_over_sequential": t_seq / t_batch, "batched_ms": t_batch * 1e3, "sequential_ms": t_seq * 1e3,
+            "note": "wall time with a stream synchronize at the end of each leg; one graph launch per batched "
+                    "iteration runs every problem's iteration as an independent child graph"}
 
 
 def cpu_baseline(w, d_M64):

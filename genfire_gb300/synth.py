@@ -136,3 +136,30 @@ def make_workload(name, projector, D=None, n_proj=None, atoms=None, seed_offset=
     return dict(name=name, vol=vol, support=support_mask(Dn, shape), angles=angles,
                 angles_in=np.asfortranarray(angles_in), projections=projs, vectors=w["vectors"], os=w["os"],
                 iters=w["iters"], D=Dn)
+
+
+BATCH_SIZES = (48, 64, 96, 128, 160, 192)
+
+
+def make_batch_workload(projector, count=24, seed=4, sizes=BATCH_SIZES, proj_range=(20, 80), iters=300):
+    """The batched workload: `count` independent problems with object sizes
+    drawn from `sizes`, 20-80 random-Euler projections each (theta in
+    [-70, 70]), one Gaussian atom (sigma 1.2, amplitude 1) per 1000 voxels in a
+    sphere of radius 0.4 D, Poisson noise at 1e4 counts per pixel, ZYZ axes,
+    oversampling 2.  Generation uses numpy.random.default_rng(1000 + seed)."""
+    rng = np.random.default_rng(1000 + seed)
+    out = []
+    for i in range(count):
+        D = int(rng.choice(sizes))
+        P = int(rng.integers(proj_range[0], proj_range[1] + 1))
+        shape = ("sphere", 0.4 * D)
+        na = max(1, D ** 3 // 1000)
+        cents = atom_centres(rng, na, shape)
+        vol = gaussian_volume(D, cents, np.ones(na), 1.2)
+        angles = angle_set(rng, ("euler", P, 70.0))
+        projs = np.asfortranarray(projector(vol, angles, ZYZ), dtype=np.float64)
+        projs = np.asfortranarray(poisson(rng, projs, 1e4))
+        out.append(dict(name="batch%d" % i, vol=vol, support=support_mask(D, shape), angles=angles,
+                        angles_in=np.asfortranarray(angles), projections=projs, vectors=ZYZ, os=2.0, iters=iters,
+                        D=D))
+    return out
