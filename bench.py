@@ -223,6 +223,7 @@ def run_ours(args, ws, rank, local, pg):
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         t_dr = float(t.item())
     names, ms, by = rec.profile(20)
+    tuned = rec.tuning()
     rec.close()
 
     # ---- DR loop, FP64
@@ -326,6 +327,9 @@ def run_ours(args, ws, rank, local, pg):
         "fft_gridding": fft_grid,
         "batch": batch,
         "roofline": roof,
+        "fft_pass_variants": {"F2": tuned[0], "F3": tuned[1], "I2": tuned[2],
+                              "legend": "autotuned at setup: 0 generic shared-memory engine, 1 register engine "
+                                        "one column per thread, 2 register engine two columns per thread"},
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": 7 * K,

@@ -35,6 +35,7 @@ EXPORTS = [
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
     "genfire_recon_batch_create", "genfire_recon_batch_iterate", "genfire_recon_batch_destroy",
+    "genfire_recon_tuning",
     "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc", "genfire_set_projector_interpolation",
     "genfire_rfactor_realspace",
     "genfire_centro_symmetricity", "genfire_hermitian_symmetrize", "genfire_make_kspace_indices",
@@ -99,6 +100,7 @@ def load():
         "genfire_recon_destroy": (C.c_int, [vp]),
         "genfire_recon_batch_create": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "genfire_recon_batch_iterate": (C.c_int, [vp, C.c_int32]),
+        "genfire_recon_tuning": (C.c_int, [vp, i32p]),
         "genfire_recon_batch_destroy": (C.c_int, [vp]),
         "genfire_recon_profile": (C.c_int, [vp, C.c_int32, dp, dp]),
         "genfire_profile_kernel_name": (C.c_char_p, [C.c_int32]),
@@ -427,6 +429,12 @@ class Recon:
         self.done += iterations
         names = [load().genfire_profile_kernel_name(k).decode() for k in range(7)]
         return names, ms, by
+
+    def tuning(self):
+        """Autotuned FFT-pass variants (F2, F3, I2): 0 generic, 1 / 2 register engine with 1 / 2 columns per thread."""
+        v = np.zeros(3, dtype=np.int32)
+        self.ctx.check(load().genfire_recon_tuning(self._h, ptr(v, C.c_int32)))
+        return [int(x) for x in v]
 
     def result_device(self, d_rec_ptr, d_errK_ptr=None):
         self.ctx.check(load().genfire_recon_result(self._h, C.c_void_p(d_rec_ptr),

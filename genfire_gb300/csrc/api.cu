@@ -290,6 +290,15 @@ genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b)
     return guarded(ctx, [&] { gf::recon_batch_destroy(b); });
 }
 
+genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants)
+{
+    if (!r || !variants) return GENFIRE_ERR_ARG;
+    int v[3];
+    gf::recon_tuning(r, v);
+    for (int i = 0; i < 3; ++i) variants[i] = v[i];
+    return GENFIRE_OK;
+}
+
 genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes)
 {
     if (!r) return GENFIRE_ERR_ARG;

@@ -53,16 +53,18 @@ template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
         h[t] = mk((T)std::cos(a), (T)std::sin(a));
     }
     if (np) {
+        // the packed table of length m = packed_length(n): W_m^x = W_n^(x * n / m)
+        const int m = packed_length(n), f = n / m;
         int L = 0;
-        while ((1 << L) < n) ++L;
+        while ((1 << L) < m) ++L;
         const int n8 = L / 3, rem = L % 3, nst = n8 + (rem ? 1 : 0);
         size_t o = (size_t)n;
         for (int st = 0, ns = 1; st < nst; ns *= (st < n8 ? 8 : (rem == 2 ? 4 : 2)), ++st) {
             const int R = st < n8 ? 8 : (rem == 2 ? 4 : 2);
             if (ns == 1) continue;
-            const int step = n / (ns * R);
+            const int step = m / (ns * R);
             for (int kk = 0; kk < ns; ++kk) {
-                for (int r = 1; r < R; ++r) h[o++] = h[(size_t)kk * r * step];
+                for (int r = 1; r < R; ++r) h[o++] = h[(size_t)kk * r * step * f];
                 h[o++] = mk((T)1, (T)0);  // pad
             }
         }
@@ -103,7 +105,7 @@ template <typename T, int N> static void set_reg_attrs()
 // float columns per thread.  The last needs unit column stride and 16-byte
 // aligned column pairs (even strides, aligned bases; tiles start at even
 // columns).
-enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2 };
+enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3 };
 
 template <typename T> static bool pair_capable(const ColPassArgs<T> &a)
 {
@@ -134,12 +136,15 @@ template <typename T, int N> static void rows_reg(const RowPassArgs<T> &a, bool 
     if (forward) k_row_r2c_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
     else k_row_c2r_reg<T, N><<<grid, N / 8 * W, reg_smem<T, N>(), st>>>(a);
 }
+// element offsets along the transform are 32-bit in the register passes
+template <typename T> static bool span_ok(const ColPassArgs<T> &a)
+{
+    return (long long)(a.pl.n - 1) * std::max(a.in_dim, a.out_dim) + 1 < (1LL << 32);
+}
 template <typename T> static bool reg_capable(const ColPassArgs<T> &a)
 {
-    // element offsets along the transform are 32-bit in the register passes
-    const long long span = (long long)(a.pl.n - 1) * std::max(a.in_dim, a.out_dim) + 1;
     const int n = a.pl.n;
-    return span < (1LL << 32) && (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024);
+    return span_ok(a) && (n == 64 || n == 128 || n == 256 || n == 512 || n == 1024);
 }
 template <typename T> static void col_reg_any(const ColPassArgs<T> &a, int other, cudaStream_t st, int nc)
 {
@@ -188,6 +193,7 @@ template <typename T> static void ensure_smem_attrs()
 template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
 {
     if (v == kColGeneric) return true;
+    if (v == kColMix) return span_ok(a) && mix_capable<T>(a.pl.n);
     if (!reg_capable(a)) return false;
     return v == kColReg1 || (v == kColReg2 && pair_capable(a));
 }
@@ -195,15 +201,19 @@ template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
 // Column pass launcher.  Without a tuned variant: two columns per thread in
 // the fused forward + constraint + inverse pass (two transforms per load),
 // one column per thread in the single-transform passes (twice the resident
-// warps), the generic engine for other lengths.
+// warps), the mixed-radix register engine for 3 or 5 times a power of two,
+// the generic engine for other lengths.
 template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st, int variant = kColAuto)
 {
     a.P = a.W + 1;
     if (variant == kColAuto || !col_variant_ok(a, variant)) {
-        if (!reg_capable(a)) variant = kColGeneric;
-        else variant = ((a.mode & 3) == 3 && pair_capable(a)) ? kColReg2 : kColReg1;
+        if (reg_capable(a)) variant = ((a.mode & 3) == 3 && pair_capable(a)) ? kColReg2 : kColReg1;
+        else if (col_variant_ok(a, kColMix)) variant = kColMix;
+        else variant = kColGeneric;
     }
-    if (variant == kColGeneric) {
+    if (variant == kColMix) {
+        if (!launch_col_mix<T>(a, other, st)) fail(GENFIRE_ERR_STATE, "internal: mixed-radix pass not available.");
+    } else if (variant == kColGeneric) {
         const size_t sm = tile_smem<T>(a.pl.n, a.W);
         dim3 grid(cdiv(a.ncols, a.W), other);
         k_colpass<T><<<grid, tile_threads(a.pl.n, a.W), sm, st>>>(a);
@@ -238,7 +248,7 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     GF_CUDA(cudaEventCreate(&e1));
     int best = kColAuto;
     float best_ms = 0;
-    for (int v : {kColGeneric, kColReg1, kColReg2}) {
+    for (int v : {kColGeneric, kColReg1, kColReg2, kColMix}) {
         if (!col_variant_ok(a, v)) continue;
         launch_colpass<T>(a, other, st, v);
         GF_CUDA(cudaEventRecord(e0, st));
@@ -259,7 +269,7 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
 template <typename T> static void launch_rows(RowPassArgs<T> a, bool forward, cudaStream_t st)
 {
     a.P = a.W + 1;
-    if (!try_rows_reg<T>(a, forward, st)) {
+    if (!try_rows_reg<T>(a, forward, st) && !launch_rows_mix<T>(a, forward, st)) {
         const size_t sm = tile_smem<T>(a.pl.n, a.W);
         const int pairs = (a.nrows + 1) / 2;
         dim3 grid(cdiv(pairs, a.W));
@@ -631,6 +641,7 @@ struct ReconBase {
     virtual int remaining() const = 0;
     virtual void advance() = 0;
     virtual void profile(int count, double *ms, double *bytes) = 0;
+    virtual void tuning(int *variants) const = 0;
     virtual void result(void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device) = 0;
 };
 
@@ -945,6 +956,10 @@ template <typename T> struct ReconT : ReconBase {
     }
 
     int remaining() const override { return p.numIterations - it_done; }
+    void tuning(int *v) const override
+    {
+        v[0] = vF2; v[1] = vF3; v[2] = vI2;
+    }
     void advance() override
     {
         ++it_done;
@@ -1040,6 +1055,7 @@ genfire_recon *recon_create(genfire_ctx *ctx, const genfire_params &p, const voi
 }
 
 void recon_iterate(genfire_recon *r, int count) { r->impl->iterate(count); }
+void recon_tuning(genfire_recon *r, int *variants) { r->impl->tuning(variants); }
 void recon_profile(genfire_recon *r, int count, double *ms, double *bytes) { r->impl->profile(count, ms, bytes); }
 void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device)
 {

@@ -12,6 +12,8 @@
 
 #include "fft.cuh"
 
+#include <type_traits>
+
 namespace gf {
 
 constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
@@ -43,12 +45,14 @@ template <int N> struct P2Plan {
 // compile-time offsets.
 template <int N, int W> struct ColLayout {   // the W columns interleaved, column fastest
     static constexpr int SIZE = (N + N / 8) * W;
+    static constexpr int CSTR = 1;               // distance between adjacent columns
     static __device__ __forceinline__ int idx(int i, int c) { return (i + (i >> 3)) * W + c; }
     static constexpr int stride(int S) { return (S % 8 == 0 ? S + S / 8 : S) * W; }
 };
 template <int N, int W> struct RowLayout {   // each column contiguous
     static constexpr int PC = N + N / 8;
     static constexpr int SIZE = PC * W;
+    static constexpr int CSTR = PC;
     static __device__ __forceinline__ int idx(int i, int c) { return c * PC + i + (i >> 3); }
     static constexpr int stride(int S) { return S % 8 == 0 ? S + S / 8 : S; }
 };
@@ -130,26 +134,28 @@ template <int N, class Lay, int S> __device__ __forceinline__ int out_base(int j
     return Lay::idx((jp - kk) * R + kk, c);
 }
 
-// register k of the NC adjacent columns at q[0 .. NC-1] (one 16-byte access
-// for two float columns; ColLayout keeps adjacent columns adjacent)
-template <typename T, int NC> __device__ __forceinline__ void st_cols(cplx<T> *q, const cplx<T> (&v)[NC][8], int k)
+// register k of the NC consecutive columns at q[c * Lay::CSTR] (one 16-byte
+// access for two adjacent float columns of a ColLayout)
+template <typename T, class Lay, int NC>
+__device__ __forceinline__ void st_cols(cplx<T> *q, const cplx<T> (&v)[NC][8], int k)
 {
-    if constexpr (NC == 2 && sizeof(T) == 4) {
+    if constexpr (NC == 2 && sizeof(T) == 4 && Lay::CSTR == 1) {
         *reinterpret_cast<float4 *>(q) = make_float4(v[0][k].x, v[0][k].y, v[1][k].x, v[1][k].y);
     } else {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) q[c] = v[c][k];
+        for (int c = 0; c < NC; ++c) q[c * Lay::CSTR] = v[c][k];
     }
 }
-template <typename T, int NC> __device__ __forceinline__ void ld_cols(const cplx<T> *q, cplx<T> (&v)[NC][8], int k)
+template <typename T, class Lay, int NC>
+__device__ __forceinline__ void ld_cols(const cplx<T> *q, cplx<T> (&v)[NC][8], int k)
 {
-    if constexpr (NC == 2 && sizeof(T) == 4) {
+    if constexpr (NC == 2 && sizeof(T) == 4 && Lay::CSTR == 1) {
         const float4 t = *reinterpret_cast<const float4 *>(q);
         v[0][k] = mk(t.x, t.y);
         v[1][k] = mk(t.z, t.w);
     } else {
 #pragma unroll
-        for (int c = 0; c < NC; ++c) v[c][k] = q[c];
+        for (int c = 0; c < NC; ++c) v[c][k] = q[c * Lay::CSTR];
     }
 }
 
@@ -163,7 +169,7 @@ __device__ __forceinline__ void store_stage(cplx<T> *s, const cplx<T> (&v)[NC][8
     for (int b = 0; b < NB; ++b) {
         cplx<T> *q = s + out_base<N, Lay, S>(j, c, b);
 #pragma unroll
-        for (int r = 0; r < R; ++r) st_cols<T, NC>(q + r * ST, v, b + r * NB);
+        for (int r = 0; r < R; ++r) st_cols<T, Lay, NC>(q + r * ST, v, b + r * NB);
     }
 }
 
@@ -173,7 +179,7 @@ __device__ __forceinline__ void load_stage(const cplx<T> *s, cplx<T> (&v)[NC][8]
 {
     constexpr int ST = Lay::stride(N / 8);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) ld_cols<T, NC>(s + in_base + k * ST, v, k);
+    for (int k = 0; k < 8; ++k) ld_cols<T, Lay, NC>(s + in_base + k * ST, v, k);
 }
 
 template <typename T, int N, class Lay, bool INV, int NC, int S = 0>
@@ -191,25 +197,30 @@ __device__ __forceinline__ void reg_fft(cplx<T> (&v)[NC][8], cplx<T> *sA, cplx<T
     }
 }
 
+// Accumulator of a thread's errK terms: FP32 for the MIXED passes (a handful
+// of terms per thread; the block and grid sums are FP64), FP64 for the FP64
+// passes.
+template <typename T> using ErrAcc = typename std::conditional<sizeof(T) == 8, double, float>::type;
+
 // Fourier constraint and errK terms on one shared-memory tile (see k_colpass);
-// returns this thread's errK terms (a handful per thread, summed in FP32; the
-// block and grid sums are FP64).
+// returns this thread's errK terms.
 template <typename T, class Lay>
-__device__ __forceinline__ float apply_table(cplx<T> *s, const ColPassArgs<T> &a, int tile, int W, int other)
+__device__ __forceinline__ ErrAcc<T> apply_table(cplx<T> *s, const ColPassArgs<T> &a, int tile, int W, int other)
 {
+    using A_ = ErrAcc<T>;
     const int cid0 = other * a.h1 + tile * W;
     const int cid1 = min(cid0 + W, other * a.h1 + a.h1);
     const int e0 = a.tab_off[cid0], e1 = a.tab_off[cid1];
     const int ci = *a.cidx;
-    float acc = 0.f;
+    A_ acc = 0;
     for (int e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
         const TabEntry<T> t = a.tab[e];
         const int q3 = t.pos & 0xFFFF, cl = t.pos >> 16;
         const int si = Lay::idx(q3, cl);
         const cplx<T> k = s[si];
-        const float mk_ = (float)sqrt(k.x * k.x + k.y * k.y);
-        if (t.eflags & 1u) acc += fabsf(mk_ - (float)sqrt(t.Mq.x * t.Mq.x + t.Mq.y * t.Mq.y));
-        if (t.eflags & 2u) acc += fabsf(mk_ - (float)sqrt(t.Mmq.x * t.Mmq.x + t.Mmq.y * t.Mmq.y));
+        const A_ mk_ = (A_)sqrt(k.x * k.x + k.y * k.y);
+        if (t.eflags & 1u) acc += fabs(mk_ - (A_)sqrt(t.Mq.x * t.Mq.x + t.Mq.y * t.Mq.y));
+        if (t.eflags & 2u) acc += fabs(mk_ - (A_)sqrt(t.Mmq.x * t.Mmq.x + t.Mmq.y * t.Mmq.y));
         const bool eq = (t.cq >> ci) & 1u, emq = (t.cmq >> ci) & 1u;
         if (eq || emq) {
             const cplx<T> A = eq ? t.Mq : k;
@@ -223,7 +234,7 @@ __device__ __forceinline__ float apply_table(cplx<T> *s, const ColPassArgs<T> &a
 // CTA sum of the per-thread errK terms: warp sums in FP32 (a few terms per
 // thread), the per-warp partials in FP64.  FP64 arithmetic is kept to one warp
 // because its throughput on this part is a small fraction of FP32's.
-__device__ __forceinline__ void block_partial(float acc, double *out)
+template <typename A_> __device__ __forceinline__ void block_partial(A_ acc, double *out)
 {
     __shared__ double red[32];
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -318,7 +329,7 @@ __global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_c
         }
     }
     int buf = 0;
-    float err = 0.f;
+    ErrAcc<T> err = 0;
     if (a.mode & 1) reg_fft<T, N, Lay, false, NC>(v, sA, sB, buf, j, c, in_base, twp);
     if (a.mode & 2) {
         if (a.mode & 1) {
@@ -458,12 +469,32 @@ template <typename T, int N> constexpr size_t reg_smem()
     return 2 * (size_t)ColLayout<N, reg_width<T>(N)>::SIZE * sizeof(cplx<T>);
 }
 
-// Size of the packed table appended to the n-entry twiddle table (0 when n
-// is not a power of two of at least 8); the host fills it in the order of
-// P2Plan::twoff.
+// Mixed-radix register passes (dr_mix.cu) for n = N1 * N2, N1 in {3, 5}:
+// each returns false when n is not covered.
+template <typename T> bool mix_capable(int n);
+template <typename T> bool launch_col_mix(const ColPassArgs<T> &a, int other, cudaStream_t st);
+template <typename T> bool launch_rows_mix(const RowPassArgs<T> &a, bool forward, cudaStream_t st);
+
+// The power-of-two length whose packed table follows the n-entry twiddle
+// table: n itself, or N2 of n = N1 * N2 (N1 in {3, 5}, N2 >= 64); 0 if none.
+inline int packed_length(int n)
+{
+    if (n >= 8 && !(n & (n - 1))) return n;
+    for (int f : {3, 5})
+        if (n % f == 0) {
+            const int m = n / f;
+            if (m >= 64 && !(m & (m - 1))) return m;
+        }
+    return 0;
+}
+
+// Size of the packed table appended to the n-entry twiddle table (0 when
+// packed_length(n) is 0); the host fills it in the order of P2Plan::twoff
+// for the length packed_length(n).
 inline int packed_twiddle_count(int n)
 {
-    if (n < 8 || (n & (n - 1))) return 0;
+    n = packed_length(n);
+    if (!n) return 0;
     int L = 0;
     while ((1 << L) < n) ++L;
     const int n8 = L / 3, rem = L % 3, nst = n8 + (rem ? 1 : 0);

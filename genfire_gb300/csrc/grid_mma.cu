@@ -160,6 +160,24 @@ __device__ __forceinline__ float2 phase_exact(int a, float w, double inv_n)
 }
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 
+// v * 2^-sh as a float for |v| < 2^62 and 1 <= sh <= 125, from three 23-bit
+// chunks, each converted exactly by the 2^23 bias trick (0x4B000000 | c is the
+// float 2^23 + c) and combined with FP32 fused multiply-adds, smallest first.
+// A 64-bit integer conversion would issue on the FP64 pipe, which this part
+// runs at 2 operations per clock per SM.
+__device__ __forceinline__ float i64_scaled(long long v, int sh)
+{
+    const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+    const float c0 = __int_as_float(0x4B000000 | (unsigned)(a & 0x7FFFFFull)) - 8388608.f;
+    const float c1 = __int_as_float(0x4B000000 | (unsigned)((a >> 23) & 0x7FFFFFull)) - 8388608.f;
+    const float c2 = __int_as_float(0x4B000000 | (unsigned)((a >> 46) & 0x7FFFFFull)) - 8388608.f;
+    auto p2 = [](int e) { return __int_as_float((127 + e) << 23); };  // 2^e, -126 < e < 128
+    float f = c0 * p2(-sh);
+    f = fmaf(c1, p2(23 - sh), f);
+    f = fmaf(c2, p2(46 - sh), f);
+    return v < 0 ? -f : f;
+}
+
 // exp(-2 pi i * a * w / 2^t) with the phase reduced exactly in integer
 // arithmetic: w = m * 2^e (m the 24-bit significand), a * m is exact in 64
 // bits, and the fraction of a*m*2^(e-t) is its low (t-e) bits.  No FP64 (the
@@ -179,12 +197,11 @@ __device__ __forceinline__ float2 phase_pow2(int a, float w, int t)
         if (sh <= 0) {
             f = 0.f;  // an integer number of turns
         } else if (sh >= 62) {
-            f = (float)P * __int_as_float((127 - (sh > 125 ? 125 : sh)) << 23);
-            if (sh > 125) f = 0.f;
+            f = sh > 125 ? 0.f : i64_scaled(P, sh);  // |P| < 2^47: below 2^-15 turns
         } else {
             long long low = P & ((1LL << sh) - 1);
             if (low >= (1LL << (sh - 1))) low -= (1LL << sh);  // to [-1/2, 1/2) turns
-            f = (float)low * __int_as_float((127 - sh) << 23);
+            f = i64_scaled(low, sh);
         }
     }
     float sv, cv;

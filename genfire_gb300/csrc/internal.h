@@ -115,6 +115,7 @@ genfire_recon_batch *recon_batch_create(genfire_ctx *ctx, genfire_recon *const *
 void recon_batch_iterate(genfire_recon_batch *b, int count);
 void recon_batch_destroy(genfire_recon_batch *b);
 void recon_profile(genfire_recon *r, int iterations, double *ms, double *bytes);
+void recon_tuning(genfire_recon *r, int *variants);
 
 // ---------------------------------------------------------------- projector
 // Trilinear projections of a volume view (base pointer, strides vs1 = stride

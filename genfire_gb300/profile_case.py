@@ -43,7 +43,8 @@ def main(argv):
     r = ctx.recon(p, M)
     t0 = time.time()
     r.iterate(iters)
-    print("iterations", iters, "wall %.4f s" % (time.time() - t0), "measured points", np.count_nonzero(M))
+    print("iterations", iters, "wall %.4f s" % (time.time() - t0), "measured points", np.count_nonzero(M),
+          "pass variants (F2, F3, I2)", r.tuning())
 
 
 if __name__ == "__main__":

@@ -217,6 +217,14 @@ genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b);
  * stream.  For kernel k < GENFIRE_PROFILE_KERNELS, ms[k] receives its mean
  * duration and bytes[k] its algorithmic HBM traffic per launch (compulsory
  * reads plus writes); genfire_profile_kernel_name(k) names it. */
+/* The FFT-pass variants the autotuner chose for this reconstruction (it times
+ * each candidate on the problem's own buffers at creation; the environment
+ * variable GENFIRE_AUTOTUNE=0 keeps the built-in choice): variants[0..2] for
+ * the dim-2 forward, the fused dim-3 and the dim-2 inverse pass; 0 = generic
+ * shared-memory engine, 1 = register-resident, one column per thread,
+ * 2 = register-resident, two columns per thread, -1 = built-in choice. */
+genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants);
+
 #define GENFIRE_PROFILE_KERNELS 7
 genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes);
 const char *genfire_profile_kernel_name(int32_t k);
