@@ -209,10 +209,12 @@ __device__ __forceinline__ float2 phase_pow2(int a, float w, int t)
     return make_float2(cv, sv);
 }
 
-// exact phase for any n: the power-of-two form when log2n >= 0, else FP64
-__device__ __forceinline__ float2 phase_any(int a, float w, int log2n, double inv_n)
+// exact phase: the integer form for power-of-two n (POW2, chosen at compile
+// time so the FP64 form is not speculated alongside), else FP64
+template <bool POW2> __device__ __forceinline__ float2 phase_any(int a, float w, int log2n, double inv_n)
 {
-    return log2n >= 0 ? phase_pow2(a, w, log2n) : phase_exact(a, w, inv_n);
+    if constexpr (POW2) return phase_pow2(a, w, log2n);
+    else return phase_exact(a, w, inv_n);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem)
@@ -244,6 +246,7 @@ struct MmaArgs {
     int *queue;               // next tile to take (starts at 0)
 };
 
+template <bool POW2>
 __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
 {
     using namespace umma;
@@ -305,8 +308,8 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
             const int N = (nc == a.nnc - 1) ? a.npad_last : kNC;
             const uint32_t idesc = idesc_bf16(kM, N);
             // A anchors for this thread: S = E_u(amin + 8h), rotations by 1 and by 32
-            float2 S = row_ok ? phase_any(amin + 8 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
-            const float2 w1 = phase_any(1, uj, a.log2n1, inv1), w32 = phase_any(32, uj, a.log2n1, inv1);
+            float2 S = row_ok ? phase_any<POW2>(amin + 8 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
+            const float2 w1 = phase_any<POW2>(1, uj, a.log2n1, inv1), w32 = phase_any<POW2>(32, uj, a.log2n1, inv1);
             const __nv_bfloat16 *Bp = a.B + ((size_t)(tl.proj * a.nnc + nc) * a.nkc) * 2 * kBTile;
             for (int kc = 0; kc < a.nkc; ++kc) {
                 const int s = kc & 1;
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                 const int quarter = N / 4;               // columns per warp quarter (multiple of 16)
                 const int c0 = equart * quarter;
                 const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-                const float2 v1 = phase_any(1, vj, a.log2n2, inv2);
+                const float2 v1 = phase_any<POW2>(1, vj, a.log2n2, inv2);
                 for (int c = 0; c < quarter; c += 32) {
                     const bool two = c + 16 < quarter;   // warp-uniform
                     uint32_t re0[16], im0[16], re1[16], im1[16];
@@ -409,8 +412,8 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                         tmem_ld16(tmem + lane_base + 256u + col + 16u, im1);
                     }
                     const int b0 = bmin + nc * kNC + c0 + c;
-                    const float2 an0 = erow_ok ? phase_any(b0, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
-                    const float2 an1 = (erow_ok && two) ? phase_any(b0 + 16, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
+                    const float2 an0 = erow_ok ? phase_any<POW2>(b0, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
+                    const float2 an1 = (erow_ok && two) ? phase_any<POW2>(b0 + 16, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
                     tmem_wait_ld();
                     float2 h0 = make_float2(__uint_as_float(re0[15]), __uint_as_float(im0[15]));
 #pragma unroll
@@ -533,9 +536,12 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     a.err = derr.as<int>();
     a.queue = derr.as<int>() + 1;
     const size_t smem = 2 * (size_t)kStageBytes + 128 + 3 * kM * sizeof(float2);
-    GF_CUDA(cudaFuncSetAttribute((const void *)k_dft_tcgen05, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const bool pow2 = a.log2n1 >= 0 && a.log2n2 >= 0;
+    const void *kern = pow2 ? (const void *)k_dft_tcgen05<true> : (const void *)k_dft_tcgen05<false>;
+    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<size_t>(tiles.size(), (size_t)ctx->sm_count);
-    k_dft_tcgen05<<<grid, kThreads, smem, st>>>(a);
+    if (pow2) k_dft_tcgen05<true><<<grid, kThreads, smem, st>>>(a);
+    else k_dft_tcgen05<false><<<grid, kThreads, smem, st>>>(a);
     GF_CHECK_LAUNCH();
     int herr = 0;
     GF_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
