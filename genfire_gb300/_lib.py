@@ -32,6 +32,7 @@ EXPORTS = [
     "genfire_abi_version", "genfire_status_string", "genfire_params_init", "genfire_grid_size",
     "genfire_create", "genfire_destroy", "genfire_last_error", "genfire_stream",
     "genfire_grid_dft", "genfire_grid_dft_device", "genfire_grid_fft", "genfire_grid_fft_device",
+    "genfire_grid_profile",
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
     "genfire_recon_batch_create", "genfire_recon_batch_iterate", "genfire_recon_batch_destroy",
@@ -92,6 +93,7 @@ def load():
         "genfire_grid_dft": (C.c_int, [vp, pp, dp, dp, vp, vp, i64p]),
         "genfire_grid_dft_device": (C.c_int, [vp, pp, vp, dp, vp, vp, i64p]),
         "genfire_grid_fft": (C.c_int, [vp, pp, dp, dp, vp, vp, i64p]),
+        "genfire_grid_profile": (C.c_int, [vp, pp, vp, dp, vp, dp]),
         "genfire_grid_fft_device": (C.c_int, [vp, pp, vp, dp, vp, vp, i64p]),
         "genfire_reconstruct": (C.c_int, [vp, pp, vp, up, up, vp, dp, dp, vp, dp, dp, dp, dp]),
         "genfire_recon_create": (C.c_int, [vp, pp, vp, vp, vp, vp, vp, vp, C.c_int32, C.POINTER(C.c_void_p)]),
@@ -215,6 +217,14 @@ class Context:
                                                   C.c_void_p(d_rec_ptr) if d_rec_ptr else None,
                                                   ptr(nk, C.c_int64)))
         return nk
+
+    def grid_profile(self, p, d_proj_ptr, angles, d_M_ptr):
+        """Device ms of the gridding stages: selection, DFT stage, DFT kernel, sums, finalize, recIFFT."""
+        A = fortran(angles, np.float64)
+        ms = np.zeros(6)
+        self.check(load().genfire_grid_profile(self._h, C.byref(p), C.c_void_p(d_proj_ptr), ptr(A, C.c_double),
+                                               C.c_void_p(d_M_ptr), ptr(ms, C.c_double)))
+        return dict(zip(("selection", "dft_stage", "dft_kernel", "sums", "finalize", "rec_ifft"), ms.tolist()))
 
     def grid_fft(self, p, projections, angles, want_rec=True):
         """fillInFourierGrid (griddingMethod 1): (measuredK m^3, recIFFT or None, gridded pairs)."""

@@ -187,6 +187,21 @@ genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p, const
     });
 }
 
+genfire_status genfire_grid_profile(genfire_ctx *ctx, const genfire_params *p, const double *d_projections,
+                                    const double *angles, void *d_measuredK, double *stage_ms)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        need(d_projections, "projections");
+        need(angles, "angles");
+        need(d_measuredK, "measuredK");
+        need(stage_ms, "stage_ms");
+        gf::check_params(*p, true);
+        gf::grid_dft(ctx, *p, d_projections, angles, d_measuredK, nullptr, nullptr, stage_ms);
+    });
+}
+
 genfire_status genfire_grid_fft_device(genfire_ctx *ctx, const genfire_params *p, const double *d_projections,
                                        const double *angles, void *d_measuredK, void *d_recIFFT, int64_t *npairs)
 {

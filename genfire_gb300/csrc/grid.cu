@@ -8,14 +8,17 @@
 //   3. k_sel_write   ordered compaction: (index, D, u, v) in ascending index
 //                    order within each projection, i.e. the order of find()
 //   4. k_dft         F_j = sum_b E_v(j,b) sum_a E_u(j,a) P(a,b) per point
-//   5. k_accum       one launch per projection, in projection order: weighted
-//                    sums in FP64 and the exact-hit overwrite, so repeated
-//                    points accumulate in the reference's order and the last
-//                    exact hit wins (fillInFourierGrid_DFT.m:268-291)
+//   5. k_accum_runs  the entries (projection-major) sorted stably by grid
+//                    index; each run of one grid point sums its contributions
+//                    in FP64 in projection order and keeps the last exact hit,
+//                    the reference's accumulation order
+//                    (fillInFourierGrid_DFT.m:268-291), in one launch
 //   6. k_finalize    FS = sum(w F) / sum(w), exact override, CentroSymmetricity
 //                    mirror, cast to the output precision
 #include "fft.cuh"
 #include "internal.h"
+
+#include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
 #include <cstring>
@@ -154,11 +157,18 @@ void check_params(const genfire_params &p, bool need_projs)
 // ===========================================================================
 // selection kernels
 // ===========================================================================
+// The thresholds are FP32 values chosen so the FP32 comparisons decide
+// exactly as the reference's comparisons in double do (this part's FP64 pipe
+// issues 2 operations per clock per SM, and a double comparison per candidate
+// would bound the selection): for a float D, D < cutoff in double holds iff
+// D < cut_lt, the smallest float not below cutoff; n/2 is exact in FP32.
 struct SelParams {
     int lo1, lo2, lo3, l1, l2;
     int nrows;    // l2 * l3 rows of the gridded index space
     int nchunks;  // CTAs per projection
-    double cutoff, half1, half2;
+    float cut_lt;      // D < cutoff  <=>  D < cut_lt
+    float cut_margin;  // cutoff + 0.01 in FP32: the candidate-interval half width
+    float half1, half2;
 };
 
 // Rows (k2, k3) of the gridded index space are the work units: the points of
@@ -176,7 +186,7 @@ __device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp,
                                          float &D, float &u, float &v)
 {
     D = fabsf(__fadd_rn(__fadd_rn(__fmul_rn(K1, g.h[0]), __fmul_rn(K2, g.h[1])), __fmul_rn(K3, g.h[2])));
-    if (!((double)D < sp.cutoff)) return false;
+    if (!(D < sp.cut_lt)) return false;
     const float s = __fadd_rn(__fadd_rn(__fmul_rn(K1, g.nrm[0]), __fmul_rn(K2, g.nrm[1])), __fmul_rn(K3, g.nrm[2]));
     const float t = __fdiv_rn(__fsub_rn(0.0f, s), g.nsq);
     float b[3] = {__fadd_rn(K1, __fmul_rn(t, g.nrm[0])), __fadd_rn(K2, __fmul_rn(t, g.nrm[1])),
@@ -198,7 +208,7 @@ __device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp,
     }
     u = b[0];
     v = b[1];
-    return fabs((double)b[0]) <= sp.half1 && fabs((double)b[1]) <= sp.half2;
+    return fabsf(b[0]) <= sp.half1 && fabsf(b[1]) <= sp.half2;
 }
 
 // Candidate k1 range [k1a, k1b] of row (K2, K3): every k1 with
@@ -208,7 +218,7 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
 {
     const int lo = sp.lo1, hi = sp.lo1 + sp.l1 - 1;
     const float x = -(K2 * g.h[1] + K3 * g.h[2]);
-    const float c = (float)sp.cutoff + 0.01f;
+    const float c = sp.cut_margin;
     const float h1 = g.h[0];
     k1a = lo;
     k1b = hi;
@@ -436,30 +446,49 @@ __global__ void __launch_bounds__(256) k_dft(const T *__restrict__ proj, int D1,
 // ===========================================================================
 // accumulation, average, mirror
 // ===========================================================================
-template <typename T>
-__global__ void k_accum(const uint32_t *__restrict__ ind, const float *__restrict__ dist,
-                        const cplx<T> *__restrict__ F, long long j0, long long nj, double2 *__restrict__ num,
-                        double *__restrict__ wsum, double2 *__restrict__ ex, uint8_t *__restrict__ hx)
+// One pass over the entries sorted (stably) by grid index: the first entry of
+// each run sums the run's contributions in their order -- projection order --
+// and keeps the last exact hit.  Grid points in no run keep the cleared weight
+// sum and flag.
+__global__ void k_iota(uint32_t *__restrict__ v, long long n)
 {
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nj; j += (long long)gridDim.x * blockDim.x) {
-        const long long o = j0 + j;
-        const uint32_t li = ind[o];
-        const double d = (double)dist[o];
-        const cplx<T> f = F[o];
-        if (d < 1e-7) {
-            ex[li] = make_double2((double)f.x, (double)f.y);
-            hx[li] = 1;
-        } else {
-            // num is not cleared beforehand: a zero weight sum marks a point
-            // no earlier projection touched (every weight is positive)
-            const double wgt = 1.0 / d;
-            const double w0 = wsum[li];
-            double2 a = make_double2(0.0, 0.0);
-            if (w0 != 0.0) a = num[li];
-            a.x += (double)f.x * wgt;
-            a.y += (double)f.y * wgt;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        v[i] = (uint32_t)i;
+}
+
+template <typename T>
+__global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order,
+                             const float *__restrict__ dist, const cplx<T> *__restrict__ F, long long n,
+                             double2 *__restrict__ num, double *__restrict__ wsum, double2 *__restrict__ ex,
+                             uint8_t *__restrict__ hx)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const uint32_t li = keys[i];
+        if (i > 0 && keys[i - 1] == li) continue;  // not the start of a run
+        double2 a = make_double2(0.0, 0.0), e = a;
+        double w = 0.0;
+        bool hit = false;
+        for (long long t = i; t < n && keys[t] == li; ++t) {
+            const uint32_t o = order[t];
+            const double d = (double)dist[o];
+            const cplx<T> f = F[o];
+            if (d < 1e-7) {
+                e = make_double2((double)f.x, (double)f.y);
+                hit = true;
+            } else {
+                const double wgt = 1.0 / d;
+                a.x += (double)f.x * wgt;
+                a.y += (double)f.y * wgt;
+                w += wgt;
+            }
+        }
+        if (w != 0.0) {
             num[li] = a;
-            wsum[li] = w0 + wgt;
+            wsum[li] = w;
+        }
+        if (hit) {
+            ex[li] = e;
+            hx[li] = 1;
         }
     }
 }
@@ -487,18 +516,34 @@ __global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ nu
                                                   const double2 *__restrict__ ex, const uint8_t *__restrict__ hx,
                                                   GridSpec g, int n1, int n2, int centro, cplx<TO> *__restrict__ M)
 {
-    __shared__ int list[256];
+    constexpr int KPT = 2;  // points per thread (independent loads in flight)
+    __shared__ int list[256 * KPT];
     __shared__ int cnt;
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
     const int c2 = blockIdx.y, c3 = blockIdx.z;
     const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
-    const int c1 = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c1 < n1) {
-        bool cj;
-        const long long li = src_index(g, n1, n2, centro, c1, c2, c3, cj);
-        if (hx[li] || wsum[li] > 0) list[atomicAdd(&cnt, 1)] = c1;
-        else M[row + c1] = mk((TO)0, cj ? -(TO)0 : (TO)0);
+    {
+        long long li[KPT];
+        bool cj[KPT], in[KPT];
+        uint8_t h[KPT];
+        long long wb[KPT];
+#pragma unroll
+        for (int q = 0; q < KPT; ++q) {
+            const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
+            in[q] = c1 < n1;
+            li[q] = in[q] ? src_index(g, n1, n2, centro, c1, c2, c3, cj[q]) : 0;
+            h[q] = in[q] ? hx[li[q]] : 0;
+            // the weight sum is >= 0: positive iff its bits, as an integer, are (no FP64 compare)
+            wb[q] = in[q] ? reinterpret_cast<const long long *>(wsum)[li[q]] : 0;
+        }
+#pragma unroll
+        for (int q = 0; q < KPT; ++q) {
+            if (!in[q]) continue;
+            const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
+            if (h[q] || wb[q] > 0) list[atomicAdd(&cnt, 1)] = c1;
+            else M[row + c1] = mk((TO)0, cj[q] ? -(TO)0 : (TO)0);
+        }
     }
     __syncthreads();
     const int m = cnt;
@@ -506,16 +551,22 @@ __global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ nu
         const int c = list[i];
         bool cj;
         const long long li = src_index(g, n1, n2, centro, c, c2, c3, cj);
-        double2 v;
         if (hx[li]) {
-            v = ex[li];
-        } else {
+            const double2 v = ex[li];
+            M[row + c] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
+        } else if constexpr (sizeof(TO) == 8) {
             const double ws = wsum[li];
-            v = num[li];
+            double2 v = num[li];
             v.x /= ws;
             v.y /= ws;
+            M[row + c] = mk(v.x, cj ? -v.y : v.y);
+        } else {
+            // single-precision output: the average is formed in FP32 from the FP64 sums
+            const float ws = (float)wsum[li];
+            const double2 v = num[li];
+            const float x = __fdiv_rn((float)v.x, ws), y = __fdiv_rn((float)v.y, ws);
+            M[row + c] = mk((TO)x, (TO)(cj ? -y : y));
         }
-        M[row + c] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
     }
 }
 
@@ -620,7 +671,10 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     sp.lo1 = g.lo1; sp.lo2 = g.lo2; sp.lo3 = g.lo3; sp.l1 = g.l1; sp.l2 = g.l2;
     sp.nrows = g.l2 * g.l3;
     sp.nchunks = (int)cdiv(sp.nrows, kSelChunk);
-    sp.cutoff = cutoff; sp.half1 = n1 / 2.0; sp.half2 = n2 / 2.0;
+    sp.cut_lt = (float)cutoff;
+    if ((double)sp.cut_lt < cutoff) sp.cut_lt = std::nextafter(sp.cut_lt, INFINITY);
+    sp.cut_margin = (float)cutoff + 0.01f;
+    sp.half1 = (float)(n1 / 2.0); sp.half2 = (float)(n2 / 2.0);
     DevBuf dgeo(sizeof(ProjGeom) * P, st);
     GF_CUDA(cudaMemcpyAsync(dgeo.p, geo.data(), sizeof(ProjGeom) * P, cudaMemcpyHostToDevice, st));
     DevBuf counts(sizeof(int) * (size_t)sp.nchunks * P, st), totals(sizeof(long long) * P, st);
@@ -649,11 +703,38 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     GF_CUDA(cudaStreamSynchronize(st));  // keeps the host-side staging buffers alive until the copies ran
 }
 
+// CUDA events on the context stream between the stages of a gridding call
+struct StageEvents {
+    std::vector<cudaEvent_t> ev;
+    StageEvents(int n, bool on)
+    {
+        if (!on) return;
+        ev.resize(n);
+        for (auto &e : ev) GF_CUDA(cudaEventCreate(&e));
+    }
+    ~StageEvents()
+    {
+        for (auto &e : ev) cudaEventDestroy(e);
+    }
+    void mark(int i, cudaStream_t st)
+    {
+        if (!ev.empty()) GF_CUDA(cudaEventRecord(ev[i], st));
+    }
+    double ms(int a, int b)
+    {
+        float t = 0;
+        GF_CUDA(cudaEventElapsedTime(&t, ev[a], ev[b]));
+        return t;
+    }
+};
+
 template <typename T>
 static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
-                       void *d_M, void *d_rec, int64_t *nk_out)
+                       void *d_M, void *d_rec, int64_t *nk_out, double *stage_ms)
 {
     cudaStream_t st = ctx->stream;
+    StageEvents se(8, stage_ms != nullptr);
+    se.mark(0, st);
     const int D1 = p.Dim1, D2 = p.Dim2, P = p.NumProjs;
     const int n1 = oversampled(D1, p.oversamplingRatio), n2 = oversampled(D2, p.oversamplingRatio);
     const GridSpec g = make_grid(n1, n2, p.DFT_CentroSymmetricity);
@@ -664,12 +745,14 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     select_points(ctx, g, p.interpolationCutoffDistance, n1, n2, geo, sel);
     if (nk_out)
         for (int i = 0; i < P; ++i) nk_out[i] = sel.nk[i];
+    se.mark(1, st);
 
     DevBuf F(sizeof(cplx<T>) * (size_t)std::max<long long>(sel.total, 1), st);
+    double dft_kernel_ms = 0;
     if (sizeof(T) == sizeof(float)) {
         // MIXED: split-BF16 tensor-core DFT (grid_mma.cu)
         dft_tcgen05(ctx, d_proj, D1, D2, n1, n2, P, sel.nk, sel.off, sel.u.as<float>(), sel.v.as<float>(),
-                    reinterpret_cast<float2 *>(F.p));
+                    reinterpret_cast<float2 *>(F.p), stage_ms ? &dft_kernel_ms : nullptr);
     } else {
         // FP64: kDftJ consecutive points of one projection per CTA
         std::vector<DftTile> tiles;
@@ -680,40 +763,68 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
         if (!tiles.empty()) {
             DevBuf dt(sizeof(DftTile) * tiles.size(), st);
             GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(DftTile) * tiles.size(), cudaMemcpyHostToDevice, st));
+            se.mark(6, st);
             k_dft<double><<<(unsigned)tiles.size(), 256, 0, st>>>(d_proj, D1, D2, n1, n2, dt.as<DftTile>(),
                                                                    sel.u.as<float>(), sel.v.as<float>(),
                                                                    reinterpret_cast<double2 *>(F.p));
             GF_CHECK_LAUNCH();
+            se.mark(7, st);
             GF_CUDA(cudaStreamSynchronize(st));
+            if (stage_ms) dft_kernel_ms = se.ms(6, 7);
         }
     }
+    se.mark(2, st);
 
     // weighted average in FP64, projection by projection
     const size_t G = (size_t)g.total;
     DevBuf num(sizeof(double2) * G, st), wsum(sizeof(double) * G, st), ex(sizeof(double2) * G, st), hx(G, st);
     GF_CUDA(cudaMemsetAsync(wsum.p, 0, wsum.bytes, st));  // num and ex are read only where wsum / hx are set
     GF_CUDA(cudaMemsetAsync(hx.p, 0, hx.bytes, st));
-    for (int i = 0; i < P; ++i) {
-        if (sel.nk[i] == 0) continue;
-        k_accum<T><<<grid_for(ctx, sel.nk[i], 256), 256, 0, st>>>(
-            sel.ind.as<uint32_t>(), sel.dist.as<float>(), F.as<cplx<T>>(), sel.off[i], sel.nk[i],
-            num.as<double2>(), wsum.as<double>(), ex.as<double2>(), hx.as<uint8_t>());
+    if (sel.total > 0) {
+        // stable radix sort of (grid index, entry) keeps projection order within a grid point
+        const long long n = sel.total;
+        int bits = 1;
+        while (bits < 32 && (1ull << bits) < (unsigned long long)G) ++bits;
+        DevBuf keys(sizeof(uint32_t) * n, st), vin(sizeof(uint32_t) * n, st), vout(sizeof(uint32_t) * n, st);
+        k_iota<<<grid_for(ctx, n, 256), 256, 0, st>>>(vin.as<uint32_t>(), n);
+        GF_CHECK_LAUNCH();
+        size_t tb = 0;
+        GF_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tb, sel.ind.as<uint32_t>(), keys.as<uint32_t>(),
+                                                vin.as<uint32_t>(), vout.as<uint32_t>(), n, 0, bits, st));
+        DevBuf tmp(std::max<size_t>(tb, 1), st);
+        GF_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, sel.ind.as<uint32_t>(), keys.as<uint32_t>(),
+                                                vin.as<uint32_t>(), vout.as<uint32_t>(), n, 0, bits, st));
+        k_accum_runs<T><<<grid_for(ctx, n, 256), 256, 0, st>>>(keys.as<uint32_t>(), vout.as<uint32_t>(),
+                                                                sel.dist.as<float>(), F.as<cplx<T>>(), n,
+                                                                num.as<double2>(), wsum.as<double>(),
+                                                                ex.as<double2>(), hx.as<uint8_t>());
         GF_CHECK_LAUNCH();
     }
-    k_finalize<T><<<dim3(cdiv(n1, 256), n2, n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
+    se.mark(3, st);
+    k_finalize<T><<<dim3(cdiv(n1, 512), n2, n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
                                                                ex.as<double2>(), hx.as<uint8_t>(), g, n1, n2,
                                                                p.DFT_CentroSymmetricity,
                                                                reinterpret_cast<cplx<T> *>(d_M));
     GF_CHECK_LAUNCH();
+    se.mark(4, st);
     if (d_rec) rec_ifft(ctx, p.precision, d_M, n1, n2, D1, D2, d_rec);
+    se.mark(5, st);
     GF_CUDA(cudaStreamSynchronize(st));
+    if (stage_ms) {
+        stage_ms[0] = se.ms(0, 1);  // selection
+        stage_ms[1] = se.ms(1, 2);  // DFT stage (operand preparation and the DFT kernel)
+        stage_ms[2] = dft_kernel_ms;  // the DFT kernel alone
+        stage_ms[3] = se.ms(2, 3);  // weighted sums
+        stage_ms[4] = se.ms(3, 4);  // average, centro mirror, cast
+        stage_ms[5] = se.ms(4, 5);  // recIFFT
+    }
 }
 
 void grid_dft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles, void *d_M,
-              void *d_rec, int64_t *nk)
+              void *d_rec, int64_t *nk, double *stage_ms)
 {
-    if (p.precision == GENFIRE_PREC_FP64) grid_dft_t<double>(ctx, p, d_proj, angles, d_M, d_rec, nk);
-    else grid_dft_t<float>(ctx, p, d_proj, angles, d_M, d_rec, nk);
+    if (p.precision == GENFIRE_PREC_FP64) grid_dft_t<double>(ctx, p, d_proj, angles, d_M, d_rec, nk, stage_ms);
+    else grid_dft_t<float>(ctx, p, d_proj, angles, d_M, d_rec, nk, stage_ms);
 }
 
 long long select_one(genfire_ctx *ctx, const genfire_params &p, double phi, double theta, double psi,

@@ -67,7 +67,7 @@ __global__ void k_pad_ishift(const double *__restrict__ proj, int D1, int D2, in
 
 struct FftGridGeom {
     int m, s;           // cube size, shift range
-    double cutoff;
+    float cut_le;       // for a float d: d <= cutoff (in double) iff d <= cut_le, the largest float not above it
 };
 
 // grid: x over the centred dim-1 index i, y = j, z = projection
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(128) k_fft_scatter(const cplx<T> *__restrict__
                         const float dx = __fsub_rn(cx, tx), dy = __fsub_rn(cy, ty), dz = __fsub_rn(cz, tz);
                         const float d = __fsqrt_rn(
                             __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-                        if (!((double)d <= g.cutoff)) continue;
+                        if (!(d <= g.cut_le)) continue;
                         const double w = (double)__fdiv_rn(1.0f, __fadd_rn(d, 1e-5f));
                         const size_t v = (size_t)ix + (size_t)m * (iy + (size_t)m * iz);
                         atomicAdd(&num[v].x, (double)val.x * w);
@@ -114,14 +114,23 @@ __global__ void __launch_bounds__(128) k_fft_scatter(const cplx<T> *__restrict__
     if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(pairs, (unsigned long long)cnt);
 }
 
-__device__ __forceinline__ double2 fs_avg(const double2 *__restrict__ num, const double *__restrict__ ws, size_t v)
+// sum(w F) / sum(w) where sum(w) > 0, else 0: in FP64 for the FP64 output,
+// in FP32 from the FP64 sums for the single-precision output (no FP64
+// arithmetic: this part's FP64 pipe issues 2 operations per clock per SM).
+// The weight sum is >= 0, so it is positive iff its bits, as an integer, are.
+template <typename TO>
+__device__ __forceinline__ cplx<TO> fs_avg(const double2 *__restrict__ num, const double *__restrict__ ws, size_t v)
 {
-    const double w = ws[v];
-    double2 a = make_double2(0.0, 0.0);
-    if (w > 0) {
-        a = num[v];
-        a.x /= w;
-        a.y /= w;
+    cplx<TO> a = mk((TO)0, (TO)0);
+    if (reinterpret_cast<const long long *>(ws)[v] > 0) {
+        const double2 s = num[v];
+        if constexpr (sizeof(TO) == 8) {
+            const double w = ws[v];
+            a = mk(s.x / w, s.y / w);
+        } else {
+            const float w = (float)ws[v];
+            a = mk(__fdiv_rn((float)s.x, w), __fdiv_rn((float)s.y, w));
+        }
     }
     return a;
 }
@@ -141,13 +150,13 @@ __global__ void k_fft_finalize(const double2 *__restrict__ num, const double *__
     const size_t mrow = (size_t)m * (mj + (size_t)m * mk_);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
         const int mi = e - 1 - i;
-        const double2 a = fs_avg(num, ws, row + i);
-        double2 b = make_double2(0.0, 0.0);
-        if (mi < m && mj < m && mk_ < m) b = fs_avg(num, ws, mrow + mi);
-        double re = a.x + b.x, im = a.y - b.y;
+        const cplx<TO> a = fs_avg<TO>(num, ws, row + i);
+        cplx<TO> b = mk((TO)0, (TO)0);
+        if (mi < m && mj < m && mk_ < m) b = fs_avg<TO>(num, ws, mrow + mi);
+        TO re = a.x + b.x, im = a.y - b.y;
         const int cnt = (a.x != 0 || a.y != 0) + (b.x != 0 || b.y != 0);
-        if (cnt) { re /= cnt; im /= cnt; }
-        M[row + i] = mk((TO)re, (TO)im);
+        if (cnt == 2) { re *= (TO)0.5; im *= (TO)0.5; }
+        M[row + i] = mk(re, im);
     }
 }
 
@@ -187,7 +196,8 @@ static void grid_fft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     FftGridGeom g;
     g.m = m;
     g.s = p.allowMultipleGridMatches ? (int)mround(p.interpolationCutoffDistance) : 0;
-    g.cutoff = p.interpolationCutoffDistance;
+    g.cut_le = (float)p.interpolationCutoffDistance;
+    if ((double)g.cut_le > p.interpolationCutoffDistance) g.cut_le = std::nextafter(g.cut_le, -INFINITY);
     k_fft_scatter<T><<<dim3(cdiv(m, 128), m, P), 128, 0, st>>>(X.as<cplx<T>>(), drot.as<float>(), g,
                                                                num.as<double2>(), ws.as<double>(),
                                                                dpairs.as<unsigned long long>());

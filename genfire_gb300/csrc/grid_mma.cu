@@ -497,7 +497,7 @@ __global__ void k_split_projections(const double *__restrict__ proj, int D1, int
 // Host: F (float2, one per selected point) for all projections.
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
                  const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
-                 const float *d_v, float2 *d_F)
+                 const float *d_v, float2 *d_F, double *kernel_ms)
 {
     using namespace umma;
     cudaStream_t st = ctx->stream;
@@ -540,12 +540,26 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     const void *kern = pow2 ? (const void *)k_dft_tcgen05<true> : (const void *)k_dft_tcgen05<false>;
     GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = (int)std::min<size_t>(tiles.size(), (size_t)ctx->sm_count);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (kernel_ms) {
+        GF_CUDA(cudaEventCreate(&e0));
+        GF_CUDA(cudaEventCreate(&e1));
+        GF_CUDA(cudaEventRecord(e0, st));
+    }
     if (pow2) k_dft_tcgen05<true><<<grid, kThreads, smem, st>>>(a);
     else k_dft_tcgen05<false><<<grid, kThreads, smem, st>>>(a);
     GF_CHECK_LAUNCH();
+    if (kernel_ms) GF_CUDA(cudaEventRecord(e1, st));
     int herr = 0;
     GF_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     GF_CUDA(cudaStreamSynchronize(st));
+    if (kernel_ms) {
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        *kernel_ms = t;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
     if (herr) fail(GENFIRE_ERR_TIMEOUT, "tensor-core gridding: a bounded wait for the tensor core or a bulk copy expired.");
 }
 

@@ -60,8 +60,11 @@ void check_params(const genfire_params &p, bool need_projs);
 // fillInFourierGrid_DFT on device buffers: d_proj (D1 x D2 x P double),
 // angles on the host (P x 3), d_M (n1 x n2 x n1, centred, complex128 for
 // FP64 / complex64 for MIXED), d_rec optional (D1 x D2 x D1 double / float).
+// stage_ms (optional, 6 entries): device time of the selection, the DFT stage,
+// the DFT kernel alone, the weighted sums, the average/mirror/cast and the
+// recIFFT, from CUDA events on the context stream.
 void grid_dft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
-              void *d_M, void *d_rec, int64_t *nk);
+              void *d_M, void *d_rec, int64_t *nk, double *stage_ms = nullptr);
 
 // Grid sizes of measuredK for the params' gridding method: DFT (griddingMethod
 // != 1) n1 x n2 x n1 with n = round(Dim * ratio); FFT (griddingMethod 1,
@@ -81,7 +84,7 @@ void grid_fft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, c
 // (complex64) for the points of every projection (counts nk, offsets off).
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
                  const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
-                 const float *d_v, float2 *d_F);
+                 const float *d_v, float2 *d_F, double *kernel_ms = nullptr);
 
 // Selection of one projection into host arrays (test entry point).
 long long select_one(genfire_ctx *ctx, const genfire_params &p, double phi, double theta, double psi,
