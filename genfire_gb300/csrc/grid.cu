@@ -448,8 +448,9 @@ __global__ void __launch_bounds__(256) k_dft(const T *__restrict__ proj, int D1,
 // ===========================================================================
 // One pass over the entries sorted (stably) by grid index: the first entry of
 // each run sums the run's contributions in their order -- projection order --
-// and keeps the last exact hit.  Grid points in no run keep the cleared weight
-// sum and flag.
+// and keeps the last exact hit, and sets the point's bit in the touched
+// bitmap.  Only touched points get their sums, flag and exact value written;
+// nothing else of the gridded space is cleared or read.
 __global__ void k_iota(uint32_t *__restrict__ v, long long n)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -460,7 +461,7 @@ template <typename T>
 __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order,
                              const float *__restrict__ dist, const cplx<T> *__restrict__ F, long long n,
                              double2 *__restrict__ num, double *__restrict__ wsum, double2 *__restrict__ ex,
-                             uint8_t *__restrict__ hx)
+                             uint8_t *__restrict__ hx, unsigned *__restrict__ touched)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const uint32_t li = keys[i];
@@ -486,10 +487,9 @@ __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *
             num[li] = a;
             wsum[li] = w;
         }
-        if (hit) {
-            ex[li] = e;
-            hx[li] = 1;
-        }
+        if (hit) ex[li] = e;
+        hx[li] = hit ? 1 : 0;
+        atomicOr(&touched[li >> 5], 1u << (li & 31));
     }
 }
 
@@ -505,16 +505,18 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
     return (long long)(k1 - g.lo1) + (long long)g.l1 * ((k2 - g.lo2) + (long long)g.l2 * (k3 - g.lo3));
 }
 
-// Grid: x over dim 1 (c1), y = c2, z = c3, one point per thread, so no index
-// has to be decoded.  Most of the grid is untouched: each thread reads the
-// exact flag and the weight sum of its point and writes zero if neither is
-// set; the touched points of the CTA are gathered into a shared list and then
-// averaged by consecutive threads, so the FP64 divisions (a slow pipe on this
-// part) run in full warps instead of one lane of many warps.
+// Grid: x over dim 1 (c1, two points per thread, independent loads), y = c2,
+// z = c3, so no index has to be decoded.  Most of the grid is untouched: each
+// thread reads its points' bits of the touched bitmap (and nothing else) and
+// writes zero where the bit is clear; the touched points of the CTA are
+// gathered into a shared list and then averaged by consecutive threads, so
+// the FP64 divisions of the FP64 output (a slow pipe on this part) run in full
+// warps instead of one lane of many warps.
 template <typename TO>
 __global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
                                                   const double2 *__restrict__ ex, const uint8_t *__restrict__ hx,
-                                                  GridSpec g, int n1, int n2, int centro, cplx<TO> *__restrict__ M)
+                                                  const unsigned *__restrict__ touched, GridSpec g, int n1, int n2,
+                                                  int centro, cplx<TO> *__restrict__ M)
 {
     constexpr int KPT = 2;  // points per thread (independent loads in flight)
     __shared__ int list[256 * KPT];
@@ -526,22 +528,19 @@ __global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ nu
     {
         long long li[KPT];
         bool cj[KPT], in[KPT];
-        uint8_t h[KPT];
-        long long wb[KPT];
+        unsigned tb[KPT];
 #pragma unroll
         for (int q = 0; q < KPT; ++q) {
             const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
             in[q] = c1 < n1;
             li[q] = in[q] ? src_index(g, n1, n2, centro, c1, c2, c3, cj[q]) : 0;
-            h[q] = in[q] ? hx[li[q]] : 0;
-            // the weight sum is >= 0: positive iff its bits, as an integer, are (no FP64 compare)
-            wb[q] = in[q] ? reinterpret_cast<const long long *>(wsum)[li[q]] : 0;
+            tb[q] = in[q] ? touched[li[q] >> 5] : 0u;
         }
 #pragma unroll
         for (int q = 0; q < KPT; ++q) {
             if (!in[q]) continue;
             const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
-            if (h[q] || wb[q] > 0) list[atomicAdd(&cnt, 1)] = c1;
+            if ((tb[q] >> (li[q] & 31)) & 1u) list[atomicAdd(&cnt, 1)] = c1;
             else M[row + c1] = mk((TO)0, cj[q] ? -(TO)0 : (TO)0);
         }
     }
@@ -778,8 +777,8 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     // weighted average in FP64, projection by projection
     const size_t G = (size_t)g.total;
     DevBuf num(sizeof(double2) * G, st), wsum(sizeof(double) * G, st), ex(sizeof(double2) * G, st), hx(G, st);
-    GF_CUDA(cudaMemsetAsync(wsum.p, 0, wsum.bytes, st));  // num and ex are read only where wsum / hx are set
-    GF_CUDA(cudaMemsetAsync(hx.p, 0, hx.bytes, st));
+    DevBuf touched(sizeof(unsigned) * ((G + 31) / 32), st);  // the only array that is cleared
+    GF_CUDA(cudaMemsetAsync(touched.p, 0, touched.bytes, st));
     if (sel.total > 0) {
         // stable radix sort of (grid index, entry) keeps projection order within a grid point
         const long long n = sel.total;
@@ -797,12 +796,14 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
         k_accum_runs<T><<<grid_for(ctx, n, 256), 256, 0, st>>>(keys.as<uint32_t>(), vout.as<uint32_t>(),
                                                                 sel.dist.as<float>(), F.as<cplx<T>>(), n,
                                                                 num.as<double2>(), wsum.as<double>(),
-                                                                ex.as<double2>(), hx.as<uint8_t>());
+                                                                ex.as<double2>(), hx.as<uint8_t>(),
+                                                                touched.as<unsigned>());
         GF_CHECK_LAUNCH();
     }
     se.mark(3, st);
     k_finalize<T><<<dim3(cdiv(n1, 512), n2, n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
-                                                               ex.as<double2>(), hx.as<uint8_t>(), g, n1, n2,
+                                                               ex.as<double2>(), hx.as<uint8_t>(),
+                                                               touched.as<unsigned>(), g, n1, n2,
                                                                p.DFT_CentroSymmetricity,
                                                                reinterpret_cast<cplx<T> *>(d_M));
     GF_CHECK_LAUNCH();
