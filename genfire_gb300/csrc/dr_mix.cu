@@ -150,30 +150,9 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_row_r2c_mix(RowPas
     const int vc = c * N1;
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
+    (void)r1;
     cplx<T> v[N1][8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-#pragma unroll
-        for (int n1 = 0; n1 < N1; ++n1) {
-            int e = n1 + N1 * (j + k * TPC) + a.c1;
-            if (e >= N) e -= N;
-            T va = 0, vb = 0;
-            if (e < a.B1) {
-                if (r0 < a.nrows) {
-                    const long long o = (long long)r0 * a.B1 + e;
-                    va = x[o];
-                    if (a.positivity && va < (T)0) va = 0;
-                    if (a.support) va = va * (T)a.support[o];
-                }
-                if (r1 < a.nrows) {
-                    const long long o = (long long)r1 * a.B1 + e;
-                    vb = x[o];
-                    if (a.positivity && vb < (T)0) vb = 0;
-                    if (a.support) vb = vb * (T)a.support[o];
-                }
-            }
-            v[n1][k] = mk(va, vb);
-        }
+    load_row_pair<T, N, N1>(a, x, r0, j, v);
     int buf = 0;
     const int in_base = Lay::idx(j, vc);
     reg_fft<T, N2, Lay, false, N1>(v, sA, sB, buf, j, vc, in_base, a.tw + N);

@@ -369,6 +369,44 @@ __global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_c
 }
 
 // Row passes (same contract as k_rows_r2c / k_rows_c2r) for N a power of two.
+// The two real rows r0, r0+1 of a box (positivity and support applied) as the
+// real and imaginary parts of register k of sequence n1: the element at
+// position n1 + NSEQ * (j + k * N / (8 * NSEQ)) of a length-N transform.  All
+// loads are issued before any value is used, so they are in flight together.
+template <typename T, int N, int NSEQ>
+__device__ __forceinline__ void load_row_pair(const RowPassArgs<T> &a, const T *__restrict__ x, int r0, int j,
+                                              cplx<T> (&v)[NSEQ][8])
+{
+    constexpr int TPC = N / (8 * NSEQ);
+    const bool ok0 = r0 < a.nrows, ok1 = r0 + 1 < a.nrows;
+    const long long o0 = (long long)r0 * a.B1, o1 = o0 + a.B1;
+    T xa[NSEQ][8], xb[NSEQ][8];
+    uint8_t sa[NSEQ][8], sb[NSEQ][8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+#pragma unroll
+        for (int n1 = 0; n1 < NSEQ; ++n1) {
+            int e = n1 + NSEQ * (j + k * TPC) + a.c1;
+            if (e >= N) e -= N;
+            const bool in = e < a.B1;
+            xa[n1][k] = (in && ok0) ? x[o0 + e] : (T)0;
+            xb[n1][k] = (in && ok1) ? x[o1 + e] : (T)0;
+            sa[n1][k] = (a.support && in && ok0) ? a.support[o0 + e] : (uint8_t)1;
+            sb[n1][k] = (a.support && in && ok1) ? a.support[o1 + e] : (uint8_t)1;
+        }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+#pragma unroll
+        for (int n1 = 0; n1 < NSEQ; ++n1) {
+            T va = xa[n1][k], vb = xb[n1][k];
+            if (a.positivity) {
+                if (va < (T)0) va = 0;
+                if (vb < (T)0) vb = 0;
+            }
+            v[n1][k] = mk(va * (T)sa[n1][k], vb * (T)sb[n1][k]);
+        }
+}
+
 template <typename T, int N>
 __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_row_r2c_reg(RowPassArgs<T> a)
 {
@@ -382,27 +420,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     cplx<T> v[1][8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        int e = j + k * TPC + a.c1;
-        if (e >= N) e -= N;
-        T va = 0, vb = 0;
-        if (e < a.B1) {
-            if (r0 < a.nrows) {
-                const long long o = (long long)r0 * a.B1 + e;
-                va = x[o];
-                if (a.positivity && va < (T)0) va = 0;
-                if (a.support) va = va * (T)a.support[o];
-            }
-            if (r1 < a.nrows) {
-                const long long o = (long long)r1 * a.B1 + e;
-                vb = x[o];
-                if (a.positivity && vb < (T)0) vb = 0;
-                if (a.support) vb = vb * (T)a.support[o];
-            }
-        }
-        v[0][k] = mk(va, vb);
-    }
+    load_row_pair<T, N, 1>(a, x, r0, j, v);
     int buf = 0;
     const int in_base = Lay::idx(j, c);
     reg_fft<T, N, Lay, false, 1>(v, sA, sB, buf, j, c, in_base, a.tw + N);
@@ -436,12 +454,22 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     // pack the two half spectra of the pair: each thread takes q = j, j + N/8, ...
+    // (h1 <= N/2 + 1); all loads are issued before the packing
     {
+        constexpr int QIT = (N / 2 + TPC) / TPC;
         const cplx<T> *ya = a.Y + (long long)r0 * a.ld1, *yb = ya + a.ld1;
-        for (int q = j; q < a.h1; q += TPC) {
-            cplx<T> ha = mk((T)0, (T)0), hb = ha;
-            if (r0 < a.nrows) ha = ya[q];
-            if (r1 < a.nrows) hb = yb[q];
+        cplx<T> HA[QIT], HB[QIT];
+#pragma unroll
+        for (int it = 0; it < QIT; ++it) {
+            const int q = j + it * TPC;
+            HA[it] = (q < a.h1 && r0 < a.nrows) ? ya[q] : mk((T)0, (T)0);
+            HB[it] = (q < a.h1 && r1 < a.nrows) ? yb[q] : mk((T)0, (T)0);
+        }
+#pragma unroll
+        for (int it = 0; it < QIT; ++it) {
+            const int q = j + it * TPC;
+            if (q >= a.h1) break;
+            cplx<T> ha = HA[it], hb = HB[it];
             if (q == 0 || 2 * q == N) { ha.y = 0; hb.y = 0; }
             sA[Lay::idx(q, c)] = mk(ha.x - hb.y, ha.y + hb.x);
             if (q != 0 && N - q >= a.h1) sA[Lay::idx(N - q, c)] = mk(ha.x + hb.y, hb.x - ha.y);
