@@ -24,6 +24,8 @@ GENFIRE_ERR_STATE = 6
 PREC_FP64 = 0
 PREC_MIXED = 1
 
+PROFILE_KERNELS = 5   # GENFIRE_PROFILE_KERNELS: kernels of one iteration
+
 INTERP_TRILINEAR = 0
 INTERP_CUBIC = 1
 
@@ -433,11 +435,11 @@ class Recon:
 
     def profile(self, iterations):
         """Per-kernel mean ms and algorithmic bytes per launch over `iterations` iterations."""
-        ms = np.zeros(7)
-        by = np.zeros(7)
+        ms = np.zeros(PROFILE_KERNELS)
+        by = np.zeros(PROFILE_KERNELS)
         self.ctx.check(load().genfire_recon_profile(self._h, iterations, ptr(ms, C.c_double), ptr(by, C.c_double)))
         self.done += iterations
-        names = [load().genfire_profile_kernel_name(k).decode() for k in range(7)]
+        names = [load().genfire_profile_kernel_name(k).decode() for k in range(PROFILE_KERNELS)]
         return names, ms, by
 
     def tuning(self):

@@ -324,9 +324,10 @@ genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, doubl
 const char *genfire_profile_kernel_name(int32_t k)
 {
     static const char *names[GENFIRE_PROFILE_KERNELS] = {
-        "k_ctl_begin", "k_rows_r2c (F1: dim-1 real->half, positivity, support)",
-        "k_colpass (F2: dim-2 forward)", "k_colpass (F3: dim-3 forward, Fourier constraint, errK, dim-3 inverse)",
-        "k_ctl_mid (errK, best object)", "k_colpass (I2: dim-2 inverse)", "k_rows_c2r (I1: half->real dim-1)"};
+        "F1 row pass (dim-1 real->half, positivity, support; starts the iteration)",
+        "F2 column pass (dim-2 forward)",
+        "F3 column pass (dim-3 forward, Fourier constraint, errK, dim-3 inverse)",
+        "I2 column pass (dim-2 inverse; errK total and best object)", "I1 row pass (half->real dim-1)"};
     return (k >= 0 && k < GENFIRE_PROFILE_KERNELS) ? names[k] : "";
 }
 

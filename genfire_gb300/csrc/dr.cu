@@ -3,12 +3,14 @@
 //
 // One iteration (reconstruct.m:117-186) is five FFT passes and two tiny
 // control kernels, captured once as a CUDA graph:
-//   ctl_begin  iteration count, constraint change points, bestErr reset
-//   F1         rows along dim 1: positivity and support, real -> half spectrum
+//   F1         rows along dim 1: positivity and support, real -> half spectrum;
+//              its CTA 0 also starts the iteration (iteration count,
+//              constraint change points, bestErr reset)
 //   F2         dim 2 forward
 //   F3         dim 3 forward, errK terms, Fourier constraint, dim 3 inverse
-//   ctl_mid    errK = sum / sum|M|, best-object bookkeeping, output buffer
-//   I2         dim 2 inverse
+//   I2         dim 2 inverse; its CTA 0 first forms errK = sum / sum|M| from
+//              F3's partials and does the best-object bookkeeping (which
+//              buffer the next object goes to, read by I1)
 //   I1         rows along dim 1: half spectrum -> real
 // The object is held only on its "box": the Dim1 x Dim2 x Dim1 region the
 // support can be non-zero on (the whole n1 x n2 x n1 grid when the support
@@ -421,63 +423,6 @@ void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, 
 // ===========================================================================
 // the iteration
 // ===========================================================================
-struct Ctl {
-    int it;       // iterations completed
-    int cur;      // next entry of the change-point list (0-based currentCutoffNum)
-    int cidx;     // delay indicator in force
-    int xcur;     // buffer holding the current object
-    int xnext;    // buffer the next object is written to
-    int xbest;    // buffer holding the best object (-1: none yet)
-    int m;        // number of delay indicators
-    int pad;
-    double bestErr;
-    double errK;
-};
-
-// reconstruct.m:118-124
-__global__ void k_ctl_begin(Ctl *c, const int *__restrict__ changes)
-{
-    if (threadIdx.x != 0) return;
-    c->xcur = c->xnext;
-    const int it = ++c->it;
-    if (c->cur < c->m && it == changes[c->cur]) {
-        int last = c->cur;
-        for (int k = 0; k < c->m; ++k)
-            if (changes[k] == it) last = k;
-        c->cidx = last;
-        c->cur = last + 1;
-        c->bestErr = 1e30;
-    }
-}
-
-// reconstruct.m:135 and :149-153
-__global__ void __launch_bounds__(1024) k_ctl_mid(Ctl *c, const double *__restrict__ partial, int np, double denom,
-                                                  double *__restrict__ hist)
-{
-    __shared__ double red[32];
-    double s = 0;
-    const int per = (np + blockDim.x - 1) / blockDim.x;
-    const int b = threadIdx.x * per, e = min(b + per, np);
-    for (int i = b; i < e; ++i) s += partial[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double v = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) {
-            const double err = v / denom;
-            c->errK = err;
-            hist[c->it - 1] = err;
-            if (err < c->bestErr) {
-                c->bestErr = err;
-                c->xbest = c->xcur;
-            }
-            c->xnext = (c->xbest == c->xcur) ? 1 - c->xcur : c->xcur;
-        }
-    }
-}
-
 // Constraint table: one entry per half-spectrum point q with q in E or -q in E
 // (E = measuredK ~= 0 & mask, reconstruct.m:99), grouped by column q1 + h1*q2.
 struct TabGeom {
@@ -822,13 +767,21 @@ template <typename T> struct ReconT : ReconBase {
         b.cidx = &c->cidx;
         return b;
     }
-    // I2: dim 2 inverse, box rows out
-    ColPassArgs<T> i2_args()
+    // I2: dim 2 inverse, box rows out; with_ctl: CTA 0 first forms errK from
+    // F3's partials and updates the best object and the output buffer
+    ColPassArgs<T> i2_args(bool with_ctl = true)
     {
         ColPassArgs<T> d = colargs<T>(pl2, tw2, W2, h1);
         d.in = Y2.as<cplx<T>>(); d.in_dim = ld1; d.in_other = (long long)ld1 * n2; d.in_cnt = n2; d.in_c = 0;
         d.out = Y1.as<cplx<T>>(); d.out_dim = ld1; d.out_other = (long long)ld1 * B2; d.out_cnt = B2; d.out_c = B2 / 2;
         d.mode = 2;
+        if (with_ctl) {
+            d.ctl = ctl.as<Ctl>();
+            d.partial = partial.as<double>();
+            d.nparts = nparts;
+            d.denom = denom;
+            d.hist = hist.as<double>();
+        }
         return d;
     }
 
@@ -841,7 +794,7 @@ template <typename T> struct ReconT : ReconBase {
         cudaStream_t st = ctx->stream;
         vF2 = autotune_colpass<T>(f2_args(), B3, st);
         vF3 = autotune_colpass<T>(f3_args(), n2, st);
-        vI2 = autotune_colpass<T>(i2_args(), B3, st);
+        vI2 = autotune_colpass<T>(i2_args(false), B3, st);  // timed launches leave the control block alone
         GF_CUDA(cudaStreamSynchronize(st));
     }
 
@@ -852,14 +805,15 @@ template <typename T> struct ReconT : ReconBase {
         int ek = 0;
         auto mark = [&]() { if (ev) GF_CUDA(cudaEventRecord(ev[ek++], st)); };
         mark();
-        k_ctl_begin<<<1, 32, 0, st>>>(c, changes.as<int>());
-        GF_CHECK_LAUNCH();
-        mark();
-        // F1: rows (dim 1) real -> half spectrum, with positivity and support
+        // F1: rows (dim 1) real -> half spectrum, with positivity and support;
+        // the object of this iteration is the previous iteration's output
+        // buffer (xnext; CTA 0 sets xcur to it)
         RowPassArgs<T> r;
         std::memset(&r, 0, sizeof(r));
         r.pl = pl1; r.tw = tw1; r.W = W1; r.nrows = B2 * B3; r.B1 = B1; r.c1 = B1 / 2; r.h1 = h1; r.ld1 = ld1;
-        r.xs[0] = xbuf[0].as<T>(); r.xs[1] = xbuf[1].as<T>(); r.xsel = &c->xcur;
+        r.xs[0] = xbuf[0].as<T>(); r.xs[1] = xbuf[1].as<T>(); r.xsel = &c->xnext;
+        r.ctl = c;
+        r.changes = changes.as<int>();
         r.support = p.constraintSupport ? S.as<uint8_t>() : nullptr;
         r.positivity = p.constraintPositivity;
         r.Y = Y1.as<cplx<T>>();
@@ -870,14 +824,13 @@ template <typename T> struct ReconT : ReconBase {
         mark();
         launch_colpass<T>(f3_args(), n2, st, vF3);
         mark();
-        k_ctl_mid<<<1, 1024, 0, st>>>(c, partial.as<double>(), nparts, denom, hist.as<double>());
-        GF_CHECK_LAUNCH();
-        mark();
         launch_colpass<T>(i2_args(), B3, st, vI2);
         mark();
         // I1: rows half spectrum -> real box, 1/N
         RowPassArgs<T> q = r;
         q.xsel = &c->xnext;
+        q.ctl = nullptr;
+        q.changes = nullptr;
         q.support = nullptr;
         q.positivity = 0;
         q.scale = (T)(1.0 / ((double)n1 * n2 * n1));
@@ -891,13 +844,11 @@ template <typename T> struct ReconT : ReconBase {
         const double S = sizeof(cplx<T>), Rs = sizeof(T);
         const double box = (double)B1 * B2 * B3;
         const double half_box = (double)h1 * B2 * B3, half_mid = (double)h1 * n2 * B3;
-        b[0] = 0;
-        b[1] = box * Rs + (p.constraintSupport ? box : 0.0) + half_box * S;
-        b[2] = half_box * S + half_mid * S;
-        b[3] = 2 * half_mid * S + ntab * (double)sizeof(TabEntry<T>) + (h1 * (double)n2 + 1) * 4 + nparts * 8.0;
-        b[4] = nparts * 8.0;
-        b[5] = half_mid * S + half_box * S;
-        b[6] = half_box * S + box * Rs;
+        b[0] = box * Rs + (p.constraintSupport ? box : 0.0) + half_box * S;
+        b[1] = half_box * S + half_mid * S;
+        b[2] = 2 * half_mid * S + ntab * (double)sizeof(TabEntry<T>) + (h1 * (double)n2 + 1) * 4 + nparts * 8.0;
+        b[3] = half_mid * S + half_box * S + nparts * 8.0;
+        b[4] = half_box * S + box * Rs;
     }
 
     void profile(int count, double *ms, double *bytes) override
@@ -905,14 +856,15 @@ template <typename T> struct ReconT : ReconBase {
         if (count < 1 || it_done + count > p.numIterations)
             fail(GENFIRE_ERR_STATE, "profile: iteration count out of range.");
         cudaStream_t st = ctx->stream;
-        cudaEvent_t ev[8];
+        constexpr int NK = GENFIRE_PROFILE_KERNELS;
+        cudaEvent_t ev[NK + 1];
         for (auto &e : ev) GF_CUDA(cudaEventCreate(&e));
-        double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+        double acc[NK] = {};
         try {
             for (int i = 0; i < count; ++i) {
                 enqueue_iteration(st, ev);
-                GF_CUDA(cudaEventSynchronize(ev[7]));
-                for (int k = 0; k < 7; ++k) {
+                GF_CUDA(cudaEventSynchronize(ev[NK]));
+                for (int k = 0; k < NK; ++k) {
                     float t = 0;
                     GF_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
                     acc[k] += t;
@@ -926,7 +878,7 @@ template <typename T> struct ReconT : ReconBase {
         }
         for (auto &e : ev) cudaEventDestroy(e);
         if (ms)
-            for (int k = 0; k < 7; ++k) ms[k] = acc[k] / count;
+            for (int k = 0; k < NK; ++k) ms[k] = acc[k] / count;
         if (bytes) kernel_bytes(bytes);
     }
 

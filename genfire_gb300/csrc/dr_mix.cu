@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_col_mix(ColPassArg
     using Full = ColLayout<N, W>;
     static_assert(Lay::SIZE == Full::SIZE, "exchange and full layouts share the buffers");
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (a.ctl && blockIdx.x == 0 && blockIdx.y == 0) ctl_mid_update(a.ctl, a.partial, a.nparts, a.denom, a.hist);
     cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *sB = sA + Lay::SIZE;
     const cplx<T> *tw = a.tw, *twp = a.tw + N;
@@ -104,6 +105,7 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_col_mix(ColPassArg
             __syncthreads();
             if (a.mode & 4) {
                 err = apply_table<T, Full>(s, a, tile, W, other);
+                block_partial(err, a.partial + (long long)other * gridDim.x + tile);
                 __syncthreads();
             }
 #pragma unroll
@@ -129,7 +131,6 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_col_mix(ColPassArg
             }
         }
     }
-    if (a.mode & 4) block_partial(err, a.partial + (long long)other * gridDim.x + tile);
 }
 
 // Row passes (contracts of k_rows_r2c / k_rows_c2r): two real rows per
@@ -148,9 +149,9 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_row_r2c_mix(RowPas
     cplx<T> *sB = sA + Lay::SIZE;
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
     const int vc = c * N1;
+    if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
-    (void)r1;
     cplx<T> v[N1][8];
     load_row_pair<T, N, N1>(a, x, r0, j, v);
     int buf = 0;

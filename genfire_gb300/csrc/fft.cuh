@@ -242,6 +242,72 @@ template <typename T> struct TabEntry {
 };
 
 // ---------------------------------------------------------------------------
+// Control block of the iteration, in device memory, so one iteration is a
+// fixed sequence of launches (a CUDA graph).  Its two updates run inside the
+// passes, in CTA 0 of a pass where nothing else reads what they change: the
+// start of an iteration in the first row pass, the errK reduction and the
+// best-object bookkeeping in the dim-2 inverse pass.
+// ---------------------------------------------------------------------------
+struct Ctl {
+    int it;           // iterations completed
+    int cur;          // next entry of the change-point list (0-based currentCutoffNum)
+    int cidx;         // delay indicator in force
+    int xcur;         // buffer holding the current object
+    int xnext;        // buffer the next object is written to
+    int xbest;        // buffer holding the best object (-1: none yet)
+    int m;            // number of delay indicators
+    int pad;
+    double bestErr;
+    double errK;
+};
+
+// reconstruct.m:118-124 (one thread)
+__device__ __forceinline__ void ctl_begin_update(Ctl *c, const int *__restrict__ changes)
+{
+    c->xcur = c->xnext;
+    const int it = ++c->it;
+    if (c->cur < c->m && it == changes[c->cur]) {
+        int last = c->cur;
+        for (int k = 0; k < c->m; ++k)
+            if (changes[k] == it) last = k;
+        c->cidx = last;
+        c->cur = last + 1;
+        c->bestErr = 1e30;
+    }
+}
+
+// reconstruct.m:135 and :149-153, run by all threads of CTA 0 of the pass
+// after the fused dim-3 pass (the dim-2 inverse, which itself needs neither
+// errK nor the output buffer; the pass after it does): sums the fused pass's
+// per-CTA errK partials in a fixed order (each thread a contiguous slice, then
+// a fixed tree) and updates errK, the best object and the output buffer.
+static __device__ __noinline__ void ctl_mid_update(Ctl *c, const double *partial, int np, double denom,
+                                                   double *hist)
+{
+    __shared__ double red[32];
+    const int nt = blockDim.x;
+    const int per = (np + nt - 1) / nt;
+    const int b = threadIdx.x * per, e = min(b + per, np);
+    double s = 0;
+    for (int i = b; i < e; ++i) s += partial[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0;
+        for (int w = 0; w < (nt + 31) / 32; ++w) v += red[w];
+        const double err = v / denom;
+        c->errK = err;
+        hist[c->it - 1] = err;
+        if (err < c->bestErr) {
+            c->bestErr = err;
+            c->xbest = c->xcur;
+        }
+        c->xnext = (c->xbest == c->xcur) ? 1 - c->xcur : c->xcur;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Column pass: length-n transforms along a strided dimension, W columns per
 // CTA.  Column c of tile t is element (t*W + c) * col_stride; entry e along
 // the transform is at e * dim_stride; blockIdx.y selects the "other"
@@ -271,11 +337,19 @@ template <typename T> struct ColPassArgs {
     int h1;
     double *partial;        // one errK partial sum per CTA
     const int *cidx;        // current delay index (device)
+    // with ctl set (the iteration's dim-2 inverse pass): CTA 0 first reduces
+    // the fused pass's partials (nparts of them) into errK and updates the
+    // best object (ctl_mid_update)
+    Ctl *ctl;
+    int nparts;
+    double denom;
+    double *hist;
 };
 
 template <typename T>
 __global__ void __launch_bounds__(kTileMaxThreads<T>) k_colpass(ColPassArgs<T> a)
 {
+    if (a.ctl && blockIdx.x == 0 && blockIdx.y == 0) ctl_mid_update(a.ctl, a.partial, a.nparts, a.denom, a.hist);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     const int n = a.pl.n, W = a.W, P = a.P;
@@ -387,6 +461,10 @@ template <typename T> struct RowPassArgs {
     int positivity;
     cplx<T> *Y;        // ld1 x nrows half spectrum
     T scale;           // inverse only
+    // with ctl set (the iteration's first pass): CTA 0 starts the iteration
+    // (ctl_begin_update) while every CTA reads the object from xs[ctl->xnext]
+    Ctl *ctl;
+    const int *changes;
 };
 
 // forward: real rows (after positivity and support, reconstruct.m:126-131) -> half spectrum
@@ -396,6 +474,7 @@ __global__ void __launch_bounds__(kTileMaxThreads<T>) k_rows_r2c(RowPassArgs<T> 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     const int n = a.pl.n, W = a.W, P = a.P, tid = threadIdx.x, nt = blockDim.x;
+    if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0base = blockIdx.x * W * 2;
     for (int i = tid; i < n * P; i += nt) s[i] = mk((T)0, (T)0);

@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_c
     using Lay = ColLayout<N, W>;
     constexpr int NST = P2Plan<N>::NST;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    if (a.ctl && blockIdx.x == 0 && blockIdx.y == 0) ctl_mid_update(a.ctl, a.partial, a.nparts, a.denom, a.hist);
     cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *sB = sA + Lay::SIZE;
     const cplx<T> *twp = a.tw + N;
@@ -339,6 +340,7 @@ __global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_c
             __syncthreads();
             if (a.mode & 4) {
                 err = apply_table<T, Lay>(s, a, tile, W, other);
+                block_partial(err, a.partial + (long long)other * gridDim.x + tile);
                 __syncthreads();
             }
             load_stage<T, N, Lay, NC>(s, v, in_base);
@@ -365,7 +367,6 @@ __global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_c
             }
         }
     }
-    if (a.mode & 4) block_partial(err, a.partial + (long long)other * gridDim.x + tile);
 }
 
 // Row passes (same contract as k_rows_r2c / k_rows_c2r) for N a power of two.
@@ -417,6 +418,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *sB = sA + Lay::SIZE;
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
+    if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     cplx<T> v[1][8];

@@ -129,6 +129,15 @@ genfire_status genfire_grid_dft_device(genfire_ctx *ctx, const genfire_params *p
                                        const double *d_projections, const double *angles,
                                        void *d_measuredK, void *d_recIFFT, int64_t *nk);
 
+/* genfire_grid_dft_device (without recIFFT) with the device time of its
+ * stages from CUDA events on the context stream (tracing; the reference
+ * prints only the total, fillInFourierGrid_DFT.m:306-308): stage_ms[0]
+ * K-point selection, [1] DFT stage (operand preparation and the DFT kernel),
+ * [2] the DFT kernel alone, [3] weighted sums, [4] average, centro mirror and
+ * cast, [5] recIFFT (0 here). */
+genfire_status genfire_grid_profile(genfire_ctx *ctx, const genfire_params *p, const double *d_projections,
+                                    const double *angles, void *d_measuredK, double *stage_ms);
+
 /* ---- gridding: fillInFourierGrid (griddingMethod = 1) -------------------
  * Replaces obj = fillInFourierGrid(obj)
  * (@GENFIRE_Reconstructor/fillInFourierGrid.m:27-168), the class's default
@@ -225,7 +234,7 @@ genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b);
  * 2 = register-resident, two columns per thread, -1 = built-in choice. */
 genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants);
 
-#define GENFIRE_PROFILE_KERNELS 7
+#define GENFIRE_PROFILE_KERNELS 5
 genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes);
 const char *genfire_profile_kernel_name(int32_t k);
 
