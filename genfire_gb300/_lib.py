@@ -38,7 +38,7 @@ EXPORTS = [
     "genfire_reconstruct", "genfire_recon_create", "genfire_recon_iterate", "genfire_recon_result",
     "genfire_recon_destroy", "genfire_recon_profile", "genfire_profile_kernel_name",
     "genfire_recon_batch_create", "genfire_recon_batch_iterate", "genfire_recon_batch_destroy",
-    "genfire_recon_tuning",
+    "genfire_recon_tuning", "genfire_rfree_candidates", "genfire_recon_set_rfree", "genfire_recon_rfree",
     "genfire_project", "genfire_rfactor", "genfire_rfactor_noalloc", "genfire_set_projector_interpolation",
     "genfire_rfactor_realspace",
     "genfire_centro_symmetricity", "genfire_hermitian_symmetrize", "genfire_make_kspace_indices",
@@ -105,6 +105,9 @@ def load():
         "genfire_recon_batch_create": (C.c_int, [vp, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "genfire_recon_batch_iterate": (C.c_int, [vp, C.c_int32]),
         "genfire_recon_tuning": (C.c_int, [vp, i32p]),
+        "genfire_rfree_candidates": (C.c_int, [vp, pp, vp, C.c_int32, C.c_int32, i64p, i64p]),
+        "genfire_recon_set_rfree": (C.c_int, [vp, C.c_int32, i64p, i64p]),
+        "genfire_recon_rfree": (C.c_int, [vp, i32p, dp]),
         "genfire_recon_batch_destroy": (C.c_int, [vp]),
         "genfire_recon_profile": (C.c_int, [vp, C.c_int32, dp, dp]),
         "genfire_profile_kernel_name": (C.c_char_p, [C.c_int32]),
@@ -363,6 +366,20 @@ class Context:
                                                        ptr(out, C.c_double)))
         return out
 
+    def rfree_candidates(self, p, measuredK, nbins):
+        """Candidate points of the nbins Rfree shells (reconstruct.m:47-50): a
+        list of ascending 0-based linear index arrays (int64), one per shell."""
+        cdt = np.complex128 if p.precision == PREC_FP64 else np.complex64
+        M = fortran(measuredK, cdt)
+        counts = np.zeros(nbins, dtype=np.int64)
+        self.check(load().genfire_rfree_candidates(self._h, C.byref(p), ptr(M), 0, nbins, ptr(counts, C.c_int64),
+                                                   None))
+        ind = np.zeros(max(int(counts.sum()), 1), dtype=np.int64)
+        self.check(load().genfire_rfree_candidates(self._h, C.byref(p), ptr(M), 0, nbins, ptr(counts, C.c_int64),
+                                                   ptr(ind, C.c_int64)))
+        off = np.concatenate([[0], np.cumsum(counts)])
+        return [ind[off[s]:off[s + 1]].copy() for s in range(nbins)]
+
     def make_kspace_indices(self, shape):
         Q = np.zeros(tuple(shape), dtype=np.float64, order="F")
         self.check(load().genfire_make_kspace_indices(self._h, shape[0], shape[1], shape[2], ptr(Q, C.c_double)))
@@ -432,6 +449,24 @@ class Recon:
         self.ctx.check(load().genfire_recon_result(self._h, ptr(rec), ptr(errK), ptr(errR, C.c_double),
                                                    ptr(Rarr, C.c_double), ptr(Rarr2, C.c_double), 0))
         return rec, errK[:self.done], errR[:nmon], Rarr[:, :nmon], Rarr2[:, :nmon]
+
+    def set_rfree(self, shells):
+        """Withheld Rfree points (list of 0-based centred linear index arrays,
+        one per shell, already cleared in the mask given at creation)."""
+        counts = np.array([len(x) for x in shells], dtype=np.int64)
+        ind = np.ascontiguousarray(np.concatenate([np.asarray(x, dtype=np.int64) for x in shells])
+                                   if len(shells) else np.zeros(1, dtype=np.int64))
+        self.ctx.check(load().genfire_recon_set_rfree(self._h, len(shells), ptr(counts, C.c_int64),
+                                                      ptr(ind, C.c_int64)))
+        self._rfree_keep = (counts, ind)
+
+    def rfree(self):
+        """Rfree_complex so far: array (nshells, iterations)."""
+        ns = C.c_int32(0)
+        self.ctx.check(load().genfire_recon_rfree(self._h, C.byref(ns), None))
+        out = np.zeros((max(ns.value, 1), max(self.done, 1)), order="F")
+        self.ctx.check(load().genfire_recon_rfree(self._h, C.byref(ns), ptr(out, C.c_double)))
+        return out[:ns.value, :self.done]
 
     def profile(self, iterations):
         """Per-kernel mean ms and algorithmic bytes per launch over `iterations` iterations."""

@@ -314,6 +314,35 @@ genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants)
     return GENFIRE_OK;
 }
 
+genfire_status genfire_recon_set_rfree(genfire_recon *r, int32_t nshells, const int64_t *counts,
+                                      const int64_t *indices)
+{
+    if (!r) return GENFIRE_ERR_ARG;
+    genfire_ctx *ctx = r->ctx;
+    return guarded(ctx, [&] { gf::recon_set_rfree(r, nshells, counts, indices); });
+}
+
+genfire_status genfire_recon_rfree(genfire_recon *r, int32_t *nshells, double *rfree)
+{
+    if (!r) return GENFIRE_ERR_ARG;
+    genfire_ctx *ctx = r->ctx;
+    return guarded(ctx, [&] {
+        const int n = gf::recon_rfree(r, rfree);
+        if (nshells) *nshells = n;
+    });
+}
+
+genfire_status genfire_rfree_candidates(genfire_ctx *ctx, const genfire_params *p, const void *measuredK,
+                                        int32_t on_device, int32_t nbins, int64_t *counts, int64_t *indices)
+{
+    if (!ctx) return GENFIRE_ERR_ARG;
+    return guarded(ctx, [&] {
+        need(p, "params");
+        gf::check_params(*p, false);
+        gf::rfree_candidates(ctx, *p, measuredK, on_device != 0, nbins, counts, indices);
+    });
+}
+
 genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes)
 {
     if (!r) return GENFIRE_ERR_ARG;

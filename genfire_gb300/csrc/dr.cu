@@ -443,6 +443,14 @@ __device__ __forceinline__ double q_radius(double kx, double ky, double kz)
     return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz)));
 }
 
+// make_Kspace_indices coordinate: (i - r) / r with r = n2K (n/2 or (n-1)/2), 0 for n == 1
+__device__ __forceinline__ double kspace_k(int n, int i)
+{
+    if (n == 1) return 0.0;
+    const int r = (n % 2 == 0) ? n / 2 : (n - 1) / 2;
+    return (double)(i - r) / (double)r;
+}
+
 template <typename T>
 __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask,
                                           const TabGeom &g, int q1, int q2, int q3, TabEntry<T> &e, double &absM)
@@ -462,11 +470,7 @@ __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const u
     e.pos = (uint32_t)q3 | ((uint32_t)(q1 % g.W3) << 16);
     e.eflags = (inEq ? 1u : 0u) | ((inEm && !mate_stored) ? 2u : 0u);
     // constraintIndicators = 1 - Q (reconstruct.m:36-42, make_Kspace_indices.m)
-    auto kv = [](int n, int i) -> double {
-        if (n == 1) return 0.0;
-        const int r = (n % 2 == 0) ? n / 2 : (n - 1) / 2;
-        return (double)(i - r) / (double)r;
-    };
+    auto kv = [](int n, int i) -> double { return kspace_k(n, i); };
     uint32_t cq = 0, cm = 0;
     if (inEq) {
         const double ci = 1.0 - q_radius(kv(n2, c2), kv(n1, c1), kv(n1, c3));
@@ -545,6 +549,140 @@ __global__ void __launch_bounds__(1024) k_scan_cols(const int *__restrict__ coun
     for (int i = b; i < e; ++i) { off[i] = (int)run; run += counts[i]; }
 }
 
+// ---------------------------------------------------------------- Rfree
+// Candidates of one shell (reconstruct.m:48): measuredK ~= 0 & Q >= lo & Q < hi,
+// Q = make_Kspace_indices (same rounding as tab_point), in ascending linear
+// order.  Pass 1 (out == NULL) counts per 1024-point block; pass 2 writes the
+// indices at the block offsets (warp ballots, block prefix in warp order).
+template <typename T>
+__global__ void __launch_bounds__(1024) k_rfree_mark(const cplx<T> *__restrict__ M, int n1, int n2, double lo, double hi,
+                                                     int *__restrict__ bcount, const int *__restrict__ boff,
+                                                     int *__restrict__ out)
+{
+    __shared__ int wc[32];
+    const long long N = (long long)n1 * n2 * n1;
+    const long long i = (long long)blockIdx.x * 1024 + threadIdx.x;
+    bool f = false;
+    if (i < N) {
+        const cplx<T> v = M[i];
+        if (v.x != 0 || v.y != 0) {
+            const int c1 = (int)(i % n1), c2 = (int)((i / n1) % n2), c3 = (int)(i / ((long long)n1 * n2));
+            const double q = q_radius(kspace_k(n2, c2), kspace_k(n1, c1), kspace_k(n1, c3));
+            f = q >= lo && q < hi;
+        }
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, f);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) wc[w] = __popc(b);
+    __syncthreads();
+    if (!out) {
+        if (threadIdx.x == 0) {
+            int t = 0;
+            for (int k = 0; k < 32; ++k) t += wc[k];
+            bcount[blockIdx.x] = t;
+        }
+        return;
+    }
+    if (f) {
+        int pre = boff[blockIdx.x];
+        for (int k = 0; k < w; ++k) pre += wc[k];
+        out[pre + __popc(b & ((1u << l) - 1u))] = (int)i;
+    }
+}
+
+template <typename T>
+__global__ void k_rfree_gather(const cplx<T> *__restrict__ M, const long long *__restrict__ idx, long long n,
+                               cplx<T> *__restrict__ vals)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        vals[i] = M[idx[i]];
+}
+
+// Rfree of each shell for the current iteration (reconstruct.m:137-146):
+// sum |k - M| / sum |M| over the shell's withheld points, from the values F3
+// captured before the constraint; FP64 sums in a fixed order.  One CTA per shell.
+template <typename T>
+__global__ void __launch_bounds__(256) k_rfree_shells(const cplx<T> *__restrict__ cap, const cplx<T> *__restrict__ vals,
+                                                      const long long *__restrict__ off, int nshells,
+                                                      const Ctl *__restrict__ ctl, double *__restrict__ out)
+{
+    __shared__ double rn[256], rd[256];
+    const int sh = blockIdx.x, t = threadIdx.x;
+    double num = 0, den = 0;
+    for (long long i = off[sh] + t; i < off[sh + 1]; i += 256) {
+        const cplx<T> k = cap[i], v = vals[i];
+        const double dx = (double)k.x - (double)v.x, dy = (double)k.y - (double)v.y;
+        num += sqrt(dx * dx + dy * dy);
+        den += sqrt((double)v.x * (double)v.x + (double)v.y * (double)v.y);
+    }
+    rn[t] = num;
+    rd[t] = den;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) {
+            rn[t] += rn[t + o];
+            rd[t] += rd[t + o];
+        }
+        __syncthreads();
+    }
+    if (t == 0) out[(long long)(ctl->it - 1) * nshells + sh] = rn[0] / rd[0];
+}
+
+template <typename T>
+static void rfree_candidates_t(genfire_ctx *ctx, const cplx<T> *dM, int n1, int n2, int nbins, int64_t *counts,
+                               int64_t *indices)
+{
+    cudaStream_t st = ctx->stream;
+    const long long N = (long long)n1 * n2 * n1;
+    const int nb = (int)cdiv(N, 1024);
+    DevBuf bc(sizeof(int) * nb, st), bo(sizeof(int) * (nb + 1), st), dz(sizeof(double) * nb, st), dt(sizeof(double), st);
+    GF_CUDA(cudaMemsetAsync(dz.p, 0, dz.bytes, st));
+    long long filled = 0;
+    for (int s = 0; s < nbins; ++s) {
+        // edges linspace(0, 1, nbins + 1): (i * 1) / nbins; resRange = -0.05 (reconstruct.m:36, :47-48)
+        const double lo = (double)s / (double)nbins + -0.05, hi = (double)(s + 1) / (double)nbins;
+        k_rfree_mark<T><<<nb, 1024, 0, st>>>(dM, n1, n2, lo, hi, bc.as<int>(), nullptr, nullptr);
+        GF_CHECK_LAUNCH();
+        k_scan_cols<<<1, 1024, 0, st>>>(bc.as<int>(), dz.as<double>(), nb, bo.as<int>(), dt.as<double>());
+        GF_CHECK_LAUNCH();
+        int tot = 0;
+        GF_CUDA(cudaMemcpyAsync(&tot, bo.as<int>() + nb, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GF_CUDA(cudaStreamSynchronize(st));
+        counts[s] = tot;
+        if (indices && tot > 0) {
+            DevBuf out(sizeof(int) * (size_t)tot, st);
+            k_rfree_mark<T><<<nb, 1024, 0, st>>>(dM, n1, n2, lo, hi, bc.as<int>(), bo.as<int>(), out.as<int>());
+            GF_CHECK_LAUNCH();
+            std::vector<int> h((size_t)tot);
+            GF_CUDA(cudaMemcpyAsync(h.data(), out.p, sizeof(int) * (size_t)tot, cudaMemcpyDeviceToHost, st));
+            GF_CUDA(cudaStreamSynchronize(st));
+            for (int k = 0; k < tot; ++k) indices[filled + k] = h[k];
+        }
+        filled += tot;
+    }
+}
+
+void rfree_candidates(genfire_ctx *ctx, const genfire_params &p, const void *M, bool on_device, int nbins,
+                      int64_t *counts, int64_t *indices)
+{
+    if (nbins < 1) fail(GENFIRE_ERR_ARG, "numBinsRfree must be positive.");
+    if (!M || !counts) fail(GENFIRE_ERR_ARG, "measuredK or counts is NULL.");
+    int n1, n2;
+    grid_dims(p, n1, n2);
+    const size_t N = (size_t)n1 * n2 * n1;
+    cudaStream_t st = ctx->stream;
+    const size_t es = p.precision == GENFIRE_PREC_FP64 ? sizeof(double2) : sizeof(float2);
+    DevBuf dM;
+    const void *d = M;
+    if (!on_device) {
+        dM.alloc(es * N, st);
+        GF_CUDA(cudaMemcpyAsync(dM.p, M, es * N, cudaMemcpyHostToDevice, st));
+        d = dM.p;
+    }
+    if (p.precision == GENFIRE_PREC_FP64) rfree_candidates_t<double>(ctx, static_cast<const double2 *>(d), n1, n2, nbins, counts, indices);
+    else rfree_candidates_t<float>(ctx, static_cast<const float2 *>(d), n1, n2, nbins, counts, indices);
+}
+
 // Object in box coordinates from an initial object (D1 x D2 x D1) or zeros.
 // grid: x over e1, y = e2, z = e3
 template <typename T>
@@ -595,6 +733,8 @@ struct ReconBase {
     virtual void profile(int count, double *ms, double *bytes) = 0;
     virtual void tuning(int *variants) const = 0;
     virtual void result(void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device) = 0;
+    virtual void set_rfree(int nshells, const int64_t *counts, const int64_t *indices) = 0;
+    virtual int rfree(double *out) const = 0;
 };
 
 template <typename T> struct ReconT : ReconBase {
@@ -604,7 +744,9 @@ template <typename T> struct ReconT : ReconBase {
     FftPlan pl1, pl2;
     const cplx<T> *tw1, *tw2;
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
-    int m = 0, nparts = 0, tiles1 = 0, ntab = 0;
+    DevBuf rtab, rtaboff, rcap, rvals, rshoff, rhist;  // Rfree monitor
+    int m = 0, nparts = 0, tiles1 = 0, ntab = 0, nshells = 0;
+    long long nrfree = 0;
     double denom = 0;
     int it_done = 0;
     int vF2 = kColAuto, vF3 = kColAuto, vI2 = kColAuto;  // column-pass variants (autotuned)
@@ -772,6 +914,11 @@ template <typename T> struct ReconT : ReconBase {
         b.mode = 1 | 2 | 4;
         b.tab_off = taboff.as<int>(); b.tab = tab.as<TabEntry<T>>(); b.h1 = h1; b.partial = partial.as<double>();
         b.cidx = &c->cidx;
+        if (nshells > 0) {
+            b.rtab_off = rtaboff.as<int>();
+            b.rtab = rtab.as<uint2>();
+            b.rcap = rcap.as<cplx<T>>();
+        }
         return b;
     }
     // I2: dim 2 inverse, box rows out; with_ctl: CTA 0 first forms errK from
@@ -830,6 +977,11 @@ template <typename T> struct ReconT : ReconBase {
         launch_colpass<T>(f2_args(), B3, st, vF2);
         mark();
         launch_colpass<T>(f3_args(), n2, st, vF3);
+        if (nshells > 0) {
+            k_rfree_shells<T><<<nshells, 256, 0, st>>>(rcap.as<cplx<T>>(), rvals.as<cplx<T>>(), rshoff.as<long long>(),
+                                                       nshells, c, rhist.as<double>());
+            GF_CHECK_LAUNCH();
+        }
         mark();
         launch_colpass<T>(i2_args(), B3, st, vI2);
         mark();
@@ -854,6 +1006,7 @@ template <typename T> struct ReconT : ReconBase {
         b[0] = box * Rs + (p.constraintSupport ? box : 0.0) + half_box * S;
         b[1] = half_box * S + half_mid * S;
         b[2] = 2 * half_mid * S + ntab * (double)sizeof(TabEntry<T>) + (h1 * (double)n2 + 1) * 4 + nparts * 8.0;
+        if (nshells > 0) b[2] += nrfree * (8.0 + 3 * S) + (h1 * (double)n2 + 1) * 4;
         b[3] = half_mid * S + half_box * S + nparts * 8.0;
         b[4] = half_box * S + box * Rs;
     }
@@ -912,6 +1065,87 @@ template <typename T> struct ReconT : ReconBase {
         cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
         GF_CUDA(e);
+    }
+
+    // Rfree monitor (reconstruct.m:46-69, :137-146): withheld points of each
+    // shell as 0-based linear indices into the centred grid; the caller has
+    // removed them from the mask given at creation.  Rebuilds the iteration graph.
+    void set_rfree(int nsh, const int64_t *counts, const int64_t *ind) override
+    {
+        if (it_done != 0) fail(GENFIRE_ERR_STATE, "set_rfree: call before the first iteration.");
+        if (nsh < 0 || (nsh > 0 && !counts)) fail(GENFIRE_ERR_ARG, "set_rfree: bad shell count.");
+        cudaStream_t st = ctx->stream;
+        const long long N = (long long)n1 * n2 * n1;
+        std::vector<long long> off((size_t)nsh + 1, 0);
+        for (int s = 0; s < nsh; ++s) {
+            if (counts[s] < 0) fail(GENFIRE_ERR_ARG, "set_rfree: negative count.");
+            off[s + 1] = off[s] + counts[s];
+        }
+        const long long tot = off[nsh];
+        if (tot >= (1LL << 31)) fail(GENFIRE_ERR_ARG, "set_rfree: too many points.");
+        if (tot > 0 && !ind) fail(GENFIRE_ERR_ARG, "set_rfree: indices is NULL.");
+        // capture entries, CSR by F3 column (stable: slot order within a column)
+        const int ncol = h1 * n2;
+        std::vector<int> roff((size_t)ncol + 1, 0), colof((size_t)tot);
+        std::vector<uint2> ent((size_t)tot);
+        for (long long i = 0; i < tot; ++i) {
+            const long long li = ind[i];
+            if (li < 0 || li >= N) fail(GENFIRE_ERR_ARG, "set_rfree: index out of range.");
+            const int c1 = (int)(li % n1), c2 = (int)((li / n1) % n2), c3 = (int)(li / ((long long)n1 * n2));
+            // FFT position (ifftshift); the half spectrum stores q1 < h1, else the mirror -q
+            int q1 = (c1 - n1 / 2 + n1) % n1, q2 = (c2 - n2 / 2 + n2) % n2, q3 = (c3 - n1 / 2 + n1) % n1;
+            uint32_t conj = 0;
+            if (q1 >= h1) {
+                q1 = (n1 - q1) % n1; q2 = (n2 - q2) % n2; q3 = (n1 - q3) % n1;
+                conj = 1;
+            }
+            colof[(size_t)i] = q2 * h1 + q1;
+            ent[(size_t)i] = make_uint2((uint32_t)q3 | ((uint32_t)(q1 % W3) << 16), (uint32_t)i | (conj << 31));
+            ++roff[(size_t)colof[(size_t)i] + 1];
+        }
+        for (int c = 0; c < ncol; ++c) roff[(size_t)c + 1] += roff[(size_t)c];
+        std::vector<uint2> sorted((size_t)std::max(tot, 1LL));
+        {
+            std::vector<int> fill(roff.begin(), roff.end() - 1);
+            for (long long i = 0; i < tot; ++i) sorted[(size_t)fill[(size_t)colof[(size_t)i]]++] = ent[(size_t)i];
+        }
+        std::vector<long long> idx(ind, ind + tot);
+        rtaboff.alloc(sizeof(int) * ((size_t)ncol + 1), st);
+        rtab.alloc(sizeof(uint2) * sorted.size(), st);
+        rcap.alloc(sizeof(cplx<T>) * (size_t)std::max(tot, 1LL), st);
+        rvals.alloc(sizeof(cplx<T>) * (size_t)std::max(tot, 1LL), st);
+        rshoff.alloc(sizeof(long long) * off.size(), st);
+        rhist.alloc(sizeof(double) * (size_t)std::max(nsh, 1) * std::max(p.numIterations, 1), st);
+        DevBuf didx(sizeof(long long) * (size_t)std::max(tot, 1LL), st);
+        GF_CUDA(cudaMemcpyAsync(rtaboff.p, roff.data(), sizeof(int) * roff.size(), cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemcpyAsync(rtab.p, sorted.data(), sizeof(uint2) * sorted.size(), cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemcpyAsync(rshoff.p, off.data(), sizeof(long long) * off.size(), cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaMemsetAsync(rhist.p, 0, rhist.bytes, st));
+        if (tot > 0) {
+            GF_CUDA(cudaMemcpyAsync(didx.p, idx.data(), sizeof(long long) * (size_t)tot, cudaMemcpyHostToDevice, st));
+            k_rfree_gather<T><<<(unsigned)std::min<long long>(cdiv(tot, 256), 4096), 256, 0, st>>>(
+                M.as<cplx<T>>(), didx.as<long long>(), tot, rvals.as<cplx<T>>());
+            GF_CHECK_LAUNCH();
+        }
+        GF_CUDA(cudaStreamSynchronize(st));
+        nshells = nsh;
+        nrfree = tot;
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
+        }
+        build_graph();
+    }
+    // Rfree(shell, iteration) for the iterations run so far, column-major
+    // (nshells x iterations); returns nshells
+    int rfree(double *out) const override
+    {
+        if (nshells > 0 && out && it_done > 0) {
+            GF_CUDA(cudaMemcpyAsync(out, rhist.p, sizeof(double) * (size_t)nshells * it_done, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+            GF_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+        return nshells;
     }
 
     int remaining() const override { return p.numIterations - it_done; }
@@ -1015,6 +1249,11 @@ genfire_recon *recon_create(genfire_ctx *ctx, const genfire_params &p, const voi
 
 void recon_iterate(genfire_recon *r, int count) { r->impl->iterate(count); }
 void recon_tuning(genfire_recon *r, int *variants) { r->impl->tuning(variants); }
+void recon_set_rfree(genfire_recon *r, int nshells, const int64_t *counts, const int64_t *indices)
+{
+    r->impl->set_rfree(nshells, counts, indices);
+}
+int recon_rfree(genfire_recon *r, double *out) { return r->impl->rfree(out); }
 void recon_profile(genfire_recon *r, int count, double *ms, double *bytes) { r->impl->profile(count, ms, bytes); }
 void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, double *Rarr, double *Rarr2, bool on_device)
 {

@@ -104,6 +104,10 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_col_mix(ColPassArg
             }
             __syncthreads();
             if (a.mode & 4) {
+                if (a.rtab) {
+                    capture_rfree<T>(s, a, tile, W, other, [](int q3, int cl) { return Full::idx(q3, cl); });
+                    __syncthreads();
+                }
                 err = apply_table<T, Full>(s, a, tile, W, other);
                 block_partial(err, a.partial + (long long)other * gridDim.x + tile);
                 __syncthreads();

@@ -344,7 +344,31 @@ template <typename T> struct ColPassArgs {
     int nparts;
     double denom;
     double *hist;
+    // Rfree monitor (mode bit 2 only; NULL when off): entries CSR by column as
+    // tab, each {pos as in TabEntry, slot | conj << 31}; the spectrum value at
+    // pos (conjugated for a withheld point whose mirror is the stored one) is
+    // copied to rcap[slot] before the Fourier constraint changes the tile
+    const int *rtab_off;
+    const uint2 *rtab;
+    cplx<T> *rcap;
 };
+
+// Copy of the withheld (Rfree) points of one tile of F3, read before the
+// constraint; idx maps (q3, column in tile) to the tile's shared-memory slot.
+// The caller synchronises before the constraint writes the tile.
+template <typename T, class Idx>
+__device__ __forceinline__ void capture_rfree(const cplx<T> *s, const ColPassArgs<T> &a, int tile, int W, int other,
+                                              Idx idx)
+{
+    const int cid0 = other * a.h1 + tile * W;
+    const int cid1 = min(cid0 + W, other * a.h1 + a.h1);
+    const int e1 = a.rtab_off[cid1];
+    for (int e = a.rtab_off[cid0] + threadIdx.x; e < e1; e += blockDim.x) {
+        const uint2 t = a.rtab[e];
+        const cplx<T> k = s[idx((int)(t.x & 0xFFFFu), (int)(t.x >> 16))];
+        a.rcap[t.y & 0x7FFFFFFFu] = (t.y >> 31) ? cconj(k) : k;
+    }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kTileMaxThreads<T>) k_colpass(ColPassArgs<T> a)
@@ -376,6 +400,10 @@ __global__ void __launch_bounds__(kTileMaxThreads<T>) k_colpass(ColPassArgs<T> a
     }
     __syncthreads();
     if (a.mode & 1) fft_tile<T>(s, a.pl, W, P, a.tw, false);
+    if ((a.mode & 4) && a.rtab) {
+        capture_rfree<T>(s, a, tile, W, other, [P](int q3, int cl) { return q3 * P + cl; });
+        __syncthreads();
+    }
     if (a.mode & 4) {
         // Fourier constraint on the half spectrum (reconstruct.m:135 and :163-165):
         // H(q) = (A(q) + conj(A(-q))) / 2 with A = measuredK on C and the

@@ -339,6 +339,10 @@ __global__ void __launch_bounds__(col_threads<T, N, NC>(), kRegMinBlocks<T>) k_c
             store_stage<T, N, Lay, NST - 1, NC>(s, v, j, c);
             __syncthreads();
             if (a.mode & 4) {
+                if (a.rtab) {
+                    capture_rfree<T>(s, a, tile, W, other, [](int q3, int cl) { return Lay::idx(q3, cl); });
+                    __syncthreads();
+                }
                 err = apply_table<T, Lay>(s, a, tile, W, other);
                 block_partial(err, a.partial + (long long)other * gridDim.x + tile);
                 __syncthreads();

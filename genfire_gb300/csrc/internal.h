@@ -119,6 +119,10 @@ void recon_batch_iterate(genfire_recon_batch *b, int count);
 void recon_batch_destroy(genfire_recon_batch *b);
 void recon_profile(genfire_recon *r, int iterations, double *ms, double *bytes);
 void recon_tuning(genfire_recon *r, int *variants);
+void recon_set_rfree(genfire_recon *r, int nshells, const int64_t *counts, const int64_t *indices);
+int recon_rfree(genfire_recon *r, double *out);
+void rfree_candidates(genfire_ctx *ctx, const genfire_params &p, const void *M, bool on_device, int nbins,
+                      int64_t *counts, int64_t *indices);
 
 // ---------------------------------------------------------------- projector
 // Trilinear projections of a volume view (base pointer, strides vs1 = stride

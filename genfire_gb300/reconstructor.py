@@ -34,6 +34,9 @@ _PROPS = dict(
     # reconstruction parameters (:41-47)
     numIterations=50, oversamplingRatio=3, interpolationCutoffDistance=.7, griddingMethod=1,
     allowMultipleGridMatches=1, calculate_Rfree=0,
+    # read by reconstruct.m:46-60 but not declared by the reference class: the
+    # number of resolution shells, the withheld fraction per shell and the seed
+    numBinsRfree=10, percentValuesForRfree=0.05, RandomSeed=None,
     # axes vectors for phi, theta, psi (:49-52)
     vector1=(0, 0, 1), vector2=(0, 1, 0), vector3=(1, 0, 0),
     particleWindowSize=None,
@@ -236,16 +239,27 @@ class GENFIRE_Reconstructor:
                 break
         else:
             raise GenfireError(_lib.GENFIRE_ERR_ARG, "GENFIRE: measuredK size does not match the projections.")
-        if self.calculate_Rfree == 1:
-            raise GenfireError(_lib.GENFIRE_ERR_UNSUPPORTED, "GENFIRE: calculate_Rfree is not in this build.")
-        print("GENFIRE: Reconstructing... \n")
+        shells = None
         mask = None
         if self.measuredK_mask is not None and not np.array_equal(self.measuredK_mask, self.measuredK != 0):
             mask = self.measuredK_mask
-        rec, errK, errR, Rarr, Rarr2 = self._ctx().reconstruct(
-            p, self.measuredK, support=self.Support, initial=self.initialObject, mask=mask,
-            projections=self.InputProjections if p.monitor_R == 1 else None,
-            angles=self.InputAngles if p.monitor_R == 1 else None)
+        if self.calculate_Rfree == 1:
+            shells, mask = self._withhold_rfree(p, mask)
+        print("GENFIRE: Reconstructing... \n")
+        kw = dict(support=self.Support, initial=self.initialObject, mask=mask,
+                  projections=self.InputProjections if p.monitor_R == 1 else None,
+                  angles=self.InputAngles if p.monitor_R == 1 else None)
+        if shells is None:
+            rec, errK, errR, Rarr, Rarr2 = self._ctx().reconstruct(p, self.measuredK, **kw)
+        else:
+            r = self._ctx().recon(p, self.measuredK, **kw)
+            try:
+                r.set_rfree(shells)
+                r.iterate(p.numIterations)
+                rec, errK, errR, Rarr, Rarr2 = r.result()
+                self.Rfree_complex = r.rfree().astype(np.float32)
+            finally:
+                r.close()
         self.reconstruction = rec
         self.errK = errK
         if p.monitor_R == 1:
@@ -253,6 +267,32 @@ class GENFIRE_Reconstructor:
             self.Rarr_record = Rarr
             self.Rarr2_record = Rarr2
         return self
+
+    def _withhold_rfree(self, p, mask):
+        """Rfree point selection (reconstruct.m:46-67): per shell, the candidates
+        (measuredK ~= 0 in the shell, computed by the library), shuffled, the first
+        floor(n * percentValuesForRfree) (at least one) withheld and cleared from
+        the mask.  The shuffle is numpy's generator seeded with RandomSeed before
+        every shell (the reference re-seeds MATLAB's rng the same way); MATLAB's
+        randperm stream itself is not reproduced.  Returns (shells, mask)."""
+        nb = int(self.numBinsRfree)
+        cands = self._ctx().rfree_candidates(p, self.measuredK, nb)
+        m = np.array(self.measuredK != 0 if mask is None else mask, dtype=bool, order="F", copy=True)
+        flat = m.reshape(-1, order="F")
+        shared = np.random.default_rng()
+        shells = []
+        for s, c in enumerate(cands):
+            rng = np.random.default_rng(self.RandomSeed) if self.RandomSeed is not None else shared
+            cut = int(np.floor(len(c) * float(self.percentValuesForRfree)))
+            if cut == 0:
+                cut = 1
+            if len(c) < cut:
+                raise GenfireError(_lib.GENFIRE_ERR_ARG,
+                                   "GENFIRE: Rfree shell %d has no measured points to withhold." % (s + 1))
+            sel = c[rng.permutation(len(c))][:cut]
+            flat[sel] = False
+            shells.append(sel)
+        return shells, m
 
     # ------------------------------------------------------------------ :194-225
     def ClearCalcVariables(self):

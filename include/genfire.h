@@ -234,6 +234,31 @@ genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b);
  * 2 = register-resident, two columns per thread, -1 = built-in choice. */
 genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants);
 
+/* ---- Rfree monitor -------------------------------------------------------
+ * reconstruct.m:46-69 (selection) and :137-146 (per iteration).
+ * genfire_rfree_candidates: the candidate points of each of nbins shells,
+ *   find(measuredK ~= 0 & Q >= edge(s) - 0.05 & Q < edge(s+1)) with
+ *   edge = linspace(0, 1, nbins + 1) and Q = make_Kspace_indices of the
+ *   measuredK grid (n1 x n2 x n1 from params, as genfire_reconstruct);
+ *   counts[s] receives the number of shell s; indices (NULL: counts only)
+ *   receives the ascending 0-based linear indices of all shells, concatenated.
+ *   measuredK is complex128 (FP64) or complex64 (MIXED), host or device.
+ * The random choice of the withheld points (randperm, :53-60) stays with the
+ * caller: MATLAB's generator is not reproduced here.
+ * genfire_recon_set_rfree: registers the withheld points (0-based centred
+ *   linear indices, counts[s] for shell s, concatenated) of a reconstruction
+ *   created with them already cleared in measuredK_mask (:65); call before the
+ *   first genfire_recon_iterate (and before adding it to a batch).  Each
+ *   iteration then records Rfree(s, it) = sum |k - measuredK| / sum |measuredK|
+ *   over shell s, k = fftn of the object before the Fourier constraint.
+ * genfire_recon_rfree: *nshells, and (rfree not NULL) the values of the
+ *   iterations run so far, column-major nshells x iterations (Rfree_complex). */
+genfire_status genfire_rfree_candidates(genfire_ctx *ctx, const genfire_params *p, const void *measuredK,
+                                        int32_t on_device, int32_t nbins, int64_t *counts, int64_t *indices);
+genfire_status genfire_recon_set_rfree(genfire_recon *r, int32_t nshells, const int64_t *counts,
+                                      const int64_t *indices);
+genfire_status genfire_recon_rfree(genfire_recon *r, int32_t *nshells, double *rfree);
+
 #define GENFIRE_PROFILE_KERNELS 5
 genfire_status genfire_recon_profile(genfire_recon *r, int32_t iterations, double *ms, double *bytes);
 const char *genfire_profile_kernel_name(int32_t k);

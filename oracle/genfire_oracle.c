@@ -995,10 +995,55 @@ static double wall(void)
 #endif
 }
 
+/* Rfree candidate points of shell s (0-based) of nbins (reconstruct.m:47-50):
+ * find(measuredK ~= 0 & Q >= edge(s) + resRange & Q < edge(s+1)) with
+ * edge = linspace(0, 1, nbins + 1) (edge(i) = i / nbins), resRange = -0.05 and
+ * Q = make_Kspace_indices of the measuredK-sized grid.  Writes the ascending
+ * 0-based linear indices to out (if not NULL) and returns their count. */
+int64_t orc_rfree_candidates(int n1, int n2, const double *measuredK, int nbins, int s, int64_t *out)
+{
+    int sz[3] = {n1, n2, n1};
+    size_t N = (size_t)n1 * n2 * n1;
+    double *Q = (double *)malloc(sizeof(double) * N);
+    orc_make_kspace_indices(sz, Q);
+    const double lo = (double)s / (double)nbins + -0.05, hi = (double)(s + 1) / (double)nbins;
+    int64_t cnt = 0;
+    for (size_t i = 0; i < N; ++i) {
+        int nz = measuredK[2 * i] != 0 || measuredK[2 * i + 1] != 0;
+        if (nz && Q[i] >= lo && Q[i] < hi) {
+            if (out) out[cnt] = (int64_t)i;
+            ++cnt;
+        }
+    }
+    free(Q);
+    return cnt;
+}
+
+int orc_reconstruct_rfree(const orc_params *prm, const double *measuredK, const unsigned char *mask,
+                          const unsigned char *support, const double *initial,
+                          const double *projs, const double *angles,
+                          double *rec_out, double *errK, double *errR, double *Rarr, double *Rarr2,
+                          int nshells, const int64_t *rcounts, const int64_t *rind, double *rfree);
+
 int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsigned char *mask,
                     const unsigned char *support, const double *initial,
                     const double *projs, const double *angles,
                     double *rec_out, double *errK, double *errR, double *Rarr, double *Rarr2)
+{
+    return orc_reconstruct_rfree(prm, measuredK, mask, support, initial, projs, angles, rec_out, errK, errR,
+                                 Rarr, Rarr2, 0, NULL, NULL, NULL);
+}
+
+/* reconstruct.m with the Rfree monitor (:137-146): rind holds the withheld
+ * 0-based centred linear indices of nshells shells (rcounts[s] each,
+ * concatenated); the caller has removed them from mask (:65).  Each iteration
+ * writes rfree[s + nshells * (it - 1)] = sum |k(shifted) - M| / sum |M| over
+ * shell s, with k = fftn of the object before the Fourier constraint. */
+int orc_reconstruct_rfree(const orc_params *prm, const double *measuredK, const unsigned char *mask,
+                          const unsigned char *support, const double *initial,
+                          const double *projs, const double *angles,
+                          double *rec_out, double *errK, double *errR, double *Rarr, double *Rarr2,
+                          int nshells, const int64_t *rcounts, const int64_t *rind, double *rfree)
 {
     int D1 = prm->Dim1, D2 = prm->Dim2;
     int n1 = orc_oversampled_size(D1, prm->oversamplingRatio);
@@ -1095,6 +1140,20 @@ int orc_reconstruct(const orc_params *prm, const double *measuredK, const unsign
         }
         double err = num / denom;
         errK[it - 1] = err;
+        if (nshells > 0 && rfree) {
+            int64_t o = 0;
+            for (int sh = 0; sh < nshells; ++sh) {
+                double rn = 0, rd = 0;
+                for (int64_t e = 0; e < rcounts[sh]; ++e, ++o) {
+                    size_t b = (size_t)rind[o];
+                    int c1 = (int)(b % n1), c2 = (int)((b / n1) % n2), c3 = (int)(b / ((size_t)n1 * n2));
+                    size_t a = (size_t)((c1 + (n1 + 1) / 2) % n1) + (size_t)n1 * (((c2 + (n2 + 1) / 2) % n2) + (size_t)n2 * ((c3 + (n1 + 1) / 2) % n1));
+                    rn += hypot(k[2 * a] - measuredK[2 * b], k[2 * a + 1] - measuredK[2 * b + 1]);
+                    rd += hypot(measuredK[2 * b], measuredK[2 * b + 1]);
+                }
+                rfree[(size_t)sh + (size_t)nshells * (it - 1)] = rn / rd;
+            }
+        }
         if (err < bestErr) { bestErr = err; memcpy(best, x, sizeof(double) * N); }
         for (int64_t e = 0; e < nE; ++e)
             if (inC[e]) {

@@ -182,8 +182,20 @@ def delay_indicators(mode):
     return np.full(5, -999.0)
 
 
-def reconstruct(M, n_iter, support, mode=3, positivity=True, use_support=True, initial=None, mask=None):
-    """reconstruct.m:28-194 without the R-factor monitor, with numpy FFTs."""
+def rfree_candidates(M, nbins, shell):
+    """reconstruct.m:47-50: find(M ~= 0 & Q >= edge(s) + resRange & Q < edge(s+1)),
+    edge = linspace(0, 1, nbins + 1), resRange = -0.05; 0-based, column-major."""
+    Q = make_kspace_indices(M.shape).ravel(order="F")
+    lo = shell / nbins + -0.05
+    hi = (shell + 1) / nbins
+    return np.flatnonzero((M.ravel(order="F") != 0) & (Q >= lo) & (Q < hi)).astype(np.int64)
+
+
+def reconstruct(M, n_iter, support, mode=3, positivity=True, use_support=True, initial=None, mask=None,
+                rfree=None):
+    """reconstruct.m:28-194 without the R-factor monitor, with numpy FFTs.  With
+    rfree (a list of withheld 0-based centred linear index arrays, already
+    cleared in mask) also returns Rfree (shells x iterations, :137-146)."""
     n = M.shape
     D = support.shape
     S = np.fft.ifftshift(paddzero(support.astype(np.float64), n))
@@ -206,6 +218,7 @@ def reconstruct(M, n_iter, support, mode=3, positivity=True, use_support=True, i
     cur = 0
     Cs = None
     errK = np.zeros(n_iter)
+    Rf = np.zeros((len(rfree) if rfree is not None else 0, n_iter))
     for it in range(1, n_iter + 1):
         if cur < m and it == changes[cur]:
             last = np.nonzero(changes == it)[0][-1]
@@ -218,11 +231,18 @@ def reconstruct(M, n_iter, support, mode=3, positivity=True, use_support=True, i
             x = x * S
         k = np.fft.fftn(x)
         errK[it - 1] = np.abs(np.abs(k[Es]) - np.abs(Ms[Es])).sum() / denom
+        if rfree is not None:
+            kc = np.fft.fftshift(k).ravel(order="F")
+            Mf = M.ravel(order="F")
+            for sh, idx in enumerate(rfree):
+                Rf[sh, it - 1] = np.abs(kc[idx] - Mf[idx]).sum() / np.abs(Mf[idx]).sum()
         if errK[it - 1] < best_err:
             best_err = errK[it - 1]
             best = x.copy()
         k[Cs] = Ms[Cs]
         x = np.real(np.fft.ifftn(k))
+    if rfree is not None:
+        return stripzero(np.fft.fftshift(best), D), errK, Rf
     return stripzero(np.fft.fftshift(best), D), errK
 
 

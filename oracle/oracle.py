@@ -81,6 +81,11 @@ def lib():
         L.orc_change_points.argtypes = [C.c_int, C.c_int, ip]
         L.orc_reconstruct.restype = C.c_int
         L.orc_reconstruct.argtypes = [C.POINTER(OrcParams), dp, up, up, dp, dp, dp, dp, dp, dp, dp, dp]
+        L.orc_reconstruct_rfree.restype = C.c_int
+        L.orc_reconstruct_rfree.argtypes = [C.POINTER(OrcParams), dp, up, up, dp, dp, dp, dp, dp, dp, dp, dp,
+                                            C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64), dp]
+        L.orc_rfree_candidates.restype = C.c_int64
+        L.orc_rfree_candidates.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_int, C.POINTER(C.c_int64)]
         L.orc_num_threads.restype = C.c_int
         L.orc_last_loop_seconds.restype = C.c_double
         _lib = L
@@ -348,6 +353,43 @@ def change_points(N, m):
     out = np.zeros(m, dtype=np.int32)
     lib().orc_change_points(N, m, _p(out, C.c_int))
     return out
+
+
+def rfree_candidates(measuredK, nbins, shell):
+    """Candidate points of Rfree shell `shell` (0-based) of `nbins`
+    (reconstruct.m:47-50): ascending 0-based linear indices (int64)."""
+    Mc, Mv = _c128_view(measuredK)
+    n1, n2 = Mc.shape[0], Mc.shape[1]
+    cnt = lib().orc_rfree_candidates(n1, n2, _p(Mv, C.c_double), nbins, shell, None)
+    out = np.zeros(max(cnt, 1), dtype=np.int64)
+    lib().orc_rfree_candidates(n1, n2, _p(Mv, C.c_double), nbins, shell, _p(out, C.c_int64))
+    return out[:cnt]
+
+
+def reconstruct_rfree(prm, measuredK, shells, support=None, initial=None, mask=None):
+    """reconstruct.m with the Rfree monitor (:137-146) for the withheld sets
+    `shells` (a list of int64 arrays of 0-based centred linear indices, already
+    removed from `mask`).  Returns (reconstruction, errK, Rfree) with Rfree of
+    shape (len(shells), numIterations)."""
+    Mc, Mv = _c128_view(measuredK)
+    D1, D2 = prm.Dim1, prm.Dim2
+    sup = None if support is None else np.asfortranarray(support, dtype=np.uint8)
+    msk = None if mask is None else np.asfortranarray(mask, dtype=np.uint8)
+    ini = None if initial is None else _f64(initial)
+    N = prm.numIterations
+    counts = np.array([len(s) for s in shells], dtype=np.int64)
+    ind = np.ascontiguousarray(np.concatenate([np.asarray(s, dtype=np.int64) for s in shells])
+                               if len(shells) else np.zeros(1, dtype=np.int64))
+    rec = np.zeros((D1, D2, D1), dtype=np.float64, order="F")
+    errK = np.zeros(N)
+    rfree = np.zeros((len(shells), max(N, 1)), order="F")
+    rc = lib().orc_reconstruct_rfree(C.byref(prm), _p(Mv, C.c_double), _p(msk, C.c_ubyte), _p(sup, C.c_ubyte),
+                                     _p(ini, C.c_double), None, None, _p(rec, C.c_double), _p(errK, C.c_double),
+                                     None, None, None, len(shells), _p(counts, C.c_int64), _p(ind, C.c_int64),
+                                     _p(rfree, C.c_double))
+    if rc != 0:
+        raise ValueError("oracle reconstruct failed (%d)" % rc)
+    return rec, errK, rfree[:, :N]
 
 
 def reconstruct(prm, measuredK, support=None, initial=None, mask=None, projs=None, angles=None):
