@@ -77,13 +77,14 @@ def build(force=False, verbose=False, extra_flags=()):
     return LIB
 
 
-HARNESS_SRC = os.path.join(HERE, "harness", "genfire_run.c")
+HARNESS_SRC = [os.path.join(HERE, "harness", f) for f in ("genfire_run.c", "matio.c")]
 HARNESS = os.path.join(OUT_DIR, "genfire_run")
 
 
 def build_harness():
-    """The standalone C driver (harness/genfire_run.c), linked against libgenfire.so."""
-    cmd = ["gcc", "-O2", "-std=c11", "-I", INCLUDE, HARNESS_SRC, "-o", HARNESS, "-L", OUT_DIR, "-lgenfire",
+    """The standalone C driver (harness/genfire_run.c with the MAT-file reader and
+    writer harness/matio.c), linked against libgenfire.so."""
+    cmd = ["gcc", "-O2", "-std=c11", "-Wall", "-I", INCLUDE] + HARNESS_SRC + ["-o", HARNESS, "-L", OUT_DIR, "-lgenfire",
            "-Wl,-rpath,$ORIGIN", "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -1,0 +1,124 @@
+"""MAT-file (Level 5) reading and writing of the standalone C harness
+(genfire_gb300/harness/matio.c), against scipy.io: plain and zlib-compressed
+variables of every numeric class, logical arrays, small and long names,
+non-numeric variables skipped, malformed files rejected.  CPU only: the
+harness's --mat-info / --mat-copy modes call no GPU function."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+scipy_io = pytest.importorskip("scipy.io")
+
+
+@pytest.fixture(scope="module")
+def harness():
+    from genfire_gb300 import build
+    build.build()
+    return build.HARNESS
+
+
+def _info(harness, path):
+    r = subprocess.run([harness, "--mat-info", path], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    out = {}
+    for tok in r.stdout.split():
+        k, v = tok.split("=", 1)
+        out[k] = v
+    return out
+
+
+def _seq_sum(a):
+    """Sum in column-major order, one term after another (the harness's order)."""
+    f = np.asarray(a, dtype=np.float64).ravel(order="F")
+    return float(np.cumsum(f)[-1]) if f.size else 0.0
+
+
+CLASSES = [np.float64, np.float32, np.int8, np.uint8, np.int16, np.uint16, np.int32, np.uint32, np.int64, np.uint64]
+
+
+@pytest.mark.parametrize("compress", [False, True])
+@pytest.mark.parametrize("dt", CLASSES)
+def test_read_numeric_classes(harness, tmp_path, compress, dt):
+    rng = np.random.default_rng(3)
+    a = np.asfortranarray((rng.random((5, 7, 3)) * 100).astype(dt))
+    f = str(tmp_path / "a.mat")
+    scipy_io.savemat(f, {"pj": a}, do_compression=compress)
+    info = _info(harness, f)
+    assert info["name"] == "pj" and info["dims"] == "5x7x3" and info["complex"] == "0"
+    flat = a.astype(np.float64).ravel(order="F")
+    assert float(info["sum"]) == _seq_sum(a)
+    assert float(info["first"]) == flat[0] and float(info["last"]) == flat[-1]
+
+
+@pytest.mark.parametrize("compress", [False, True])
+def test_first_numeric_after_other_variables(harness, tmp_path, compress):
+    """importdata of a one-array file is that array; text and cells are skipped."""
+    f = str(tmp_path / "b.mat")
+    x = np.arange(12.0).reshape(3, 4, order="F")
+    scipy_io.savemat(f, {"a_note": "projections of the test", "b_cell": np.array([[1.0, "x"]], dtype=object),
+                         "c": x}, do_compression=compress)
+    info = _info(harness, f)
+    assert info["name"] == "c" and info["dims"] == "3x4" and float(info["sum"]) == 66.0
+
+
+@pytest.mark.parametrize("compress", [False, True])
+def test_copy_round_trip(harness, tmp_path, compress):
+    rng = np.random.default_rng(5)
+    src, dst = str(tmp_path / "s.mat"), str(tmp_path / "d.mat")
+    a = np.asfortranarray(rng.standard_normal((64, 64, 9)))
+    scipy_io.savemat(src, {"projections_with_a_long_name": a}, do_compression=compress)
+    r = subprocess.run([harness, "--mat-copy", src, dst], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    back = scipy_io.loadmat(dst)
+    assert np.array_equal(back["projections_with_a_long_name"], a)
+
+
+def test_logical_round_trip(harness, tmp_path):
+    src, dst = str(tmp_path / "s.mat"), str(tmp_path / "d.mat")
+    m = np.asfortranarray(np.random.default_rng(1).random((6, 5, 6)) > 0.5)
+    scipy_io.savemat(src, {"sup": m}, do_compression=True)
+    assert _info(harness, src)["logical"] == "1"
+    r = subprocess.run([harness, "--mat-copy", src, dst], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    # scipy reads logical arrays (its own included) as uint8; the flag is checked on our side
+    back = scipy_io.loadmat(dst)["sup"]
+    assert np.array_equal(back.astype(bool), m) and back.max() == 1
+    assert _info(harness, dst)["logical"] == "1"
+
+
+def test_rejects_bad_files(harness, tmp_path):
+    f = str(tmp_path / "t.mat")
+    scipy_io.savemat(f, {"x": np.arange(1000.0)}, do_compression=True)
+    raw = open(f, "rb").read()
+    for k, data in enumerate([raw[:60], raw[:200], raw[:128] + bytes(40), b"MATLAB 7.3 MAT-file" + bytes(200)]):
+        g = str(tmp_path / ("bad%d.mat" % k))
+        open(g, "wb").write(data)
+        r = subprocess.run([harness, "--mat-info", g], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 1 and r.stderr.strip(), (k, r.stdout)
+    # a flipped byte inside the compressed stream fails its checksum or its codes
+    bad = bytearray(raw)
+    bad[len(bad) // 2] ^= 0x5A
+    g = str(tmp_path / "flip.mat")
+    open(g, "wb").write(bytes(bad))
+    r = subprocess.run([harness, "--mat-info", g], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1
+
+
+REF_DATA = "/root/reference/data_turb3"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_DATA), reason="the reference's data files are not on this machine")
+def test_reference_data_files(harness):
+    """The reference's own compressed MAT files read as scipy reads them."""
+    for fn in sorted(os.listdir(REF_DATA)):
+        if not fn.endswith(".mat"):
+            continue
+        path = os.path.join(REF_DATA, fn)
+        d = {k: v for k, v in scipy_io.loadmat(path).items() if not k.startswith("__")}
+        (name, arr), = d.items()
+        info = _info(harness, path)
+        assert info["name"] == name
+        assert info["dims"] == "x".join(str(s) for s in arr.shape)
+        assert float(info["sum"]) == _seq_sum(arr)
