@@ -308,15 +308,6 @@ __global__ void k_half_from_centered(const cplx<T> *__restrict__ M, int n1, int 
     }
 }
 
-static unsigned grid_for(genfire_ctx *ctx, long long n, int threads)
-{
-    long long b = (n + threads - 1) / threads;
-    long long cap = (long long)ctx->sm_count * 8;
-    if (b > cap) b = cap;
-    if (b < 1) b = 1;
-    return (unsigned)b;
-}
-
 static int round_up(int a, int b) { return (a + b - 1) / b * b; }
 
 // inverse chain: half spectrum Hs (ld1 x n2 x n1) -> real box B1 x B2 x B3
