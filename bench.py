@@ -61,6 +61,23 @@ def dist_setup(args):
     return ws, rank, local, pg
 
 
+def max_over_ranks(t_local, pg, device):
+    """The whole job's time: the slowest rank's, after a barrier (replicas only;
+    no collective runs inside the timed region)."""
+    if not pg:
+        return t_local
+    import torch
+    pg.barrier()
+    t = torch.tensor([t_local], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, t_max, ws):
+    """Units all ranks processed per second of the slowest rank's time."""
+    return units_per_rank * ws / t_max
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons during the timed region."""
 
@@ -219,11 +236,7 @@ def run_ours(args, ws, rank, local, pg):
     ev1.synchronize()
     t_dr = ev0.elapsed_time(ev1) / 1e3
     clk = clocks.stop()
-    if pg:
-        pg.barrier()
-        t = torch.tensor([t_dr], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_dr = float(t.item())
+    t_dr = max_over_ranks(t_dr, pg, "cuda")
     names, ms, by = rec.profile(20)
     tuned = rec.tuning()
     rec.close()
@@ -305,7 +318,7 @@ def run_ours(args, ws, rank, local, pg):
         except Exception as e:  # reported, not fatal
             cpu = {"value": None, "error": str(e)[:200]}
 
-    iters_per_s = K / t_dr * ws
+    iters_per_s = whole_job_rate(K, t_dr, ws)
     res = {
         "metric": METRIC, "value": iters_per_s, "unit": "iters/s", "n_gpus": ws, "steps": K, "warmup": W,
         "ms_per_step": t_dr / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

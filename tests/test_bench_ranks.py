@@ -1,0 +1,65 @@
+"""bench.py's multi-rank path on CPU (gloo, world size 2): the whole-job time is
+the slowest rank's, the rate counts every rank's units, and the reference arm
+runs on rank 0 only.  The GPU legs are replicas: no collective in the timed
+region, so the host logic is all there is to test without GPUs."""
+import multiprocessing as mp
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, ws, port, q):
+    sys.path.insert(0, ROOT)
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws))
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    import bench
+    t = bench.max_over_ranks(0.25 + 0.5 * rank, dist, "cpu")
+    q.put((rank, t, bench.whole_job_rate(100, t, ws)))
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_world2():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    ps = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r for r, _, _ in out] == [0, 1]
+    for _, t, rate in out:
+        assert t == 0.75                  # the slower rank's time on both
+        assert rate == 100 * 2 / 0.75     # units of both ranks over it
+
+
+def test_single_rank_passthrough():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.max_over_ranks(1.5, None, "cpu") == 1.5
+    assert bench.whole_job_rate(30, 1.5, 1) == 20.0
+
+
+def test_reference_arm_rank0_only():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class A:
+        quick = True
+        steps = 1
+    assert bench.run_reference(A(), 2, 1) is None
