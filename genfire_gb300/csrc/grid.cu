@@ -223,7 +223,10 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
     k1a = lo;
     k1b = hi;
     if (fabsf(h1) >= 0.01f) {
-        float b0 = (x - c) / h1, b1 = (x + c) / h1;
+        // bounds through the reciprocal: within a few ulps of the quotients,
+        // which the one-point padding below covers
+        const float ih = 1.0f / h1;
+        float b0 = (x - c) * ih, b1 = (x + c) * ih;
         if (b0 > b1) { const float t = b0; b0 = b1; b1 = t; }
         b0 = fmaxf(b0, (float)lo - 4.f);
         b1 = fminf(b1, (float)hi + 4.f);
@@ -260,8 +263,10 @@ __device__ __forceinline__ int block_exclusive_scan(int x, int *total)
     return woff + inc - x;
 }
 
+// Counts per CTA chunk, and per row (uint16: a row holds at most l1 <= 32769
+// points) so the write pass tests only the rows that hold points.
 __global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__restrict__ geo, SelParams sp,
-                                                          int *__restrict__ counts)
+                                                          int *__restrict__ counts, uint16_t *__restrict__ rowcnt)
 {
     const int p = blockIdx.y, chunk = blockIdx.x;
     const ProjGeom g = geo[p];
@@ -278,6 +283,7 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__res
                 float D, u, v;
                 cnt += sel_test(g, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
             }
+            rowcnt[(long long)p * sp.nrows + ri] = (uint16_t)cnt;
         }
         int tot;
         block_exclusive_scan(cnt, &tot);
@@ -310,6 +316,7 @@ __global__ void __launch_bounds__(1024) k_sel_scan(int *counts, int nchunks, lon
 __global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__restrict__ geo, SelParams sp,
                                                           const int *__restrict__ chunk_off,
                                                           const long long *__restrict__ proj_off,
+                                                          const uint16_t *__restrict__ rowcnt,
                                                           uint32_t *__restrict__ ind, float *__restrict__ dist,
                                                           float *__restrict__ uu, float *__restrict__ vv)
 {
@@ -318,18 +325,13 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__res
     long long base = proj_off[p] + chunk_off[(long long)p * sp.nchunks + chunk];
     for (int it = 0; it < kSelItems; ++it) {
         const int ri = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
-        int cnt = 0, a0 = 1, a1 = 0, i2 = 0, i3 = 0;
+        const int cnt = ri < sp.nrows ? (int)rowcnt[(long long)p * sp.nrows + ri] : 0;
+        int a0 = 1, a1 = 0;
         float K2 = 0.f, K3 = 0.f;
-        if (ri < sp.nrows) {
-            i2 = ri % sp.l2;
-            i3 = ri / sp.l2;
-            K2 = (float)(sp.lo2 + i2);
-            K3 = (float)(sp.lo3 + i3);
+        if (cnt > 0) {
+            K2 = (float)(sp.lo2 + ri % sp.l2);
+            K3 = (float)(sp.lo3 + ri / sp.l2);
             row_range(g, sp, K2, K3, a0, a1);
-            for (int k1 = a0; k1 <= a1; ++k1) {
-                float D, u, v;
-                cnt += sel_test(g, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
-            }
         }
         int tot;
         long long o = base + block_exclusive_scan(cnt, &tot);
@@ -505,49 +507,56 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
     return (long long)(k1 - g.lo1) + (long long)g.l1 * ((k2 - g.lo2) + (long long)g.l2 * (k3 - g.lo3));
 }
 
-// Grid: x over dim 1 (c1, two points per thread, independent loads), y = c2,
-// z = c3, so no index has to be decoded.  Most of the grid is untouched: each
-// thread reads its points' bits of the touched bitmap (and nothing else) and
-// writes zero where the bit is clear; the touched points of the CTA are
-// gathered into a shared list and then averaged by consecutive threads, so
-// the FP64 divisions of the FP64 output (a slow pipe on this part) run in full
-// warps instead of one lane of many warps.
+// Grid: x over dim 1 (c1, two points per thread, independent loads), y over
+// groups of kFinRows values of c2, z = c3, so no index has to be decoded.
+// Most of the grid is untouched: each thread reads its points' bits of the
+// touched bitmap (and nothing else) and writes zero where the bit is clear;
+// the touched points of the CTA's rows are gathered into one shared list and
+// then averaged by consecutive threads, so the FP64 divisions of the FP64
+// output (a slow pipe on this part) run in full warps instead of one lane of
+// many warps.  Several rows per CTA keep the CTA count (and the per-CTA
+// setup) small against the bytes written.
+constexpr int kFinRows = 4;
 template <typename TO>
 __global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
                                                   const double2 *__restrict__ ex, const uint8_t *__restrict__ hx,
                                                   const unsigned *__restrict__ touched, GridSpec g, int n1, int n2,
                                                   int centro, cplx<TO> *__restrict__ M)
 {
-    constexpr int KPT = 2;  // points per thread (independent loads in flight)
-    __shared__ int list[256 * KPT];
+    constexpr int KPT = 2;  // points per thread and row (independent loads in flight)
+    __shared__ int list[256 * KPT * kFinRows];  // (row in group) << 16 | c1
     __shared__ int cnt;
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
-    const int c2 = blockIdx.y, c3 = blockIdx.z;
-    const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
-    {
-        long long li[KPT];
-        bool cj[KPT], in[KPT];
-        unsigned tb[KPT];
+    const int c3 = blockIdx.z;
+    // every bitmap word of the CTA's points is requested before any is used
+    constexpr int NP = KPT * kFinRows;
+    int li[NP];  // gridded-space index (< 2^31)
+    bool cj[NP], in[NP];
+    unsigned tb[NP];
 #pragma unroll
-        for (int q = 0; q < KPT; ++q) {
-            const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
-            in[q] = c1 < n1;
-            li[q] = in[q] ? src_index(g, n1, n2, centro, c1, c2, c3, cj[q]) : 0;
-            tb[q] = in[q] ? touched[li[q] >> 5] : 0u;
-        }
+    for (int k = 0; k < NP; ++k) {
+        const int r = k / KPT, q = k % KPT;
+        const int c2 = blockIdx.y * kFinRows + r;
+        const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
+        in[k] = c1 < n1 && c2 < n2;
+        li[k] = in[k] ? (int)src_index(g, n1, n2, centro, c1, c2, c3, cj[k]) : 0;
+        tb[k] = in[k] ? touched[li[k] >> 5] : 0u;
+    }
 #pragma unroll
-        for (int q = 0; q < KPT; ++q) {
-            if (!in[q]) continue;
-            const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
-            if ((tb[q] >> (li[q] & 31)) & 1u) list[atomicAdd(&cnt, 1)] = c1;
-            else M[row + c1] = mk((TO)0, cj[q] ? -(TO)0 : (TO)0);
-        }
+    for (int k = 0; k < NP; ++k) {
+        if (!in[k]) continue;
+        const int r = k / KPT, q = k % KPT;
+        const int c2 = blockIdx.y * kFinRows + r;
+        const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
+        if ((tb[k] >> (li[k] & 31)) & 1u) list[atomicAdd(&cnt, 1)] = (r << 16) | c1;
+        else M[(long long)n1 * (c2 + (long long)n2 * c3) + c1] = mk((TO)0, cj[k] ? -(TO)0 : (TO)0);
     }
     __syncthreads();
     const int m = cnt;
     for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const int c = list[i];
+        const int c = list[i] & 0xFFFF, c2 = blockIdx.y * kFinRows + (list[i] >> 16);
+        const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
         bool cj;
         const long long li = src_index(g, n1, n2, centro, c, c2, c3, cj);
         if (hx[li]) {
@@ -677,8 +686,9 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     DevBuf dgeo(sizeof(ProjGeom) * P, st);
     GF_CUDA(cudaMemcpyAsync(dgeo.p, geo.data(), sizeof(ProjGeom) * P, cudaMemcpyHostToDevice, st));
     DevBuf counts(sizeof(int) * (size_t)sp.nchunks * P, st), totals(sizeof(long long) * P, st);
+    DevBuf rowcnt(sizeof(uint16_t) * (size_t)sp.nrows * P, st);
     dim3 grid(sp.nchunks, P);
-    k_sel_count<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>());
+    k_sel_count<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), rowcnt.as<uint16_t>());
     GF_CHECK_LAUNCH();
     k_sel_scan<<<P, 1024, 0, st>>>(counts.as<int>(), sp.nchunks, totals.as<long long>());
     GF_CHECK_LAUNCH();
@@ -696,7 +706,7 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     DevBuf doff(sizeof(long long) * P, st);
     GF_CUDA(cudaMemcpyAsync(doff.p, sel.off.data(), sizeof(long long) * P, cudaMemcpyHostToDevice, st));
     k_sel_write<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), doff.as<long long>(),
-                                              sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
+                                              rowcnt.as<uint16_t>(), sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
                                               sel.v.as<float>());
     GF_CHECK_LAUNCH();
     GF_CUDA(cudaStreamSynchronize(st));  // keeps the host-side staging buffers alive until the copies ran
@@ -801,7 +811,7 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
         GF_CHECK_LAUNCH();
     }
     se.mark(3, st);
-    k_finalize<T><<<dim3(cdiv(n1, 512), n2, n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
+    k_finalize<T><<<dim3(cdiv(n1, 512), cdiv(n2, kFinRows), n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
                                                                ex.as<double2>(), hx.as<uint8_t>(),
                                                                touched.as<unsigned>(), g, n1, n2,
                                                                p.DFT_CentroSymmetricity,
