@@ -222,6 +222,9 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo_elem, float hi_elem)
     __nv_bfloat162 t = __floats2bfloat162_rn(lo_elem, hi_elem);  // .x = first (lower address)
     return *reinterpret_cast<uint32_t *>(&t);
 }
+// the two BF16 halves of a packed word as floats (exact)
+__device__ __forceinline__ float bf16_lo_f(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi_f(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
 
 }  // namespace umma
 
@@ -340,14 +343,12 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                         e = cmulf(e, w1);
                         float2 e1 = e;
                         e = cmulf(e, w1);
-                        const float r0h = __bfloat162float(__float2bfloat16_rn(e0.x));
-                        const float r1h = __bfloat162float(__float2bfloat16_rn(e1.x));
-                        const float i0h = __bfloat162float(__float2bfloat16_rn(e0.y));
-                        const float i1h = __bfloat162float(__float2bfloat16_rn(e1.y));
-                        rh[q] = pack_bf16(r0h, r1h);
-                        rl[q] = pack_bf16(e0.x - r0h, e1.x - r1h);
-                        ih[q] = pack_bf16(i0h, i1h);
-                        il[q] = pack_bf16(e0.y - i0h, e1.y - i1h);
+                        // hi: both values rounded in one conversion; lo from the
+                        // exact float values of the packed halves
+                        rh[q] = pack_bf16(e0.x, e1.x);
+                        ih[q] = pack_bf16(e0.y, e1.y);
+                        rl[q] = pack_bf16(e0.x - bf16_lo_f(rh[q]), e1.x - bf16_hi_f(rh[q]));
+                        il[q] = pack_bf16(e0.y - bf16_lo_f(ih[q]), e1.y - bf16_hi_f(ih[q]));
                     }
                     S = cmulf(S, w32);
                     // one 16-byte core-matrix row (k = 8h..8h+7) per array
@@ -467,30 +468,27 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
 
 // Pre-split projections into BF16 hi/lo in the B layout (one 16 KB array per
 // (projection, N chunk, K chunk, hi|lo)); zero beyond D1 x D2.
-__global__ void k_split_projections(const double *__restrict__ proj, int D1, int D2, int P, int nkc, int nnc,
-                                    __nv_bfloat16 *__restrict__ B)
+// Grid: x = (projection, N chunk, K chunk) block of B, y = 1024-element slice
+// of its kBTile elements (four per thread).
+constexpr int kSplitSlice = 1024;
+__global__ void __launch_bounds__(256) k_split_projections(const double *__restrict__ proj, int D1, int D2, int nkc,
+                                                           int nnc, __nv_bfloat16 *__restrict__ B)
 {
     using namespace umma;
-    const long long total = (long long)P * nnc * nkc * kBTile;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-        const int e = (int)(t % kBTile);
-        long long blk = t / kBTile;  // (p * nnc + nc) * nkc + kc
-        const int kc = (int)(blk % nkc);
-        blk /= nkc;
-        const int nc = (int)(blk % nnc);
-        const int p = (int)(blk / nnc);
+    const int blk = blockIdx.x;  // (p * nnc + nc) * nkc + kc
+    const int kc = blk % nkc, nc = (blk / nkc) % nnc, p = blk / (nkc * nnc);
+    const double *src = proj + (long long)p * D1 * D2;
+    __nv_bfloat16 *dst = B + (long long)blk * 2 * kBTile;
+#pragma unroll
+    for (int i = 0; i < kSplitSlice / 256; ++i) {
+        const int e = blockIdx.y * kSplitSlice + i * 256 + threadIdx.x;
         // e is the linear position in the layout: invert kmaj_index
         const int rg = e >> 8, kg = (e >> 6) & 3, rr = (e >> 3) & 7, kk = e & 7;
-        const int row = rg * 8 + rr, k = kg * 8 + kk;
-        const int b = nc * kNC + row, aa = kc * kKC + k;
-        double x = 0.0;
-        if (b < D2 && aa < D1) x = proj[(long long)p * D1 * D2 + aa + (long long)D1 * b];
-        const float xf = (float)x;
+        const int b = nc * kNC + rg * 8 + rr, aa = kc * kKC + kg * 8 + kk;
+        const float xf = (b < D2 && aa < D1) ? (float)src[aa + (long long)D1 * b] : 0.f;
         const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(xf - __bfloat162float(hi));
-        const long long base = (((long long)p * nnc + nc) * nkc + kc) * 2 * kBTile;
-        B[base + e] = hi;
-        B[base + kBTile + e] = lo;
+        dst[e] = hi;
+        dst[kBTile + e] = __float2bfloat16_rn(xf - __bfloat162float(hi));
     }
 }
 
@@ -508,10 +506,9 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     const size_t nB = (size_t)P * nnc * nkc * 2 * kBTile;
     DevBuf B(nB * sizeof(__nv_bfloat16), st);
     {
-        const long long total = (long long)P * nnc * nkc * kBTile;
-        long long blocks = (total + 255) / 256;
-        if (blocks > (long long)ctx->sm_count * 16) blocks = (long long)ctx->sm_count * 16;
-        k_split_projections<<<(unsigned)blocks, 256, 0, st>>>(d_proj, D1, D2, P, nkc, nnc, B.as<__nv_bfloat16>());
+        static_assert(kBTile % kSplitSlice == 0, "split slices");
+        k_split_projections<<<dim3((unsigned)(P * nnc * nkc), kBTile / kSplitSlice), 256, 0, st>>>(
+            d_proj, D1, D2, nkc, nnc, B.as<__nv_bfloat16>());
         GF_CHECK_LAUNCH();
     }
     std::vector<MmaTile> tiles;
