@@ -249,15 +249,26 @@ class GENFIRE_Reconstructor:
         kw = dict(support=self.Support, initial=self.initialObject, mask=mask,
                   projections=self.InputProjections if p.monitor_R == 1 else None,
                   angles=self.InputAngles if p.monitor_R == 1 else None)
-        if shells is None:
+        save_every = int(self.save_loopLength) if int(self.save_temp) == 1 else 0
+        if shells is None and save_every <= 0:
             rec, errK, errR, Rarr, Rarr2 = self._ctx().reconstruct(p, self.measuredK, **kw)
         else:
             r = self._ctx().recon(p, self.measuredK, **kw)
             try:
-                r.set_rfree(shells)
-                r.iterate(p.numIterations)
+                if shells is not None:
+                    r.set_rfree(shells)
+                done = 0
+                while done < p.numIterations:
+                    step = p.numIterations - done
+                    if save_every > 0:
+                        step = min(step, save_every - done % save_every)
+                    r.iterate(step)
+                    done += step
+                    if save_every > 0 and done % save_every == 0:
+                        self._save_temp(r.result()[0], done)
                 rec, errK, errR, Rarr, Rarr2 = r.result()
-                self.Rfree_complex = r.rfree().astype(np.float32)
+                if shells is not None:
+                    self.Rfree_complex = r.rfree().astype(np.float32)
             finally:
                 r.close()
         self.reconstruction = rec
@@ -267,6 +278,17 @@ class GENFIRE_Reconstructor:
             self.Rarr_record = Rarr
             self.Rarr2_record = Rarr2
         return self
+
+    def _save_temp(self, rec, iteration):
+        """reconstruct.m:155-158: the best object so far (cropped, after
+        positivity and support) saved as temp_reconstruction to
+        [saveFilename, num2str(iterationNum), '.mat']."""
+        fn = "%s%d.mat" % (self.saveFilename, iteration)
+        d = os.path.dirname(fn)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        import scipy.io
+        scipy.io.savemat(fn, {"temp_reconstruction": rec})
 
     def _withhold_rfree(self, p, mask):
         """Rfree point selection (reconstruct.m:46-67): per shell, the candidates

@@ -151,3 +151,40 @@ def test_reconstructor_calculate_rfree(lib, ctx):
         assert np.all(np.isfinite(G.Rfree_complex)) and np.all(G.Rfree_complex > 0)
         out.append((G.Rfree_complex, G.errK, G.reconstruction))
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_reconstructor_save_temp(lib, ctx, tmp_path):
+    """save_temp = 1 writes the best object so far every save_loopLength
+    iterations (reconstruct.m:155-158); the last file is the final result, and
+    the staged run equals the one-shot run."""
+    scipy_io = pytest.importorskip("scipy.io")
+    from genfire_gb300.reconstructor import GENFIRE_Reconstructor
+    D, os_ = 8, 2.0
+    M = _measured(9, D, D, os_)
+    outs = []
+    for save in (0, 1):
+        G = GENFIRE_Reconstructor()
+        G.Dim1 = G.Dim2 = D
+        G.NumProjs = 1
+        G.oversamplingRatio = os_
+        G.numIterations = 10
+        G.constraintEnforcementMode = 1
+        G.Support = np.ones((D, D, D), bool)
+        G.measuredK = M
+        G.measuredK_mask = M != 0
+        G.save_temp = save
+        G.save_loopLength = 4
+        G.saveFilename = str(tmp_path / "temp_rec")
+        G = G.reconstruct()
+        outs.append((G.reconstruction, G.errK))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    files = sorted(p.name for p in tmp_path.iterdir())
+    assert files == ["temp_rec4.mat", "temp_rec8.mat"]
+    t8 = scipy_io.loadmat(str(tmp_path / "temp_rec8.mat"))["temp_reconstruction"]
+    # the best object after 8 iterations of the same reconstruction
+    p = params(lib, D, D, 1, oversamplingRatio=os_, numIterations=10, constraintEnforcementMode=1)
+    r = ctx.recon(p, M, support=np.ones((D, D, D), bool))
+    r.iterate(8)
+    rec8 = r.result()[0]
+    r.close()
+    assert np.array_equal(t8, rec8)
