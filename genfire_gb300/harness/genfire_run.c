@@ -13,7 +13,8 @@
  *               [--positivity 0|1] [--support-constraint 0|1]
  *               [--multiple-matches 0|1] [--centro 0|1] [--vector1 x,y,z]
  *               [--vector2 x,y,z] [--vector3 x,y,z] [--precision fp64|mixed]
- *               [--no-rfactor]
+ *               [--no-rfactor] [--save-temp L [--save-prefix results/temp_rec]]
+ *               [--rfree NBINS [--rfree-percent 0.05] [--seed S]]
  *   (defaults: the class defaults of GENFIRE_Reconstructor.m:30-70)
  *
  * Synthetic mode (no --projections) runs fillInFourierGrid_DFT and reconstruct
@@ -192,6 +193,91 @@ static int load(const char *what, const char *path, mat_array *a)
     return 0;
 }
 
+/* reconstruct through the staged entry points: temporary saves every
+ * save_every iterations (reconstruct.m:155-158) and the Rfree monitor
+ * (:46-69, :137-146).  The withheld points of each shell are a random
+ * permutation of its candidates (Fisher-Yates with this file's xorshift
+ * generator, re-seeded before every shell when seed >= 0, as the reference
+ * re-seeds rng; MATLAB's randperm stream itself is not reproduced). */
+static int staged(genfire_ctx *ctx, const genfire_params *p, const void *M, const uint8_t *support, const void *init,
+                  const double *projs, const double *angles, int n1, int n2, int save_every, const char *prefix,
+                  int nbins, double pct, long long seed, void *rec, double *errK, double **rfree_out)
+{
+    const size_t N = (size_t)n1 * n2 * n1, es = p->precision == GENFIRE_PREC_MIXED ? sizeof(float) : sizeof(double);
+    uint8_t *mask = NULL;
+    int64_t *counts = NULL, *ind = NULL, *wcounts = NULL, *wind = NULL;
+    if (nbins > 0) {
+        mask = malloc(N);
+        for (size_t i = 0; i < N; ++i) {
+            if (es == sizeof(float)) mask[i] = ((const float *)M)[2 * i] != 0 || ((const float *)M)[2 * i + 1] != 0;
+            else mask[i] = ((const double *)M)[2 * i] != 0 || ((const double *)M)[2 * i + 1] != 0;
+        }
+        counts = calloc(nbins, sizeof(int64_t));
+        CHECK(genfire_rfree_candidates(ctx, p, M, 0, nbins, counts, NULL));
+        int64_t tot = 0;
+        for (int s = 0; s < nbins; ++s) tot += counts[s];
+        ind = malloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
+        wind = malloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
+        wcounts = calloc(nbins, sizeof(int64_t));
+        CHECK(genfire_rfree_candidates(ctx, p, M, 0, nbins, counts, ind));
+        int64_t o = 0, w = 0;
+        for (int s = 0; s < nbins; o += counts[s], ++s) {
+            if (seed >= 0) {
+                rng_state = 88172645463325252ull ^ (uint64_t)seed;
+                if (!rng_state) rng_state = 1;  /* xorshift needs a nonzero state */
+            }
+            int64_t *c = ind + o;
+            for (int64_t i = counts[s] - 1; i > 0; --i) {  /* Fisher-Yates */
+                const int64_t j = (int64_t)(urand() * (double)(i + 1));
+                const int64_t t = c[i]; c[i] = c[j]; c[j] = t;
+            }
+            int64_t cut = (int64_t)floor((double)counts[s] * pct);
+            if (cut == 0) cut = 1;
+            if (counts[s] < cut) {
+                fprintf(stderr, "GENFIRE: Rfree shell %d has no measured points to withhold.\n", s + 1);
+                return 1;
+            }
+            for (int64_t k = 0; k < cut; ++k) {
+                wind[w + k] = c[k];
+                mask[c[k]] = 0;
+            }
+            wcounts[s] = cut;
+            w += cut;
+        }
+    }
+    genfire_recon *r = NULL;
+    CHECK(genfire_recon_create(ctx, p, M, mask, support, init, projs, angles, 0, &r));
+    genfire_status st = nbins > 0 ? genfire_recon_set_rfree(r, nbins, wcounts, wind) : GENFIRE_OK;
+    const int D1 = p->Dim1, D2 = p->Dim2, Nit = p->numIterations;
+    const int64_t dv[3] = {D1, D2, D1};
+    for (int done = 0; st == GENFIRE_OK && done < Nit;) {
+        int step = Nit - done;
+        if (save_every > 0 && step > save_every - done % save_every) step = save_every - done % save_every;
+        st = genfire_recon_iterate(r, step);
+        done += step;
+        if (st == GENFIRE_OK && save_every > 0 && done % save_every == 0) {
+            st = genfire_recon_result(r, rec, NULL, NULL, NULL, NULL, 0);
+            char fn[1024], err[256] = {0};
+            snprintf(fn, sizeof fn, "%s%d.mat", prefix, done);
+            mat_var v = {"temp_reconstruction", 3, dv, es == sizeof(float) ? MAT_SINGLE : MAT_DOUBLE, rec};
+            if (st == GENFIRE_OK && mat_write(fn, 1, &v, err, sizeof err)) {
+                fprintf(stderr, "GENFIRE: %s\n", err);
+                genfire_recon_destroy(r);
+                return 1;
+            }
+        }
+    }
+    if (st == GENFIRE_OK) st = genfire_recon_result(r, rec, errK, NULL, NULL, NULL, 0);
+    if (st == GENFIRE_OK && nbins > 0) {
+        *rfree_out = malloc(sizeof(double) * (size_t)nbins * (Nit > 0 ? Nit : 1));
+        st = genfire_recon_rfree(r, NULL, *rfree_out);
+    }
+    genfire_recon_destroy(r);
+    CHECK(st);
+    free(mask); free(counts); free(ind); free(wcounts); free(wind);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc > 2 && !strcmp(argv[1], "--mat-info")) return mat_info(argv[2]);
@@ -199,7 +285,10 @@ int main(int argc, char **argv)
     if (argc < 2 || argv[1][0] != '-') return synthetic(argc, argv);
 
     const char *fproj = NULL, *fang = NULL, *fsup = NULL, *finit = NULL, *fres = "Factor_GENFIRE_test_gdref.mat";
-    int want_r = 1;
+    int want_r = 1, save_every = 0, nbins = 0;
+    double rfree_pct = 0.05;
+    long long seed = -1;
+    const char *save_prefix = "./results/temp_rec";
     genfire_params p;
     genfire_params_init(&p);
     p.griddingMethod = 1;  /* the class default (GENFIRE_Reconstructor.m:44) */
@@ -226,6 +315,11 @@ int main(int argc, char **argv)
         else if (!strcmp(k, "--vector2") && !vec3(v, p.vector2)) {}
         else if (!strcmp(k, "--vector3") && !vec3(v, p.vector3)) {}
         else if (!strcmp(k, "--precision")) p.precision = !strcmp(v, "mixed") ? GENFIRE_PREC_MIXED : GENFIRE_PREC_FP64;
+        else if (!strcmp(k, "--save-temp")) save_every = atoi(v);
+        else if (!strcmp(k, "--save-prefix")) save_prefix = v;
+        else if (!strcmp(k, "--rfree")) nbins = atoi(v);
+        else if (!strcmp(k, "--rfree-percent")) rfree_pct = atof(v);
+        else if (!strcmp(k, "--seed")) seed = atoll(v);
         else { fprintf(stderr, "GENFIRE: Invalid option %s provided.\n", k); return 2; }
         i += used;
     }
@@ -295,7 +389,13 @@ int main(int argc, char **argv)
     const int N = p.numIterations;
     void *rec = malloc(es * nv);
     double *errK = malloc(sizeof(double) * (N > 0 ? N : 1));
-    CHECK(genfire_reconstruct(ctx, &p, M, NULL, support, init, pj.re, angles, rec, errK, NULL, NULL, NULL));
+    double *rfree = NULL;
+    if (save_every <= 0 && nbins <= 0) {
+        CHECK(genfire_reconstruct(ctx, &p, M, NULL, support, init, pj.re, angles, rec, errK, NULL, NULL, NULL));
+    } else if (staged(ctx, &p, M, support, init, pj.re, angles, n1, n2, save_every, save_prefix, nbins, rfree_pct,
+                      seed, rec, errK, &rfree)) {
+        return 1;
+    }
     double t2 = now();
     printf("GENFIRE: Reconstruction completed in %.12g seconds.\n\n", round(10 * (t2 - t1)) / 10);
 
@@ -310,22 +410,27 @@ int main(int argc, char **argv)
         CHECK(genfire_rfactor_realspace(ctx, GENFIRE_PREC_FP64, recd, D1, D2, D1, pj.re, D1, D2, P, angles, Rarr, &Rtot,
                                         simu));
     const int64_t dv[3] = {D1, D2, D1}, dk[2] = {1, N}, d1[2] = {1, 1}, dr[2] = {P, 1}, ds[3] = {D1, D2, P};
-    mat_var vars[6] = {
+    const int64_t dfree[2] = {nbins, N};
+    mat_var vars[7] = {
         {"final_Rec", 3, dv, mixed ? MAT_SINGLE : MAT_DOUBLE, rec},
         {"final_errK", 2, dk, MAT_DOUBLE, errK},
         {"final_Kfactor", 2, d1, MAT_DOUBLE, &Kmin},
         {"final_Rfactor", 2, d1, MAT_DOUBLE, &Rtot},
         {"final_Rarray", 2, dr, MAT_DOUBLE, Rarr},
         {"final_simuProjs", 3, ds, MAT_SINGLE, simu},
+        {"final_Rfree", 2, dfree, MAT_DOUBLE, rfree},
     };
+    int nvar = want_r ? 6 : 3;
+    if (rfree) vars[nvar++] = vars[6];
     char err[256] = {0};
-    if (mat_write(fres, want_r ? 6 : 3, vars, err, sizeof err)) {
+    if (mat_write(fres, nvar, vars, err, sizeof err)) {
         fprintf(stderr, "GENFIRE: %s\n", err);
         return 1;
     }
     printf("D=%dx%d P=%d n=%dx%d %s gridding %d: %.3f s; %d iterations: %.3f s; errK min %.6f; Rfactor %.6f; saved %s\n",
            D1, D2, P, n1, n2, mixed ? "mixed" : "fp64", p.griddingMethod, t1 - t0, N, t2 - t1, Kmin, Rtot, fres);
     free(angles); free(support); free(init); free(M); free(rec); free(errK); free(recd); free(Rarr); free(simu);
+    free(rfree);
     mat_free(&pj); mat_free(&an); mat_free(&sp); mat_free(&x0);
     genfire_destroy(ctx);
     return 0;

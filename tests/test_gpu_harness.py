@@ -96,3 +96,29 @@ def test_harness_input_errors(harness, tmp_path):
     r = subprocess.run([harness, "--projections", str(tmp_path / "none.mat"), "--angles", fa], capture_output=True,
                        text=True, timeout=60)
     assert r.returncode == 1 and "cannot open" in r.stderr
+
+
+def test_harness_save_temp_and_rfree(lib, ctx, harness, tmp_path):
+    """--save-temp writes temp_reconstruction every L iterations without
+    changing the result; --rfree withholds points per shell (seeded, so
+    repeatable) and saves final_Rfree (shells x iterations)."""
+    pj, ang, fp, fa = _inputs(ctx, tmp_path, D=12, P=6, seed=7)
+    N = 10
+    base = ["--projections", fp, "--angles", fa, "--gridding", "2", "--oversampling", "2", "--cutoff", "0.4",
+            "--iterations", str(N), "--mode", "1", "--no-rfactor"]
+    plain, saved = str(tmp_path / "plain.mat"), str(tmp_path / "saved.mat")
+    _run(harness, base + ["--results", plain])
+    _run(harness, base + ["--results", saved, "--save-temp", "4", "--save-prefix", str(tmp_path / "tmp_")])
+    a, b = scipy_io.loadmat(plain), scipy_io.loadmat(saved)
+    assert np.array_equal(a["final_Rec"], b["final_Rec"]) and np.array_equal(a["final_errK"], b["final_errK"])
+    assert sorted(p.name for p in tmp_path.glob("tmp_*.mat")) == ["tmp_4.mat", "tmp_8.mat"]
+    assert scipy_io.loadmat(str(tmp_path / "tmp_8.mat"))["temp_reconstruction"].shape == (12, 12, 12)
+    outs = []
+    for k in range(2):
+        f = str(tmp_path / ("rf%d.mat" % k))
+        _run(harness, base + ["--results", f, "--rfree", "4", "--rfree-percent", "0.1", "--seed", "3"])
+        outs.append(scipy_io.loadmat(f))
+    rf = outs[0]["final_Rfree"]
+    assert rf.shape == (4, N) and np.all(np.isfinite(rf)) and np.all(rf > 0)
+    assert np.array_equal(rf, outs[1]["final_Rfree"])
+    assert not np.array_equal(outs[0]["final_errK"], a["final_errK"])  # the withheld points left errK
