@@ -20,6 +20,7 @@
 // inverse passes only produce the box.
 #include "fft.cuh"
 #include "fft_reg.cuh"
+#include "fft_r32.cuh"
 #include "internal.h"
 
 #include <algorithm>
@@ -107,7 +108,15 @@ template <typename T, int N> static void set_reg_attrs()
 // float columns per thread.  The last needs unit column stride and 16-byte
 // aligned column pairs (even strides, aligned bases; tiles start at even
 // columns).
-enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3 };
+enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3, kColR32 = 4 };
+
+// GENFIRE_COL_VARIANT=<v> forces variant v wherever it is valid (tuning and
+// tests); unset, the built-in choice or the autotuner decides
+static int forced_col_variant()
+{
+    const char *e = std::getenv("GENFIRE_COL_VARIANT");
+    return (e && *e) ? std::atoi(e) : kColAuto;
+}
 
 template <typename T> static bool pair_capable(const ColPassArgs<T> &a)
 {
@@ -189,12 +198,16 @@ template <typename T> static void ensure_smem_attrs()
     set_reg_attrs<T, 256>();
     set_reg_attrs<T, 512>();
     set_reg_attrs<T, 1024>();
+    if constexpr (sizeof(T) == 4)
+        GF_CUDA(cudaFuncSetAttribute((const void *)k_col_r32<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)r32_smem<T>()));
     done.insert(dev);
 }
 
 template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
 {
     if (v == kColGeneric) return true;
+    if (v == kColR32) return sizeof(T) == 4 && a.pl.n == kR32N && span_ok(a) && (!(a.mode & 4) || a.W == kR32W);
     if (v == kColMix) return span_ok(a) && mix_capable<T>(a.pl.n);
     if (!reg_capable(a)) return false;
     return v == kColReg1 || (v == kColReg2 && pair_capable(a));
@@ -215,8 +228,15 @@ template <typename T> static int default_col_variant(const ColPassArgs<T> &a)
 template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st, int variant = kColAuto)
 {
     a.P = a.W + 1;
+    const int forced = forced_col_variant();
+    if (forced != kColAuto && col_variant_ok(a, forced)) variant = forced;
     if (variant == kColAuto || !col_variant_ok(a, variant)) variant = default_col_variant(a);
-    if (variant == kColMix) {
+    if (variant == kColR32) {
+        if constexpr (sizeof(T) == 4) {
+            dim3 grid(cdiv(a.ncols, kR32W), other);
+            k_col_r32<T><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
+        }
+    } else if (variant == kColMix) {
         if (!launch_col_mix<T>(a, other, st)) fail(GENFIRE_ERR_STATE, "internal: mixed-radix pass not available.");
     } else if (variant == kColGeneric) {
         const size_t sm = tile_smem<T>(a.pl.n, a.W);
@@ -239,6 +259,10 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     static std::mutex mu;
     static std::map<std::vector<long long>, int> cache;
     ensure_smem_attrs<T>();
+    {
+        const int f = forced_col_variant();
+        if (f != kColAuto && col_variant_ok(a, f)) return f;
+    }
     int dev = 0;
     GF_CUDA(cudaGetDevice(&dev));
     const std::vector<long long> key = {dev, (long long)sizeof(T), a.pl.n, a.mode, a.ncols, other, a.in_cnt,
@@ -255,7 +279,7 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     // (keeps the choice stable against timing noise)
     int best = kColAuto;
     float best_ms = 0, default_ms = -1;
-    for (int v : {kColGeneric, kColReg1, kColReg2, kColMix}) {
+    for (int v : {kColGeneric, kColReg1, kColReg2, kColMix, kColR32}) {
         if (!col_variant_ok(a, v)) continue;
         launch_colpass<T>(a, other, st, v);
         GF_CUDA(cudaEventRecord(e0, st));
@@ -275,9 +299,26 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     return best;
 }
 
+// Row passes of 512 complex64 points run on the radix-32 x 16 engine
+// (GENFIRE_ROW_VARIANT=1 selects the radix-8 register engine instead).
+static bool rows_r32_enabled()
+{
+    const char *e = std::getenv("GENFIRE_ROW_VARIANT");
+    return !(e && e[0] == '1');
+}
+
 template <typename T> static void launch_rows(RowPassArgs<T> a, bool forward, cudaStream_t st)
 {
     a.P = a.W + 1;
+    if constexpr (sizeof(T) == 4) {
+        if (a.pl.n == kR32N && rows_r32_enabled()) {
+            const dim3 grid(cdiv((a.nrows + 1) / 2, kR32W));
+            if (forward) k_row_r2c_r32<T><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
+            else k_row_c2r_r32<T><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
+            GF_CHECK_LAUNCH();
+            return;
+        }
+    }
     if (!try_rows_reg<T>(a, forward, st) && !launch_rows_mix<T>(a, forward, st)) {
         const size_t sm = tile_smem<T>(a.pl.n, a.W);
         const int pairs = (a.nrows + 1) / 2;
