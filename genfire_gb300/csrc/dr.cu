@@ -105,9 +105,10 @@ template <typename T, int N> static void set_reg_attrs()
 
 // Launch variants of a column pass: the generic shared-memory engine, the
 // register-resident engine with one column per thread, or with two adjacent
-// float columns per thread.  The last needs unit column stride and 16-byte
-// aligned column pairs (even strides, aligned bases; tiles start at even
-// columns).
+// float columns per thread (unit column stride and 16-byte aligned column
+// pairs: even strides, aligned bases; tiles start at even columns), the
+// mixed-radix engine, and the radix-32 x 16 engine for 512 complex64 points
+// (fft_r32.cuh).
 enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3, kColR32 = 4 };
 
 // GENFIRE_COL_VARIANT=<v> forces variant v wherever it is valid (tuning and
@@ -213,13 +214,17 @@ template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
     return v == kColReg1 || (v == kColReg2 && pair_capable(a));
 }
 
-// Column pass launcher.  Without a tuned variant: two columns per thread in
-// the fused forward + constraint + inverse pass (two transforms per load),
-// one column per thread in the single-transform passes (twice the resident
-// warps), the mixed-radix register engine for 3 or 5 times a power of two,
-// the generic engine for other lengths.
+// Column pass launcher.  Without a tuned variant: the radix-32 x 16 engine
+// for 512 complex64 points (one exchange per transform: 8-28 % faster than
+// the radix-8 engine on the three column passes at 512^3); otherwise, for
+// powers of two, two columns per thread in the fused forward + constraint +
+// inverse pass (two transforms per load) and one column per thread in the
+// single-transform passes (twice the resident warps); the mixed-radix
+// register engine for 3 or 5 times a power of two; the generic engine for
+// other lengths.
 template <typename T> static int default_col_variant(const ColPassArgs<T> &a)
 {
+    if (col_variant_ok(a, kColR32)) return kColR32;
     if (reg_capable(a)) return ((a.mode & 3) == 3 && pair_capable(a)) ? kColReg2 : kColReg1;
     if (col_variant_ok(a, kColMix)) return kColMix;
     return kColGeneric;

@@ -172,6 +172,10 @@ __global__ void __launch_bounds__(kR32Threads) k_col_r32(ColPassArgs<T> a)
 // part, row b the imaginary part), sixteen threads per pair with the index
 // along the row fastest within a warp (64-byte row segments per access).
 using R32RowLay = RowLayout<kR32N, kR32W>;
+// elements whose loads are in flight together in the forward row pass: 8 keeps
+// the pass at 118 registers (4 CTAs per SM); 16 and 32 cost occupancy and
+// measured 13 % and 54 % slower at 512^3
+constexpr int kRowLoadGroup = 8;
 static_assert(R32RowLay::SIZE <= kR32Elems, "row tile fits the pass's buffer");
 
 template <typename T>
@@ -187,13 +191,13 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
     const long long o0 = (long long)r0 * a.B1, o1 = o0 + a.B1;
     cplx<T> x[32];
     // positivity and support (reconstruct.m:126-131) on the way in; the loads
-    // of each quarter of the elements are in flight together
+    // of each group of kRowLoadGroup elements are in flight together
 #pragma unroll
-    for (int m0 = 0; m0 < 32; m0 += 8) {
-        T xa[8], xb[8];
-        uint8_t sa[8], sb[8];
+    for (int m0 = 0; m0 < 32; m0 += kRowLoadGroup) {
+        T xa[kRowLoadGroup], xb[kRowLoadGroup];
+        uint8_t sa[kRowLoadGroup], sb[kRowLoadGroup];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < kRowLoadGroup; ++i) {
             int e = t + 16 * (m0 + i) + a.c1;
             if (e >= kR32N) e -= kR32N;
             const bool in = e < a.B1;
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
             sb[i] = (a.support && in && ok1) ? a.support[o1 + e] : (uint8_t)1;
         }
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
+        for (int i = 0; i < kRowLoadGroup; ++i) {
             T va = xa[i], vb = xb[i];
             if (a.positivity) {
                 if (va < (T)0) va = 0;

@@ -230,8 +230,11 @@ genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b);
  * each candidate on the problem's own buffers at creation; the environment
  * variable GENFIRE_AUTOTUNE=0 keeps the built-in choice): variants[0..2] for
  * the dim-2 forward, the fused dim-3 and the dim-2 inverse pass; 0 = generic
- * shared-memory engine, 1 = register-resident, one column per thread,
- * 2 = register-resident, two columns per thread, -1 = built-in choice. */
+ * shared-memory engine, 1 = register-resident radix 8, one column per thread,
+ * 2 = the same with two columns per thread, 3 = mixed radix (3 or 5 times a
+ * power of two), 4 = radix 32 x 16 for 512 complex64 points (one shared-memory
+ * exchange per transform), -1 = built-in choice.  GENFIRE_COL_VARIANT=<v>
+ * forces variant v wherever it is valid. */
 genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants);
 
 /* ---- Rfree monitor -------------------------------------------------------
