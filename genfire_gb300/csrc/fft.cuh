@@ -104,6 +104,100 @@ template <typename T> struct Dft<8, T> {
     }
 };
 
+// Single-precision radix 4 and 8 in packed FP32 pairs (add/sub/fma/mul
+// .rn.f32x2 of sm_100-class parts: one instruction for both halves of a
+// complex value).  Each pair operation rounds as the two scalar operations of
+// the generic versions above, so the results are the same bit for bit;
+// multiplying by -i or +i is a swap of the halves and an exact sign product.
+// The twiddle products elsewhere stay scalar: their packed form needs
+// (re, re) / (im, im) operand pairs, which cost more than they saved.
+typedef unsigned long long f32x2_t;
+__device__ __forceinline__ f32x2_t pk2(float2 a)
+{
+    f32x2_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2_t r)
+{
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ f32x2_t add2(f32x2_t a, f32x2_t b)
+{
+    f32x2_t r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2_t sub2(f32x2_t a, f32x2_t b)
+{
+    f32x2_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2_t mul2(f32x2_t a, f32x2_t b)
+{
+    f32x2_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2_t fma2(f32x2_t a, f32x2_t b, f32x2_t c)
+{
+    f32x2_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ f32x2_t swap2(f32x2_t a)
+{
+    const float2 v = upk2(a);
+    return pk2(make_float2(v.y, v.x));
+}
+
+// (The order of the operations below is the one that kept the 512-point
+// column pass at 91 registers; other orders of the same operations took 128.)
+template <> struct Dft<4, float> {
+    static __device__ __forceinline__ void run(float2 *v, bool inv, const float2 *, int)
+    {
+        const f32x2_t a0 = pk2(v[0]), a1 = pk2(v[1]), a2 = pk2(v[2]), a3 = pk2(v[3]);
+        const f32x2_t s02 = add2(a0, a2), d02 = sub2(a0, a2), s13 = add2(a1, a3), d13 = sub2(a1, a3);
+        // -i d13 (forward) = swap(d13) (1, -1); +i d13 (inverse) = swap(d13) (-1, 1)
+        const f32x2_t sw = swap2(d13);
+        const f32x2_t sg = inv ? pk2(make_float2(-1.f, 1.f)) : pk2(make_float2(1.f, -1.f));
+        v[0] = upk2(add2(s02, s13));
+        v[2] = upk2(sub2(s02, s13));
+        v[1] = upk2(fma2(sw, sg, d02));
+        const f32x2_t ng = inv ? pk2(make_float2(1.f, -1.f)) : pk2(make_float2(-1.f, 1.f));
+        v[3] = upk2(fma2(sw, ng, d02));
+    }
+};
+
+template <> struct Dft<8, float> {
+    static __device__ __forceinline__ void run(float2 *v, bool inv, const float2 *tw, int n)
+    {
+        float2 e[4] = {v[0], v[2], v[4], v[6]};
+        float2 o[4] = {v[1], v[3], v[5], v[7]};
+        Dft<4, float>::run(e, inv, tw, n);
+        Dft<4, float>::run(o, inv, tw, n);
+        const float c = 0.70710678118654752440f;
+        const f32x2_t pp = pk2(make_float2(1.f, -1.f)), mp = pk2(make_float2(-1.f, 1.f));
+        const f32x2_t cc = pk2(make_float2(c, c));
+        const f32x2_t o1 = pk2(o[1]), o2 = pk2(o[2]), o3 = pk2(o[3]);
+        const f32x2_t s1 = swap2(o1), s2 = swap2(o2), s3 = swap2(o3);
+        // o W8 = c (o + swap(o) sg), o W8^2 = swap(o) sg, o W8^3 = c (swap(o) sg - o),
+        // sg = (1, -1) forward, (-1, 1) inverse (W8 = exp(-+ i pi / 4))
+        const f32x2_t sg = inv ? mp : pp;
+        const f32x2_t r1 = mul2(fma2(s1, sg, o1), cc);
+        const f32x2_t r2 = mul2(s2, sg);
+        const f32x2_t r3 = mul2(sub2(mul2(s3, sg), o3), cc);
+        const f32x2_t e0 = pk2(e[0]), e1 = pk2(e[1]), e2 = pk2(e[2]), e3 = pk2(e[3]), o0 = pk2(o[0]);
+        v[0] = upk2(add2(e0, o0)); v[4] = upk2(sub2(e0, o0));
+        v[1] = upk2(add2(e1, r1)); v[5] = upk2(sub2(e1, r1));
+        v[2] = upk2(add2(e2, r2)); v[6] = upk2(sub2(e2, r2));
+        v[3] = upk2(add2(e3, r3)); v[7] = upk2(sub2(e3, r3));
+    }
+};
+
 template <typename T> struct Dft<3, T> {
     static __device__ __forceinline__ void run(cplx<T> *v, bool inv, const cplx<T> *, int)
     {

@@ -5,6 +5,8 @@
 // fft_reg.cuh needs two, and its exchanges are what bound those passes.
 // Thread t (0..15) of a column holds the elements t + 16 m (m = 0..31) before
 // and after a transform:
+// The radix-4 and radix-8 butterflies are the packed-pair (f32x2) ones of
+// fft.cuh for complex64.
 //   stage 1: Y_t[k1] = sum_m x[t + 16 m] W32^(m k1) in registers
 //            (m = 8a + b: radix 4 over a, rotation W32^(b k1'), radix 8 over b),
 //            then times W512^(t k1) from the twiddle table;
@@ -51,106 +53,6 @@ template <typename T> __device__ __forceinline__ cplx<T> w32(int j)
     return mk((T)c, (T)-s);
 }
 
-// The butterflies' complex additions as packed FP32 pairs (add/sub/fma/mul
-// .rn.f32x2 on sm_100-class parts: one instruction for both halves of a
-// complex value).  Each operation rounds as the two scalar ones it replaces,
-// so the results are those of Dft<4> and Dft<8> bit for bit.  The twiddle
-// products stay scalar: their operands would need (re, re) / (im, im) pairs,
-// and building those cost more than they saved (measured).
-typedef unsigned long long f32x2_t;
-__device__ __forceinline__ f32x2_t pk2(float2 a)
-{
-    f32x2_t r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
-    return r;
-}
-__device__ __forceinline__ float2 upk2(f32x2_t r)
-{
-    float2 a;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
-    return a;
-}
-__device__ __forceinline__ f32x2_t add2(f32x2_t a, f32x2_t b)
-{
-    f32x2_t r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2_t sub2(f32x2_t a, f32x2_t b)
-{
-    f32x2_t r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2_t mul2(f32x2_t a, f32x2_t b)
-{
-    f32x2_t r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2_t fma2(f32x2_t a, f32x2_t b, f32x2_t c)
-{
-    f32x2_t r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-__device__ __forceinline__ f32x2_t swap2(f32x2_t a)
-{
-    const float2 v = upk2(a);
-    return pk2(make_float2(v.y, v.x));
-}
-
-// radix 4 in place: v[k] = sum_r v[r] W4^(rk); -i d (forward) is swap(d) * (1, -1),
-// +i d (inverse) is swap(d) * (-1, 1), both exact
-template <bool INV> __device__ __forceinline__ void dft4_x2(float2 *v)
-{
-    const f32x2_t a0 = pk2(v[0]), a1 = pk2(v[1]), a2 = pk2(v[2]), a3 = pk2(v[3]);
-    const f32x2_t s02 = add2(a0, a2), d02 = sub2(a0, a2), s13 = add2(a1, a3), d13 = sub2(a1, a3);
-    const f32x2_t sw = swap2(d13);
-    const f32x2_t sg = INV ? pk2(make_float2(-1.f, 1.f)) : pk2(make_float2(1.f, -1.f));
-    v[0] = upk2(add2(s02, s13));
-    v[2] = upk2(sub2(s02, s13));
-    v[1] = upk2(fma2(sw, sg, d02));
-    const f32x2_t ng = INV ? pk2(make_float2(1.f, -1.f)) : pk2(make_float2(-1.f, 1.f));
-    v[3] = upk2(fma2(sw, ng, d02));
-}
-
-// radix 8 in place: radix 4 on the even and odd halves, the odd half rotated
-// by W8^k (W8 = exp(-+ i pi / 4)), then the final additions
-template <bool INV> __device__ __forceinline__ void dft8_x2(float2 *v)
-{
-    float2 e[4] = {v[0], v[2], v[4], v[6]};
-    float2 o[4] = {v[1], v[3], v[5], v[7]};
-    dft4_x2<INV>(e);
-    dft4_x2<INV>(o);
-    const float c = 0.70710678118654752440f;
-    const f32x2_t pp = pk2(make_float2(1.f, -1.f)), mp = pk2(make_float2(-1.f, 1.f)), cc = pk2(make_float2(c, c));
-    const f32x2_t o1 = pk2(o[1]), o2 = pk2(o[2]), o3 = pk2(o[3]);
-    const f32x2_t s1 = swap2(o1), s2 = swap2(o2), s3 = swap2(o3);
-    // o W8 = c (o + swap(o) sg), o W8^2 = swap(o) sg, o W8^3 = c (swap(o) sg - o),
-    // sg = (1, -1) forward, (-1, 1) inverse
-    const f32x2_t sg = INV ? mp : pp;
-    const f32x2_t r1 = mul2(fma2(s1, sg, o1), cc);
-    const f32x2_t r2 = mul2(s2, sg);
-    const f32x2_t r3 = mul2(sub2(mul2(s3, sg), o3), cc);
-    const f32x2_t e0 = pk2(e[0]), e1 = pk2(e[1]), e2 = pk2(e[2]), e3 = pk2(e[3]), o0 = pk2(o[0]);
-    v[0] = upk2(add2(e0, o0)); v[4] = upk2(sub2(e0, o0));
-    v[1] = upk2(add2(e1, r1)); v[5] = upk2(sub2(e1, r1));
-    v[2] = upk2(add2(e2, r2)); v[6] = upk2(sub2(e2, r2));
-    v[3] = upk2(add2(e3, r3)); v[7] = upk2(sub2(e3, r3));
-}
-
-template <typename T, bool INV> __device__ __forceinline__ void r32_dft4(cplx<T> *v)
-{
-    if constexpr (sizeof(T) == 4) dft4_x2<INV>(v);
-    else Dft<4, T>::run(v, INV, nullptr, 4);
-}
-template <typename T, bool INV> __device__ __forceinline__ void r32_dft8(cplx<T> *v)
-{
-    if constexpr (sizeof(T) == 4) dft8_x2<INV>(v);
-    else Dft<8, T>::run(v, INV, nullptr, 8);
-}
-
 // One 512-point transform of the thread's 32 elements.  In: slot m holds
 // element t + 16 m.  Out: slot s holds element t + 16 r32_out_m(s).  Uses
 // the CTA's exchange buffer (synchronises before and after writing it).
@@ -166,13 +68,13 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
         cplx<T> u[4] = {x[b], x[8 + b], x[16 + b], x[24 + b]};
-        r32_dft4<T, INV>(u);
+        Dft<4, T>::run(u, INV, nullptr, 4);
 #pragma unroll
         for (int k = 0; k < 4; ++k) x[8 * k + b] = (b && k) ? ctw(u[k], w32<T>(b * k), INV) : u[k];
     }
     // radix 8 over b: slots 8 k1' .. 8 k1' + 7 -> Y[k1' + 4 k2] in slot 8 k1' + k2
 #pragma unroll
-    for (int kp = 0; kp < 4; ++kp) r32_dft8<T, INV>(&x[8 * kp]);
+    for (int kp = 0; kp < 4; ++kp) Dft<8, T>::run(&x[8 * kp], INV, nullptr, 8);
     // W512^(t k1) and the exchange: S[k1][t]
     __syncthreads();  // the buffer may still be read by the previous step
     cplx<T> *Sc = S + c * kR32ColStride;
@@ -194,13 +96,13 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             cplx<T> u[4] = {x[16 * h + q], x[16 * h + 4 + q], x[16 * h + 8 + q], x[16 * h + 12 + q]};
-            r32_dft4<T, INV>(u);
+            Dft<4, T>::run(u, INV, nullptr, 4);
 #pragma unroll
             for (int k = 0; k < 4; ++k) x[16 * h + 4 * k + q] = (q && k) ? ctw(u[k], w32<T>(2 * q * k), INV) : u[k];
         }
         // radix 4 over q: slots 16h + 4k2' .. +3 -> X[k1 + 32 (k2' + 4 k3)] in slot 16h + 4k2' + k3
 #pragma unroll
-        for (int kp = 0; kp < 4; ++kp) r32_dft4<T, INV>(&x[16 * h + 4 * kp]);
+        for (int kp = 0; kp < 4; ++kp) Dft<4, T>::run(&x[16 * h + 4 * kp], INV, nullptr, 4);
     }
 }
 
