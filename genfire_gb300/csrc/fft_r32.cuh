@@ -61,14 +61,41 @@ __device__ __forceinline__ constexpr int r32_out_m(int s)
     return (s >> 4) + 2 * (((s & 15) >> 2) + 4 * (s & 3));
 }
 
-template <typename T, bool INV>
+// Radix 4 of (v0, 0, 0, v3): X[k] = v0 + v3 W4^(3k), the same operations as
+// Dft<4> applied to those inputs (v0 + 0 and 0 - v3 are exact).
+template <typename T, bool INV> __device__ __forceinline__ void dft4_outer(cplx<T> (&u)[4])
+{
+    if constexpr (sizeof(T) == 4) {
+        // packed pairs: +i v = swap(v) (-1, 1), -i v = swap(v) (1, -1)
+        const f32x2_t v0 = pk2(u[0]), v3 = pk2(u[3]), sw = swap2(v3);
+        const f32x2_t sp = INV ? pk2(make_float2(1.f, -1.f)) : pk2(make_float2(-1.f, 1.f));
+        u[0] = upk2(add2(v0, v3));
+        u[2] = upk2(sub2(v0, v3));
+        u[1] = upk2(fma2(sw, sp, v0));
+        const f32x2_t sn = INV ? pk2(make_float2(-1.f, 1.f)) : pk2(make_float2(1.f, -1.f));
+        u[3] = upk2(fma2(sw, sn, v0));
+    } else {
+        const cplx<T> v0 = u[0], v3 = u[3];
+        const cplx<T> r = INV ? mul_mi(v3) : mul_pi(v3);  // W4^3 = +i forward, -i inverse
+        u[0] = cadd(v0, v3);
+        u[2] = csub(v0, v3);
+        u[1] = cadd(v0, r);
+        u[3] = csub(v0, r);
+    }
+}
+
+// ZIN: the elements of slots 8..23 are known to be zero (the centred half of
+// a box transform: entries t + 16 m + 128 mod 512 below 256 lie in slots
+// 0..7 and 24..31), so the first radix-4 stage takes two inputs.
+template <typename T, bool INV, bool ZIN = false>
 __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int t, const cplx<T> *__restrict__ tw)
 {
     // stage 1, radix 4 over a: slot 8a + b -> Z_b[k1'] in slot 8 k1' + b, rotated by W32^(b k1')
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
         cplx<T> u[4] = {x[b], x[8 + b], x[16 + b], x[24 + b]};
-        Dft<4, T>::run(u, INV, nullptr, 4);
+        if constexpr (ZIN) dft4_outer<T, INV>(u);
+        else Dft<4, T>::run(u, INV, nullptr, 4);
 #pragma unroll
         for (int k = 0; k < 4; ++k) x[8 * k + b] = (b && k) ? ctw(u[k], w32<T>(b * k), INV) : u[k];
     }
@@ -106,8 +133,18 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
     }
 }
 
-// Column pass (the contract of k_colpass) for n = 512.
-template <typename T>
+// slots of a transform's output (slot s holds element t + 16 r32_out_m(s)) that
+// the centred half of a box keeps: r32_out_m(s) in 0..7 or 24..31
+__device__ __forceinline__ constexpr bool r32_keep(int s)
+{
+    return r32_out_m(s) < 8 || r32_out_m(s) >= 24;
+}
+
+// Column pass (the contract of k_colpass) for n = 512.  ZIN: the input is the
+// centred half of a box (in_cnt 256, in_c 128) and the pass starts with a
+// forward transform; ZOUT: only the centred half is written (out_cnt 256,
+// out_c 128), so the final transform's other outputs are never formed.
+template <typename T, bool ZIN, bool ZOUT>
 __global__ void __launch_bounds__(kR32Threads) k_col_r32(ColPassArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -124,6 +161,10 @@ __global__ void __launch_bounds__(kR32Threads) k_col_r32(ColPassArgs<T> a)
         const unsigned idim = (unsigned)a.in_dim;
 #pragma unroll
         for (int m = 0; m < 32; ++m) {
+            if (ZIN && m >= 8 && m < 24) {
+                x[m] = mk((T)0, (T)0);
+                continue;
+            }
             int e = t + 16 * m + a.in_c;
             if (e >= kR32N) e -= kR32N;
             x[m] = (cv && e < a.in_cnt) ? in[(unsigned)e * idim] : mk((T)0, (T)0);
@@ -132,7 +173,7 @@ __global__ void __launch_bounds__(kR32Threads) k_col_r32(ColPassArgs<T> a)
     ErrAcc<T> err = 0;
     bool fwd_layout = false;  // slots in the output order of a transform
     if (a.mode & 1) {
-        r32_fft<T, false>(x, s, c, t, twp);
+        r32_fft<T, false, ZIN>(x, s, c, t, twp);
         fwd_layout = true;
     }
     if (a.mode & 2) {
@@ -163,6 +204,7 @@ __global__ void __launch_bounds__(kR32Threads) k_col_r32(ColPassArgs<T> a)
     const unsigned odim = (unsigned)a.out_dim;
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) {
+        if (ZOUT && !r32_keep(sl)) continue;
         int e = t + 16 * r32_out_m(sl) + a.out_c;
         if (e >= kR32N) e -= kR32N;
         if (e < a.out_cnt) out[(unsigned)e * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
@@ -180,7 +222,8 @@ using R32RowLay = RowLayout<kR32N, kR32W>;
 constexpr int kRowLoadGroup = 8;
 static_assert(R32RowLay::SIZE <= kR32Elems, "row tile fits the pass's buffer");
 
-template <typename T>
+// ZIN: the rows are the centred half of the transform (B1 256, c1 128)
+template <typename T, bool ZIN>
 __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -200,6 +243,11 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
         uint8_t sa[kRowLoadGroup], sb[kRowLoadGroup];
 #pragma unroll
         for (int i = 0; i < kRowLoadGroup; ++i) {
+            if (ZIN && m0 + i >= 8 && m0 + i < 24) {
+                xa[i] = xb[i] = (T)0;
+                sa[i] = sb[i] = 1;
+                continue;
+            }
             int e = t + 16 * (m0 + i) + a.c1;
             if (e >= kR32N) e -= kR32N;
             const bool in = e < a.B1;
@@ -218,7 +266,7 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
             x[m0 + i] = mk(va * (T)sa[i], vb * (T)sb[i]);
         }
     }
-    r32_fft<T, false>(x, s, c, t, a.tw);
+    r32_fft<T, false, ZIN>(x, s, c, t, a.tw);
     __syncthreads();  // the exchange buffer becomes the natural-order tile
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) s[R32RowLay::idx(t + 16 * r32_out_m(sl), c)] = x[sl];
@@ -234,7 +282,8 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
     }
 }
 
-template <typename T>
+// ZOUT: only the centred half of each row is written (B1 256, c1 128)
+template <typename T, bool ZOUT>
 __global__ void __launch_bounds__(kR32Threads) k_row_c2r_r32(RowPassArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -272,6 +321,7 @@ __global__ void __launch_bounds__(kR32Threads) k_row_c2r_r32(RowPassArgs<T> a)
     r32_fft<T, true>(x, s, c, t, a.tw);  // synchronises before it reuses the buffer
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) {
+        if (ZOUT && !r32_keep(sl)) continue;
         int e = t + 16 * r32_out_m(sl) + a.c1;
         if (e >= kR32N) e -= kR32N;
         if (e < a.B1) {

@@ -94,3 +94,24 @@ def test_r32_row_passes_reconstruct(lib, ctx, oracle, D1, D2, mode, pos, sup):
     reco, errKo, _, _, _ = oracle.reconstruct(oracle.make_params(D1, D2, 1, **kw), M, support=support)
     assert np.abs(errK - errKo).max() < 1e-4
     assert rel(rec, reco) < 1e-4
+
+
+@pytest.mark.parametrize("D,os_", [(256, 2.0), (200, 2.56)])
+def test_r32_box_pruned_passes(lib, ctx, oracle, D, os_):
+    """n = 512 grids: a 256 box (oversampling 2) is the centred-half case the
+    pruned variants take (the dim-1 forward row pass, the fused dim-3 pass and
+    the dim-2 and dim-1 inverses); a 200 box (oversampling 2.56) takes the
+    unpruned ones.  20 k random measured points keep the table small."""
+    D1 = D2 = D
+    N = 2
+    n1, n2 = int(np.floor(D1 * os_ + 0.5)), int(np.floor(D2 * os_ + 0.5))
+    assert n1 == n2 == 512
+    rng = np.random.default_rng(D1 + D2)
+    M = np.zeros((n1, n2, n1), dtype=np.complex128, order="F")
+    idx = rng.integers(0, [n1, n2, n1], size=(20000, 3))
+    M[idx[:, 0], idx[:, 1], idx[:, 2]] = rng.standard_normal(20000) + 1j * rng.standard_normal(20000)
+    kw = dict(oversamplingRatio=os_, numIterations=N, constraintEnforcementMode=3)
+    rec, errK, _, _, _ = ctx.reconstruct(params(lib, D1, D2, 1, precision="mixed", **kw), M.astype(np.complex64))
+    reco, errKo, _, _, _ = oracle.reconstruct(oracle.make_params(D1, D2, 1, **kw), M)
+    assert np.abs(errK - errKo).max() < 1e-4
+    assert rel(rec, reco) < 1e-4
