@@ -144,8 +144,10 @@ __device__ __forceinline__ constexpr bool r32_keep(int s)
 // centred half of a box (in_cnt 256, in_c 128) and the pass starts with a
 // forward transform; ZOUT: only the centred half is written (out_cnt 256,
 // out_c 128), so the final transform's other outputs are never formed.
+// Occupancy: 5 CTAs per SM (<= 96 registers) for the single-transform passes;
+// the fused pass keeps 4 (at 96 registers it spills, and measured no faster).
 template <typename T, bool ZIN, bool ZOUT>
-__global__ void __launch_bounds__(kR32Threads) k_col_r32(ColPassArgs<T> a)
+__global__ void __launch_bounds__(kR32Threads, (ZIN && ZOUT) ? 4 : 5) k_col_r32(ColPassArgs<T> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
