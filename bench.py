@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-problems leg")
     ap.add_argument("--batch-steps", type=int, default=300, help="iterations per problem in the batched leg")
     ap.add_argument("--quick", action="store_true", help="small workload (for checking the script)")
+    ap.add_argument("--workload", default=WORKLOAD, choices=["tilt64", "euler128", "euler256", "euler512"],
+                    help="synthetic workload (default: the 256^3 headline; euler512 is the 512^3 object on a "
+                         "1024^3 grid, best run with --no-cpu-baseline --no-e2e --no-batch)")
     return ap.parse_args()
 
 
@@ -155,14 +158,14 @@ def gridding_flops(nk, D1, D2):
     return float((4.0 * nk * D1 * D2 + 8.0 * nk * D2).sum())
 
 
-def make_inputs(G, ctx, quick):
+def make_inputs(G, ctx, quick, workload=WORKLOAD):
     from genfire_gb300 import synth
 
     def proj(vol, angles, vectors):
         return ctx.project(vol.astype(np.float64), angles, vectors=np.asarray(vectors, float).reshape(-1))
     if quick:
-        return synth.make_workload(WORKLOAD, proj, D=64, n_proj=30, atoms=120)
-    return synth.make_workload(WORKLOAD, proj)
+        return synth.make_workload(workload, proj, D=64, n_proj=30, atoms=120)
+    return synth.make_workload(workload, proj)
 
 
 def params_for(G, w, precision, iters):
@@ -190,7 +193,7 @@ def run_ours(args, ws, rank, local, pg):
     torch.cuda.set_device(local)
     ctx = G.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    w = make_inputs(G, ctx, args.quick)
+    w = make_inputs(G, ctx, args.quick, args.workload)
     D = w["D"]
     P = w["projections"].shape[2]
     n1, _ = G.grid_size(params_for(G, w, G.PREC_FP64, 1))
@@ -324,10 +327,11 @@ def run_ours(args, ws, rank, local, pg):
         "ms_per_step": t_dr / K * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "%s: %d^3 object, %d^3 Fourier grid, %d projections %dx%d, mixed precision "
-                               "(complex64 FFT passes, FP64 errK/weight/phase sums)" % (WORKLOAD, D, n1, P, D, D),
+                               "(complex64 FFT passes, FP64 errK/weight/phase sums)" % (args.workload, D, n1, P, D, D),
                    "oversamplingRatio": w["os"], "interpolationCutoffDistance": 0.125,
                    "constraintEnforcementMode": 3, "parallelism": "replicas" if ws > 1 else "single GPU",
-                   "l2": "per-iteration working set (object, half spectra, constraint table) exceeds the 129 MB L2"},
+                   "l2": ("per-iteration working set (object, half spectra, constraint table) exceeds the 129 MB L2"
+                          if n1 >= 512 else "per-iteration working set partly L2-resident (no flush)")},
         "gridding_gflops": flops / t_grid_mixed / 1e9,
         "gridding_stages_ms": stages,
         "gridding_roofline": gridding_roofline(flops, nk, D, stages),
@@ -461,13 +465,13 @@ def run_reference(args, ws, rank):
     import genfire_gb300.synth as synth
     # inputs: the same seeded workload, projected by the oracle's own projector
     from genfire_gb300.synth import WORKLOADS
-    wl = WORKLOADS[WORKLOAD]
+    wl = WORKLOADS[args.workload]
 
     def proj(vol, angles, vectors):
         v = np.asarray(vectors, float).reshape(-1)
         return np.stack([O.project(vol.astype(np.float64), *a, vectors=v) for a in angles], axis=2)
     kw = dict(D=64, n_proj=30, atoms=120) if args.quick else {}
-    w = synth.make_workload(WORKLOAD, proj, **kw)
+    w = synth.make_workload(args.workload, proj, **kw)
     D = w["D"]
     P = w["projections"].shape[2]
     steps = max(1, min(args.steps, 2 if not args.quick else 5))
@@ -486,7 +490,7 @@ def run_reference(args, ws, rank):
             "ms_per_step": t_loop / steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": "%s: %d^3 object, %d^3 Fourier grid, %d projections (CPU restatement of the "
-                                   "reference's host path, FP64)" % (WORKLOAD, D, n1, P)},
+                                   "reference's host path, FP64)" % (args.workload, D, n1, P)},
             "gridding_gflops": gridding_flops(nk, D, D) / t_grid / 1e9,
             "cpu_baseline": {"value": v, "unit": "iters/s", "cores": O.num_threads(), "kind": "port",
                              "sample": sample, "cpu": cpu_model()},

@@ -255,9 +255,13 @@ class Context:
                                                   C.c_void_p(d_rec_ptr) if d_rec_ptr else None, C.byref(n)))
         return n.value
 
-    def select(self, p, phi, theta, psi):
+    def select(self, p, phi, theta, psi, cap=None):
+        """One projection's selected points (ind, dist, u, v).  cap bounds the
+        count (default: the whole gridded extent); more points are an error."""
         n1, n2 = grid_size(p, method=2)
-        if p.DFT_CentroSymmetricity:
+        if cap is not None:
+            cap = int(cap)
+        elif p.DFT_CentroSymmetricity:
             cap = (n1 // 2 + 1) * (2 * (n2 // 2) + 1) * (2 * (n1 // 2) + 1)
         else:
             cap = n1 * n2 * n1

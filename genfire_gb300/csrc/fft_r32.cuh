@@ -140,6 +140,14 @@ __device__ __forceinline__ constexpr bool r32_keep(int s)
     return r32_out_m(s) < 8 || r32_out_m(s) >= 24;
 }
 
+// For the centred half of a box (count 256 at offset 128), slot m (0..7 or
+// 24..31) of thread t is box element t + r32_half_off(m), in 0..255: the
+// offsets are compile-time constants once the slot loops are unrolled.
+__device__ __forceinline__ constexpr int r32_half_off(int m)
+{
+    return m < 8 ? 16 * m + 128 : 16 * m - 384;
+}
+
 // Column pass (the contract of k_colpass) for n = 512.  ZIN: the input is the
 // centred half of a box (in_cnt 256, in_c 128) and the pass starts with a
 // forward transform; ZOUT: only the centred half is written (out_cnt 256,
@@ -163,8 +171,12 @@ __global__ void __launch_bounds__(kR32Threads, (ZIN && ZOUT) ? 4 : 5) k_col_r32(
         const unsigned idim = (unsigned)a.in_dim;
 #pragma unroll
         for (int m = 0; m < 32; ++m) {
-            if (ZIN && m >= 8 && m < 24) {
-                x[m] = mk((T)0, (T)0);
+            if constexpr (ZIN) {
+                if (m >= 8 && m < 24) {
+                    x[m] = mk((T)0, (T)0);
+                    continue;
+                }
+                x[m] = cv ? in[(unsigned)(t + r32_half_off(m)) * idim] : mk((T)0, (T)0);
                 continue;
             }
             int e = t + 16 * m + a.in_c;
@@ -206,7 +218,11 @@ __global__ void __launch_bounds__(kR32Threads, (ZIN && ZOUT) ? 4 : 5) k_col_r32(
     const unsigned odim = (unsigned)a.out_dim;
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) {
-        if (ZOUT && !r32_keep(sl)) continue;
+        if constexpr (ZOUT) {
+            if (r32_keep(sl))
+                out[(unsigned)(t + r32_half_off(r32_out_m(sl))) * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
+            continue;
+        }
         int e = t + 16 * r32_out_m(sl) + a.out_c;
         if (e >= kR32N) e -= kR32N;
         if (e < a.out_cnt) out[(unsigned)e * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
@@ -245,9 +261,17 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
         uint8_t sa[kRowLoadGroup], sb[kRowLoadGroup];
 #pragma unroll
         for (int i = 0; i < kRowLoadGroup; ++i) {
-            if (ZIN && m0 + i >= 8 && m0 + i < 24) {
-                xa[i] = xb[i] = (T)0;
-                sa[i] = sb[i] = 1;
+            if constexpr (ZIN) {
+                if (m0 + i >= 8 && m0 + i < 24) {
+                    xa[i] = xb[i] = (T)0;
+                    sa[i] = sb[i] = 1;
+                    continue;
+                }
+                const int e = t + r32_half_off(m0 + i);
+                xa[i] = ok0 ? xs[o0 + e] : (T)0;
+                xb[i] = ok1 ? xs[o1 + e] : (T)0;
+                sa[i] = (a.support && ok0) ? a.support[o0 + e] : (uint8_t)1;
+                sb[i] = (a.support && ok1) ? a.support[o1 + e] : (uint8_t)1;
                 continue;
             }
             int e = t + 16 * (m0 + i) + a.c1;
@@ -323,7 +347,14 @@ __global__ void __launch_bounds__(kR32Threads) k_row_c2r_r32(RowPassArgs<T> a)
     r32_fft<T, true>(x, s, c, t, a.tw);  // synchronises before it reuses the buffer
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) {
-        if (ZOUT && !r32_keep(sl)) continue;
+        if constexpr (ZOUT) {
+            if (r32_keep(sl)) {
+                const int e = t + r32_half_off(r32_out_m(sl));
+                if (ok0) xs[(long long)r0 * a.B1 + e] = x[sl].x * a.scale;
+                if (ok1) xs[(long long)r1 * a.B1 + e] = x[sl].y * a.scale;
+            }
+            continue;
+        }
         int e = t + 16 * r32_out_m(sl) + a.c1;
         if (e >= kR32N) e -= kR32N;
         if (e < a.B1) {

@@ -198,10 +198,12 @@ def proj_geometry(prm, phi, theta, psi):
     return Rf, nrm
 
 
-def select(n1, n2, centro, cutoff, Rf, nrm):
-    """One projection's selected K-points: (ind0, dist, u, v, offplane)."""
-    ext = grid_extent(n1, n2, centro)
-    cap = int(ext[3]) * int(ext[4]) * int(ext[5])
+def select(n1, n2, centro, cutoff, Rf, nrm, cap=None):
+    """One projection's selected K-points: (ind0, dist, u, v, offplane); cap
+    bounds the count (default: the whole gridded extent)."""
+    if cap is None:
+        ext = grid_extent(n1, n2, centro)
+        cap = int(ext[3]) * int(ext[4]) * int(ext[5])
     ind = np.zeros(cap, dtype=np.int64)
     dist = np.zeros(cap, dtype=np.float32); u = np.zeros(cap, dtype=np.float32)
     v = np.zeros(cap, dtype=np.float32); off = np.zeros(1, dtype=np.int64)
