@@ -107,8 +107,8 @@ template <typename T, int N> static void set_reg_attrs()
 // register-resident engine with one column per thread, or with two adjacent
 // float columns per thread (unit column stride and 16-byte aligned column
 // pairs: even strides, aligned bases; tiles start at even columns), the
-// mixed-radix engine, and the radix-32 x 16 engine for 512 complex64 points
-// (fft_r32.cuh).
+// mixed-radix engine, and the radix-32 engines for 512 and 1024 complex64
+// points (fft_r32.cuh: 32 x 16 and 32 x 32, one exchange per transform).
 enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3, kColR32 = 4 };
 
 // GENFIRE_COL_VARIANT=<v> forces variant v wherever it is valid (tuning and
@@ -206,15 +206,17 @@ template <typename T> static void ensure_smem_attrs()
 template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
 {
     if (v == kColGeneric) return true;
-    if (v == kColR32) return sizeof(T) == 4 && a.pl.n == kR32N && span_ok(a) && (!(a.mode & 4) || a.W == kR32W);
+    if (v == kColR32)
+        return sizeof(T) == 4 && (a.pl.n == 512 || a.pl.n == 1024) && span_ok(a) &&
+               (!(a.mode & 4) || a.W == (a.pl.n == 512 ? R32<512>::W : R32<1024>::W));
     if (v == kColMix) return span_ok(a) && mix_capable<T>(a.pl.n);
     if (!reg_capable(a)) return false;
     return v == kColReg1 || (v == kColReg2 && pair_capable(a));
 }
 
-// Column pass launcher.  Without a tuned variant: the radix-32 x 16 engine
-// for 512 complex64 points (one exchange per transform: 8-28 % faster than
-// the radix-8 engine on the three column passes at 512^3); otherwise, for
+// Column pass launcher.  Without a tuned variant: the radix-32 engines for
+// 512 and 1024 complex64 points (one exchange per transform: 8-28 % faster
+// than the radix-8 engine on the three column passes at 512^3); otherwise, for
 // powers of two, two columns per thread in the fused forward + constraint +
 // inverse pass (two transforms per load) and one column per thread in the
 // single-transform passes (twice the resident warps); the mixed-radix
@@ -228,6 +230,36 @@ template <typename T> static int default_col_variant(const ColPassArgs<T> &a)
     return kColGeneric;
 }
 
+// The radix-32 engines (512 or 1024 complex64 points), with compile-time
+// pruning when the pass reads / writes the centred half of a box.  Input
+// pruning only with output pruning (the fused dim-3 pass): the forward-only
+// 512-point variant with it takes 128 registers and measured 3 % slower.
+template <typename T, int N> static void col_r32(const ColPassArgs<T> &a, int other, cudaStream_t st)
+{
+    using G = R32<N>;
+    const bool zin = (a.mode & 1) && a.in_cnt == N / 2 && a.in_c == N / 4;
+    const bool zout = a.out_cnt == N / 2 && a.out_c == N / 4;
+    const dim3 grid(cdiv(a.ncols, G::W), other);
+    const size_t sm = G::template smem<T>();
+    if (zin && zout) k_col_r32<T, N, true, true><<<grid, kR32Threads, sm, st>>>(a);
+    else if (zout) k_col_r32<T, N, false, true><<<grid, kR32Threads, sm, st>>>(a);
+    else k_col_r32<T, N, false, false><<<grid, kR32Threads, sm, st>>>(a);
+}
+template <typename T, int N> static void rows_r32(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
+{
+    using G = R32<N>;
+    const dim3 grid(cdiv((a.nrows + 1) / 2, G::W));
+    const size_t sm = G::template smem<T>();
+    const bool half = a.B1 == N / 2 && a.c1 == N / 4;  // the centred half of the row
+    if (forward) {
+        if (half) k_row_r2c_r32<T, N, true><<<grid, kR32Threads, sm, st>>>(a);
+        else k_row_r2c_r32<T, N, false><<<grid, kR32Threads, sm, st>>>(a);
+    } else {
+        if (half) k_row_c2r_r32<T, N, true><<<grid, kR32Threads, sm, st>>>(a);
+        else k_row_c2r_r32<T, N, false><<<grid, kR32Threads, sm, st>>>(a);
+    }
+}
+
 template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cudaStream_t st, int variant = kColAuto)
 {
     a.P = a.W + 1;
@@ -236,15 +268,8 @@ template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cu
     if (variant == kColAuto || !col_variant_ok(a, variant)) variant = default_col_variant(a);
     if (variant == kColR32) {
         if constexpr (sizeof(T) == 4) {
-            // compile-time pruning when the pass reads / writes the centred half of a
-            // box.  Input pruning only with output pruning (the fused dim-3 pass): the
-            // forward-only variant with it takes 128 registers and measured 3 % slower
-            const bool zin = (a.mode & 1) && a.in_cnt == kR32N / 2 && a.in_c == kR32N / 4;
-            const bool zout = a.out_cnt == kR32N / 2 && a.out_c == kR32N / 4;
-            dim3 grid(cdiv(a.ncols, kR32W), other);
-            if (zin && zout) k_col_r32<T, true, true><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
-            else if (zout) k_col_r32<T, false, true><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
-            else k_col_r32<T, false, false><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
+            if (a.pl.n == 512) col_r32<T, 512>(a, other, st);
+            else col_r32<T, 1024>(a, other, st);
         }
     } else if (variant == kColMix) {
         if (!launch_col_mix<T>(a, other, st)) fail(GENFIRE_ERR_STATE, "internal: mixed-radix pass not available.");
@@ -309,7 +334,7 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     return best;
 }
 
-// Row passes of 512 complex64 points run on the radix-32 x 16 engine
+// Row passes of 512 and 1024 complex64 points run on the radix-32 engines
 // (GENFIRE_ROW_VARIANT=1 selects the radix-8 register engine instead).
 static bool rows_r32_enabled()
 {
@@ -321,16 +346,9 @@ template <typename T> static void launch_rows(RowPassArgs<T> a, bool forward, cu
 {
     a.P = a.W + 1;
     if constexpr (sizeof(T) == 4) {
-        if (a.pl.n == kR32N && rows_r32_enabled()) {
-            const dim3 grid(cdiv((a.nrows + 1) / 2, kR32W));
-            const bool half = a.B1 == kR32N / 2 && a.c1 == kR32N / 4;  // the centred half of the row
-            if (forward) {
-                if (half) k_row_r2c_r32<T, true><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
-                else k_row_r2c_r32<T, false><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
-            } else {
-                if (half) k_row_c2r_r32<T, true><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
-                else k_row_c2r_r32<T, false><<<grid, kR32Threads, r32_smem<T>(), st>>>(a);
-            }
+        if ((a.pl.n == 512 || a.pl.n == 1024) && rows_r32_enabled()) {
+            if (a.pl.n == 512) rows_r32<T, 512>(a, forward, st);
+            else rows_r32<T, 1024>(a, forward, st);
             GF_CHECK_LAUNCH();
             return;
         }

@@ -1,34 +1,58 @@
-// fft_r32.cuh -- 512-point column passes with 32 elements per thread.
+// fft_r32.cuh -- 512- and 1024-point passes with 32 elements per thread.
 //
-// A 512-point transform as one radix-32 and one radix-16 stage (512 = 32 x 16)
-// with a single shared-memory exchange between them; the radix-8 engine of
-// fft_reg.cuh needs two, and its exchanges are what bound those passes.
-// Thread t (0..15) of a column holds the elements t + 16 m (m = 0..31) before
-// and after a transform:
-// The radix-4 and radix-8 butterflies are the packed-pair (f32x2) ones of
-// fft.cuh for complex64.
-//   stage 1: Y_t[k1] = sum_m x[t + 16 m] W32^(m k1) in registers
+// An N-point transform (N = 32 * P, P = 16 or 32 threads per column) as one
+// radix-32 stage and one radix-P stage with a single shared-memory exchange
+// between them; the radix-8 engine of fft_reg.cuh needs two (three at 1024),
+// and its exchanges are what bound those passes.  Thread t (0..P-1) of a
+// column holds the elements t + P m (m = 0..31) before and after a transform:
+//   stage 1: Y_t[k1] = sum_m x[t + P m] W32^(m k1) in registers
 //            (m = 8a + b: radix 4 over a, rotation W32^(b k1'), radix 8 over b),
-//            then times W512^(t k1) from the twiddle table;
+//            then times WN^(t k1) from the twiddle table;
 //   exchange: S[k1][t] = Y_t[k1];
-//   stage 2: X[k1 + 32 k2] = sum_t S[k1][t] W16^(t k2) for k1 = t and t + 16
-//            (radix 4 x 4), which are the elements t + 16 m' again.
-// Eight columns per CTA (the constraint table's tile width for n = 512),
-// sixteen threads per column, the column fastest within a warp.
+//   stage 2: X[k1 + 32 k2] = sum_t S[k1][t] WP^(t k2): for N = 512 the two
+//            16-point DFTs (radix 4 x 4) of k1 = t and t + 16, for N = 1024
+//            the 32-point DFT of k1 = t (the stage-1 schedule again); either
+//            way the thread ends with the elements t + P m' again.
+// The radix-4 and radix-8 butterflies are the packed-pair (f32x2) ones of
+// fft.cuh for complex64.  Every CTA has 128 threads: 8 columns of 16 threads
+// (N = 512) or 4 columns of 32 (N = 1024) -- the constraint table's tile
+// width for those lengths -- with the column fastest within a warp.
 #pragma once
 
 #include "fft_reg.cuh"
 
 namespace gf {
 
-constexpr int kR32N = 512;
-constexpr int kR32W = 8;                     // columns per CTA
-constexpr int kR32Threads = 16 * kR32W;      // 128
-constexpr int kR32ColStride = 32 * 17 + 2;   // one column's S[k1][t] block, rows padded to 17:
-                                             // every half-warp access is conflict-free
-using R32Lay = ColLayout<kR32N, kR32W>;      // natural-order tile for the constraint table
-constexpr int kR32Elems = R32Lay::SIZE > kR32W * kR32ColStride ? R32Lay::SIZE : kR32W * kR32ColStride;
-template <typename T> constexpr size_t r32_smem() { return (size_t)kR32Elems * sizeof(cplx<T>); }
+constexpr int kR32Threads = 128;
+
+template <int N> struct R32 {
+    static_assert(N == 512 || N == 1024, "radix-32 engines: 512 or 1024 points");
+    static constexpr int P = N / 32;                 // threads per column
+    static constexpr int W = kR32Threads / P;        // columns per CTA (8 or 4)
+    static constexpr int ROW = P + 1;                // S[k1][t] row stride (odd: conflict-free reads)
+    // column stride of the exchange buffer, 16 / W modulo 16: the W columns x
+    // 16 / W threads of a half-warp hit 16 distinct 8-byte bank pairs
+    static constexpr int CS = 32 * ROW + 16 / W;
+    using Lay = ColLayout<N, W>;                     // natural-order tile for the constraint table
+    using RowLay = RowLayout<N, W>;                  // natural-order tile of the row passes
+    static constexpr int ELEMS_ = Lay::SIZE > W * CS ? Lay::SIZE : W * CS;
+    static constexpr int ELEMS = RowLay::SIZE > ELEMS_ ? RowLay::SIZE : ELEMS_;
+    template <typename T> static constexpr size_t smem() { return (size_t)ELEMS * sizeof(cplx<T>); }
+
+    // Out: slot s holds element t + P out_m(s)
+    static __device__ __forceinline__ constexpr int out_m(int s)
+    {
+        if constexpr (N == 512) return (s >> 4) + 2 * (((s & 15) >> 2) + 4 * (s & 3));
+        else return 4 * (s & 7) + (s >> 3);
+    }
+    // slots of a transform's output that the centred half of a box keeps:
+    // out_m(s) in 0..7 or 24..31
+    static __device__ __forceinline__ constexpr bool keep(int s) { return out_m(s) < 8 || out_m(s) >= 24; }
+    // For the centred half of a box (count N/2 at offset N/4), slot m (0..7 or
+    // 24..31) of thread t is box element t + half_off(m), in 0 .. N/2 - 1: the
+    // offsets are compile-time constants once the slot loops are unrolled.
+    static __device__ __forceinline__ constexpr int half_off(int m) { return m < 8 ? P * m + N / 4 : P * m - 3 * N / 4; }
+};
 
 // W32^j = exp(-2 pi i j / 32) for j known at compile time after unrolling,
 // from cos(pi k / 16), k = 0..8, by quadrant symmetry (exact zeros and ones)
@@ -51,14 +75,6 @@ template <typename T> __device__ __forceinline__ cplx<T> w32(int j)
     else if (q == 2) { c = -C[k]; s = -C[8 - k]; }
     else { c = C[8 - k]; s = -C[k]; }
     return mk((T)c, (T)-s);
-}
-
-// One 512-point transform of the thread's 32 elements.  In: slot m holds
-// element t + 16 m.  Out: slot s holds element t + 16 r32_out_m(s).  Uses
-// the CTA's exchange buffer (synchronises before and after writing it).
-__device__ __forceinline__ constexpr int r32_out_m(int s)
-{
-    return (s >> 4) + 2 * (((s & 15) >> 2) + 4 * (s & 3));
 }
 
 // Radix 4 of (v0, 0, 0, v3): X[k] = v0 + v3 W4^(3k), the same operations as
@@ -84,13 +100,13 @@ template <typename T, bool INV> __device__ __forceinline__ void dft4_outer(cplx<
     }
 }
 
-// ZIN: the elements of slots 8..23 are known to be zero (the centred half of
-// a box transform: entries t + 16 m + 128 mod 512 below 256 lie in slots
-// 0..7 and 24..31), so the first radix-4 stage takes two inputs.
-template <typename T, bool INV, bool ZIN = false>
-__device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int t, const cplx<T> *__restrict__ tw)
+// 32-point DFT of the thread's slots in registers: slot m = 8a + b holds
+// input m; output k ends in slot 8 (k & 3) + (k >> 2).  ZIN: slots 8..23 are
+// known to be zero, so the first radix-4 stage takes two inputs.
+template <typename T, bool INV, bool ZIN>
+__device__ __forceinline__ void dft32_regs(cplx<T> (&x)[32])
 {
-    // stage 1, radix 4 over a: slot 8a + b -> Z_b[k1'] in slot 8 k1' + b, rotated by W32^(b k1')
+    // radix 4 over a: slot 8a + b -> Z_b[k1'] in slot 8 k1' + b, rotated by W32^(b k1')
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
         cplx<T> u[4] = {x[b], x[8 + b], x[16 + b], x[24 + b]};
@@ -102,69 +118,86 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
     // radix 8 over b: slots 8 k1' .. 8 k1' + 7 -> Y[k1' + 4 k2] in slot 8 k1' + k2
 #pragma unroll
     for (int kp = 0; kp < 4; ++kp) Dft<8, T>::run(&x[8 * kp], INV, nullptr, 8);
-    // W512^(t k1) and the exchange: S[k1][t]
+}
+
+// One N-point transform of the thread's 32 elements.  In: slot m holds
+// element t + P m.  Out: slot s holds element t + P out_m(s).  Uses the
+// CTA's exchange buffer (synchronises before and after writing it).  ZIN:
+// the elements of slots 8..23 are zero (the centred half of a box
+// transform: entries t + P m + N/4 mod N below N/2 lie in slots 0..7 and
+// 24..31).
+template <typename T, int N, bool INV, bool ZIN = false>
+__device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int t, const cplx<T> *__restrict__ tw)
+{
+    using G = R32<N>;
+    dft32_regs<T, INV, ZIN>(x);
+    // WN^(t k1) and the exchange: S[k1][t]
     __syncthreads();  // the buffer may still be read by the previous step
-    cplx<T> *Sc = S + c * kR32ColStride;
+    cplx<T> *Sc = S + c * G::CS;
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) {
         const int slot = 8 * (k1 & 3) + (k1 >> 2);
         const cplx<T> y = k1 ? ctw(x[slot], __ldg(tw + t * k1), INV) : x[slot];
-        Sc[k1 * 17 + t] = y;
+        Sc[k1 * G::ROW + t] = y;
     }
     __syncthreads();
-    // stage 2 for k1 = t + 16 h: slot 16 h + t' <- S[k1][t']
+    if constexpr (N == 512) {
+        // stage 2 for k1 = t + 16 h: slot 16 h + t' <- S[k1][t']
 #pragma unroll
-    for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
-        for (int tp = 0; tp < 16; ++tp) x[16 * h + tp] = Sc[(t + 16 * h) * 17 + tp];
+            for (int tp = 0; tp < 16; ++tp) x[16 * h + tp] = Sc[(t + 16 * h) * G::ROW + tp];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        // radix 4 over p of slot 16h + 4p + q -> slot 16h + 4 k2' + q, rotated by W16^(q k2')
+        for (int h = 0; h < 2; ++h) {
+            // radix 4 over p of slot 16h + 4p + q -> slot 16h + 4 k2' + q, rotated by W16^(q k2')
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            cplx<T> u[4] = {x[16 * h + q], x[16 * h + 4 + q], x[16 * h + 8 + q], x[16 * h + 12 + q]};
-            Dft<4, T>::run(u, INV, nullptr, 4);
+            for (int q = 0; q < 4; ++q) {
+                cplx<T> u[4] = {x[16 * h + q], x[16 * h + 4 + q], x[16 * h + 8 + q], x[16 * h + 12 + q]};
+                Dft<4, T>::run(u, INV, nullptr, 4);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) x[16 * h + 4 * k + q] = (q && k) ? ctw(u[k], w32<T>(2 * q * k), INV) : u[k];
+                for (int k = 0; k < 4; ++k) x[16 * h + 4 * k + q] = (q && k) ? ctw(u[k], w32<T>(2 * q * k), INV) : u[k];
+            }
+            // radix 4 over q: slots 16h + 4k2' .. +3 -> X[k1 + 32 (k2' + 4 k3)] in slot 16h + 4k2' + k3
+#pragma unroll
+            for (int kp = 0; kp < 4; ++kp) Dft<4, T>::run(&x[16 * h + 4 * kp], INV, nullptr, 4);
         }
-        // radix 4 over q: slots 16h + 4k2' .. +3 -> X[k1 + 32 (k2' + 4 k3)] in slot 16h + 4k2' + k3
+    } else {
+        // stage 2 for k1 = t: slot t' <- S[t][t'], a 32-point DFT over t'
+        // (X[t + 32 k2] in slot 8 (k2 & 3) + (k2 >> 2))
 #pragma unroll
-        for (int kp = 0; kp < 4; ++kp) Dft<4, T>::run(&x[16 * h + 4 * kp], INV, nullptr, 4);
+        for (int tp = 0; tp < 32; ++tp) x[tp] = Sc[t * G::ROW + tp];
+        dft32_regs<T, INV, false>(x);
     }
 }
 
-// slots of a transform's output (slot s holds element t + 16 r32_out_m(s)) that
-// the centred half of a box keeps: r32_out_m(s) in 0..7 or 24..31
-__device__ __forceinline__ constexpr bool r32_keep(int s)
+// CTAs per SM the column passes are built for (registers <= 65536 / (128 x
+// this)).  512 points: 5 for the single-transform passes (96 registers), 4 for
+// the fused one (at 96 it spills, and measured no faster).  1024 points: 3
+// (168 registers; the 32-point second stage keeps more values live, and at 4
+// CTAs every variant spills).
+constexpr int r32_col_min_blocks(int n, bool fused)
 {
-    return r32_out_m(s) < 8 || r32_out_m(s) >= 24;
+    return n == 512 ? (fused ? 4 : 5) : 3;
 }
 
-// For the centred half of a box (count 256 at offset 128), slot m (0..7 or
-// 24..31) of thread t is box element t + r32_half_off(m), in 0..255: the
-// offsets are compile-time constants once the slot loops are unrolled.
-__device__ __forceinline__ constexpr int r32_half_off(int m)
+// Column pass (the contract of k_colpass) for n = N.  ZIN: the input is the
+// centred half of a box (in_cnt N/2, in_c N/4) and the pass starts with a
+// forward transform; ZOUT: only the centred half is written (out_cnt N/2,
+// out_c N/4), so the final transform's other outputs are never formed.
+template <typename T, int N, bool ZIN, bool ZOUT>
+__global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N, ZIN && ZOUT)) k_col_r32(ColPassArgs<T> a)
 {
-    return m < 8 ? 16 * m + 128 : 16 * m - 384;
-}
-
-// Column pass (the contract of k_colpass) for n = 512.  ZIN: the input is the
-// centred half of a box (in_cnt 256, in_c 128) and the pass starts with a
-// forward transform; ZOUT: only the centred half is written (out_cnt 256,
-// out_c 128), so the final transform's other outputs are never formed.
-// Occupancy: 5 CTAs per SM (<= 96 registers) for the single-transform passes;
-// the fused pass keeps 4 (at 96 registers it spills, and measured no faster).
-template <typename T, bool ZIN, bool ZOUT>
-__global__ void __launch_bounds__(kR32Threads, (ZIN && ZOUT) ? 4 : 5) k_col_r32(ColPassArgs<T> a)
-{
+    using G = R32<N>;
+    constexpr int P = G::P, W = G::W;
+    using Lay = typename G::Lay;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     if (a.ctl && blockIdx.x == 0 && blockIdx.y == 0) ctl_mid_update(a.ctl, a.partial, a.nparts, a.denom, a.hist);
-    const int c = threadIdx.x % kR32W, t = threadIdx.x / kR32W;
+    const int c = threadIdx.x % W, t = threadIdx.x / W;
     const int tile = blockIdx.x, other = blockIdx.y;
-    const int col = tile * kR32W + c;
+    const int col = tile * W + c;
     const bool cv = col < a.ncols;
-    const cplx<T> *twp = a.tw;  // tw[j] = exp(-2 pi i j / 512)
+    const cplx<T> *twp = a.tw;  // tw[j] = exp(-2 pi i j / N)
     cplx<T> x[32];
     {
         const cplx<T> *in = a.in + (long long)other * a.in_other + (long long)col * a.col_stride;
@@ -176,41 +209,41 @@ __global__ void __launch_bounds__(kR32Threads, (ZIN && ZOUT) ? 4 : 5) k_col_r32(
                     x[m] = mk((T)0, (T)0);
                     continue;
                 }
-                x[m] = cv ? in[(unsigned)(t + r32_half_off(m)) * idim] : mk((T)0, (T)0);
+                x[m] = cv ? in[(unsigned)(t + G::half_off(m)) * idim] : mk((T)0, (T)0);
                 continue;
             }
-            int e = t + 16 * m + a.in_c;
-            if (e >= kR32N) e -= kR32N;
+            int e = t + P * m + a.in_c;
+            if (e >= N) e -= N;
             x[m] = (cv && e < a.in_cnt) ? in[(unsigned)e * idim] : mk((T)0, (T)0);
         }
     }
     ErrAcc<T> err = 0;
     bool fwd_layout = false;  // slots in the output order of a transform
     if (a.mode & 1) {
-        r32_fft<T, false, ZIN>(x, s, c, t, twp);
+        r32_fft<T, N, false, ZIN>(x, s, c, t, twp);
         fwd_layout = true;
     }
     if (a.mode & 2) {
         if (a.mode & 1) {
-            // back to slot m = element t + 16 m, through the natural-order tile
+            // back to slot m = element t + P m, through the natural-order tile
             // (where the Fourier constraint is applied)
             __syncthreads();
 #pragma unroll
-            for (int sl = 0; sl < 32; ++sl) s[R32Lay::idx(t + 16 * r32_out_m(sl), c)] = x[sl];
+            for (int sl = 0; sl < 32; ++sl) s[Lay::idx(t + P * G::out_m(sl), c)] = x[sl];
             __syncthreads();
             if (a.mode & 4) {
                 if (a.rtab) {
-                    capture_rfree<T>(s, a, tile, kR32W, other, [](int q3, int cl) { return R32Lay::idx(q3, cl); });
+                    capture_rfree<T>(s, a, tile, W, other, [](int q3, int cl) { return Lay::idx(q3, cl); });
                     __syncthreads();
                 }
-                err = apply_table<T, R32Lay>(s, a, tile, kR32W, other);
+                err = apply_table<T, Lay>(s, a, tile, W, other);
                 block_partial(err, a.partial + (long long)other * gridDim.x + tile);
                 __syncthreads();
             }
 #pragma unroll
-            for (int m = 0; m < 32; ++m) x[m] = s[R32Lay::idx(t + 16 * m, c)];
+            for (int m = 0; m < 32; ++m) x[m] = s[Lay::idx(t + P * m, c)];
         }
-        r32_fft<T, true>(x, s, c, t, twp);
+        r32_fft<T, N, true>(x, s, c, t, twp);
         fwd_layout = true;
     }
     if (!fwd_layout || !cv) return;
@@ -219,37 +252,38 @@ __global__ void __launch_bounds__(kR32Threads, (ZIN && ZOUT) ? 4 : 5) k_col_r32(
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) {
         if constexpr (ZOUT) {
-            if (r32_keep(sl))
-                out[(unsigned)(t + r32_half_off(r32_out_m(sl))) * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
+            if (G::keep(sl))
+                out[(unsigned)(t + G::half_off(G::out_m(sl))) * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
             continue;
         }
-        int e = t + 16 * r32_out_m(sl) + a.out_c;
-        if (e >= kR32N) e -= kR32N;
+        int e = t + P * G::out_m(sl) + a.out_c;
+        if (e >= N) e -= N;
         if (e < a.out_cnt) out[(unsigned)e * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
     }
 }
 
-// Row passes (the contracts of k_rows_r2c / k_rows_c2r) for n = 512: eight
-// pairs of real rows per CTA, each pair one complex transform (row a the real
-// part, row b the imaginary part), sixteen threads per pair with the index
-// along the row fastest within a warp (64-byte row segments per access).
-using R32RowLay = RowLayout<kR32N, kR32W>;
-// elements whose loads are in flight together in the forward row pass: 8 keeps
-// the pass at 118 registers (4 CTAs per SM); 16 and 32 cost occupancy and
-// measured 13 % and 54 % slower at 512^3
+// Row passes (the contracts of k_rows_r2c / k_rows_c2r) for n = N: W pairs of
+// real rows per CTA, each pair one complex transform (row a the real part,
+// row b the imaginary part), P threads per pair with the index along the row
+// fastest within a warp (64- or 128-byte row segments per access).
+// Elements whose loads are in flight together in the forward row pass: 8 keeps
+// the 512-point pass at 118 registers (4 CTAs per SM); 16 and 32 cost
+// occupancy and measured 13 % and 54 % slower at 512^3.
 constexpr int kRowLoadGroup = 8;
-static_assert(R32RowLay::SIZE <= kR32Elems, "row tile fits the pass's buffer");
 
-// ZIN: the rows are the centred half of the transform (B1 256, c1 128)
-template <typename T, bool ZIN>
+// ZIN: the rows are the centred half of the transform (B1 N/2, c1 N/4)
+template <typename T, int N, bool ZIN>
 __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
 {
+    using G = R32<N>;
+    constexpr int P = G::P, W = G::W;
+    using RowLay = typename G::RowLay;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
-    const int t = threadIdx.x % 16, c = threadIdx.x / 16;
+    const int t = threadIdx.x % P, c = threadIdx.x / P;
     if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
     const T *xs = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
-    const int r0 = (blockIdx.x * kR32W + c) * 2, r1 = r0 + 1;
+    const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     const bool ok0 = r0 < a.nrows, ok1 = r1 < a.nrows;
     const long long o0 = (long long)r0 * a.B1, o1 = o0 + a.B1;
     cplx<T> x[32];
@@ -267,15 +301,15 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
                     sa[i] = sb[i] = 1;
                     continue;
                 }
-                const int e = t + r32_half_off(m0 + i);
+                const int e = t + G::half_off(m0 + i);
                 xa[i] = ok0 ? xs[o0 + e] : (T)0;
                 xb[i] = ok1 ? xs[o1 + e] : (T)0;
                 sa[i] = (a.support && ok0) ? a.support[o0 + e] : (uint8_t)1;
                 sb[i] = (a.support && ok1) ? a.support[o1 + e] : (uint8_t)1;
                 continue;
             }
-            int e = t + 16 * (m0 + i) + a.c1;
-            if (e >= kR32N) e -= kR32N;
+            int e = t + P * (m0 + i) + a.c1;
+            if (e >= N) e -= N;
             const bool in = e < a.B1;
             xa[i] = (in && ok0) ? xs[o0 + e] : (T)0;
             xb[i] = (in && ok1) ? xs[o1 + e] : (T)0;
@@ -292,71 +326,74 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
             x[m0 + i] = mk(va * (T)sa[i], vb * (T)sb[i]);
         }
     }
-    r32_fft<T, false, ZIN>(x, s, c, t, a.tw);
+    r32_fft<T, N, false, ZIN>(x, s, c, t, a.tw);
     __syncthreads();  // the exchange buffer becomes the natural-order tile
 #pragma unroll
-    for (int sl = 0; sl < 32; ++sl) s[R32RowLay::idx(t + 16 * r32_out_m(sl), c)] = x[sl];
+    for (int sl = 0; sl < 32; ++sl) s[RowLay::idx(t + P * G::out_m(sl), c)] = x[sl];
     __syncthreads();
     // split the pair's spectrum Z into the rows' half spectra:
     // Xa(q) = (Z(q) + conj Z(-q)) / 2, Xb(q) = (Z(q) - conj Z(-q)) / 2i
     cplx<T> *ya = a.Y + (long long)r0 * a.ld1, *yb = ya + a.ld1;
-    for (int q = t; q < a.h1; q += 16) {
-        const cplx<T> Z = s[R32RowLay::idx(q, c)];
-        const cplx<T> Zm = s[R32RowLay::idx(q == 0 ? 0 : kR32N - q, c)];
+    for (int q = t; q < a.h1; q += P) {
+        const cplx<T> Z = s[RowLay::idx(q, c)];
+        const cplx<T> Zm = s[RowLay::idx(q == 0 ? 0 : N - q, c)];
         if (ok0) ya[q] = mk((T)0.5 * (Z.x + Zm.x), (T)0.5 * (Z.y - Zm.y));
         if (ok1) yb[q] = mk((T)0.5 * (Z.y + Zm.y), (T)0.5 * (Zm.x - Z.x));
     }
 }
 
-// ZOUT: only the centred half of each row is written (B1 256, c1 128)
-template <typename T, bool ZOUT>
+// ZOUT: only the centred half of each row is written (B1 N/2, c1 N/4)
+template <typename T, int N, bool ZOUT>
 __global__ void __launch_bounds__(kR32Threads) k_row_c2r_r32(RowPassArgs<T> a)
 {
+    using G = R32<N>;
+    constexpr int P = G::P, W = G::W;
+    using RowLay = typename G::RowLay;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
-    const int t = threadIdx.x % 16, c = threadIdx.x / 16;
+    const int t = threadIdx.x % P, c = threadIdx.x / P;
     T *xs = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
-    const int r0 = (blockIdx.x * kR32W + c) * 2, r1 = r0 + 1;
+    const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     const bool ok0 = r0 < a.nrows, ok1 = r1 < a.nrows;
     {
         // pack the two half spectra: Z = Ha + i Hb on q < h1, Z(-q) from the
         // conjugate symmetry of each row; all loads issued before the packing
-        constexpr int QIT = (kR32N / 2 + 16) / 16;  // q = t + 16 it covers 0 .. N/2
+        constexpr int QIT = (N / 2 + P) / P;  // q = t + P it covers 0 .. N/2
         const cplx<T> *ya = a.Y + (long long)r0 * a.ld1, *yb = ya + a.ld1;
         cplx<T> HA[QIT], HB[QIT];
 #pragma unroll
         for (int it = 0; it < QIT; ++it) {
-            const int q = t + 16 * it;
+            const int q = t + P * it;
             HA[it] = (q < a.h1 && ok0) ? ya[q] : mk((T)0, (T)0);
             HB[it] = (q < a.h1 && ok1) ? yb[q] : mk((T)0, (T)0);
         }
 #pragma unroll
         for (int it = 0; it < QIT; ++it) {
-            const int q = t + 16 * it;
+            const int q = t + P * it;
             if (q >= a.h1) break;
             cplx<T> ha = HA[it], hb = HB[it];
-            if (q == 0 || 2 * q == kR32N) { ha.y = 0; hb.y = 0; }
-            s[R32RowLay::idx(q, c)] = mk(ha.x - hb.y, ha.y + hb.x);
-            if (q != 0 && kR32N - q >= a.h1) s[R32RowLay::idx(kR32N - q, c)] = mk(ha.x + hb.y, hb.x - ha.y);
+            if (q == 0 || 2 * q == N) { ha.y = 0; hb.y = 0; }
+            s[RowLay::idx(q, c)] = mk(ha.x - hb.y, ha.y + hb.x);
+            if (q != 0 && N - q >= a.h1) s[RowLay::idx(N - q, c)] = mk(ha.x + hb.y, hb.x - ha.y);
         }
     }
     __syncthreads();
     cplx<T> x[32];
 #pragma unroll
-    for (int m = 0; m < 32; ++m) x[m] = s[R32RowLay::idx(t + 16 * m, c)];
-    r32_fft<T, true>(x, s, c, t, a.tw);  // synchronises before it reuses the buffer
+    for (int m = 0; m < 32; ++m) x[m] = s[RowLay::idx(t + P * m, c)];
+    r32_fft<T, N, true>(x, s, c, t, a.tw);  // synchronises before it reuses the buffer
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) {
         if constexpr (ZOUT) {
-            if (r32_keep(sl)) {
-                const int e = t + r32_half_off(r32_out_m(sl));
+            if (G::keep(sl)) {
+                const int e = t + G::half_off(G::out_m(sl));
                 if (ok0) xs[(long long)r0 * a.B1 + e] = x[sl].x * a.scale;
                 if (ok1) xs[(long long)r1 * a.B1 + e] = x[sl].y * a.scale;
             }
             continue;
         }
-        int e = t + 16 * r32_out_m(sl) + a.c1;
-        if (e >= kR32N) e -= kR32N;
+        int e = t + P * G::out_m(sl) + a.c1;
+        if (e >= N) e -= N;
         if (e < a.B1) {
             if (ok0) xs[(long long)r0 * a.B1 + e] = x[sl].x * a.scale;
             if (ok1) xs[(long long)r1 * a.B1 + e] = x[sl].y * a.scale;

@@ -1,9 +1,9 @@
-"""The radix-32 x 16 column pass (n = 512, complex64; one shared-memory
-exchange per transform), forced with GENFIRE_COL_VARIANT=4 wherever it is
-valid: transforms against numpy, and the fused dim-3 pass (constraint table,
-errK, Rfree capture) and the dim-2 passes of a reconstruction against the
-oracle.  Bar: 1e-5 relative for single transforms, the MIXED bar 1e-4 for
-reconstructions."""
+"""The radix-32 engines (n = 512 as 32 x 16 and n = 1024 as 32 x 32,
+complex64; one shared-memory exchange per transform), forced with
+GENFIRE_COL_VARIANT=4 wherever they are valid: transforms against numpy, and
+the fused dim-3 pass (constraint table, errK, Rfree capture), the dim-2
+passes and the row passes of a reconstruction against the oracle.  Bar: 1e-5
+relative for single transforms, the MIXED bar 1e-4 for reconstructions."""
 import numpy as np
 import pytest
 
@@ -18,7 +18,8 @@ def r32(monkeypatch):
     monkeypatch.setenv("GENFIRE_COL_VARIANT", "4")
 
 
-@pytest.mark.parametrize("shape", [(8, 4, 512), (6, 512, 3), (512, 3, 5), (16, 512, 512)])
+@pytest.mark.parametrize("shape", [(8, 4, 512), (6, 512, 3), (512, 3, 5), (16, 512, 512),
+                                   (8, 4, 1024), (6, 1024, 3), (1024, 3, 5), (4, 1024, 1024)])
 @pytest.mark.parametrize("inverse", [False, True])
 def test_r32_transforms(lib, ctx, r32, shape, inverse):
     rng = np.random.default_rng(sum(shape) + inverse)
@@ -37,11 +38,14 @@ def _measured(seed, D1, D2, os_, keep=0.5):
     return np.asfortranarray(M)
 
 
-@pytest.mark.parametrize("D1,D2,mode", [(256, 4, 3), (4, 256, 1), (256, 4, 2)])
-def test_r32_reconstruct_mixed(lib, ctx, oracle, r32, D1, D2, mode):
-    """n1 = 512 puts the fused dim-3 pass (forward, constraint, errK, inverse)
-    on the new engine; n2 = 512 the dim-2 forward and inverse passes."""
-    os_, N = 2.0, 4
+@pytest.mark.parametrize("D1,D2,mode,os_", [(256, 4, 3, 2.0), (4, 256, 1, 2.0), (256, 4, 2, 2.0),
+                                           (512, 4, 3, 2.0), (4, 512, 1, 2.0), (400, 3, 3, 2.56)])
+def test_r32_reconstruct_mixed(lib, ctx, oracle, r32, D1, D2, mode, os_):
+    """n1 = 512 or 1024 puts the fused dim-3 pass (forward, constraint, errK,
+    inverse) on the engine; n2 = 512 or 1024 the dim-2 forward and inverse
+    passes.  A 400 box at oversampling 2.56 (n1 = 1024) takes the unpruned
+    variants."""
+    N = 4
     M = _measured(D1 + D2 + mode, D1, D2, os_)
     kw = dict(oversamplingRatio=os_, numIterations=N, constraintEnforcementMode=mode)
     p = params(lib, D1, D2, 1, precision="mixed", **kw)
@@ -55,8 +59,9 @@ def test_r32_reconstruct_mixed(lib, ctx, oracle, r32, D1, D2, mode):
     assert rel(rec, reco) < 1e-4
 
 
-def test_r32_rfree_capture(lib, ctx, oracle, r32):
-    D1, D2, os_, N, nb = 256, 4, 2.0, 3, 3
+@pytest.mark.parametrize("D1", [256, 512])
+def test_r32_rfree_capture(lib, ctx, oracle, r32, D1):
+    D2, os_, N, nb = 4, 2.0, 3, 3
     M = _measured(5, D1, D2, os_)
     kw = dict(oversamplingRatio=os_, numIterations=N, constraintEnforcementMode=3)
     p = params(lib, D1, D2, 1, precision="mixed", **kw)
@@ -77,11 +82,12 @@ def test_r32_rfree_capture(lib, ctx, oracle, r32):
     assert np.abs(Rf - Rfo).max() < 1e-4
 
 
-@pytest.mark.parametrize("D1,D2,mode,pos,sup", [(256, 4, 3, 1, 1), (256, 6, 1, 0, 1), (256, 3, 3, 1, 0)])
+@pytest.mark.parametrize("D1,D2,mode,pos,sup", [(256, 4, 3, 1, 1), (256, 6, 1, 0, 1), (256, 3, 3, 1, 0),
+                                               (512, 3, 3, 1, 1), (512, 2, 1, 0, 1)])
 def test_r32_row_passes_reconstruct(lib, ctx, oracle, D1, D2, mode, pos, sup):
-    """n1 = 512: the dim-1 row passes (real rows to half spectra with
-    positivity and support, and back) on the radix-32 x 16 engine, the
-    built-in choice for 512-point complex64 rows; odd row counts leave the
+    """n1 = 512 or 1024: the dim-1 row passes (real rows to half spectra with
+    positivity and support, and back) on the radix-32 engines, the built-in
+    choice for 512- and 1024-point complex64 rows; odd row counts leave the
     last pair half empty."""
     os_, N = 2.0, 4
     M = _measured(D1 + 3 * D2 + mode, D1, D2, os_)
