@@ -36,7 +36,9 @@ namespace gf {
 // ===========================================================================
 // twiddle tables, one per (device, n, precision), kept for the process: the
 // n entries exp(-2 pi i t / n), then (power-of-two n) the packed per-stage
-// table of the register-resident passes (P2Plan::twoff), copied from them
+// table of the register-resident passes (P2Plan::twoff), copied from them,
+// then (n = 512, 1024) the radix-32 engines' table W_n^(t k1) ordered by k1
+// then t (R32<n>::TWT)
 // ===========================================================================
 template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
 {
@@ -49,7 +51,8 @@ template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
     auto it = cache.find(key);
     if (it != cache.end()) return static_cast<const cplx<T> *>(it->second);
     const int np = packed_twiddle_count(n);
-    std::vector<cplx<T>> h((size_t)n + np);
+    const int nr = (n == 512 || n == 1024) ? 32 * (n / 32) : 0;  // radix-32 table: k1 < 32, t < n / 32
+    std::vector<cplx<T>> h((size_t)n + np + nr);
     const double pi = 3.14159265358979323846;
     for (int t = 0; t < n; ++t) {
         double a = -2.0 * pi * (double)t / (double)n;
@@ -71,7 +74,14 @@ template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
                 h[o++] = mk((T)1, (T)0);  // pad
             }
         }
-        if (o != h.size()) fail(GENFIRE_ERR_STATE, "internal: packed twiddle table size.");
+        if (o != (size_t)n + np) fail(GENFIRE_ERR_STATE, "internal: packed twiddle table size.");
+    }
+    if (nr) {
+        const int P = n / 32;
+        const size_t o = (size_t)(n == 512 ? R32<512>::TWT : R32<1024>::TWT);
+        if (o != (size_t)n + np) fail(GENFIRE_ERR_STATE, "internal: radix-32 twiddle table offset.");
+        for (int k1 = 0; k1 < 32; ++k1)
+            for (int t = 0; t < P; ++t) h[o + (size_t)k1 * P + t] = h[(size_t)t * k1];
     }
     void *d = nullptr;
     GF_CUDA(cudaMalloc(&d, sizeof(cplx<T>) * h.size()));

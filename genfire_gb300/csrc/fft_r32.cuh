@@ -38,6 +38,11 @@ template <int N> struct R32 {
     static constexpr int ELEMS_ = Lay::SIZE > W * CS ? Lay::SIZE : W * CS;
     static constexpr int ELEMS = RowLay::SIZE > ELEMS_ ? RowLay::SIZE : ELEMS_;
     template <typename T> static constexpr size_t smem() { return (size_t)ELEMS * sizeof(cplx<T>); }
+    // the twiddle buffer of length N holds, after its N entries and the packed
+    // per-stage table, WN^(t k1) at TWT + k1 P + t: the P threads of a column
+    // read consecutive entries (one or two sectors per warp request; the
+    // table in its natural order, at t k1, spreads a request over 4-8)
+    static constexpr int TWT = N + packed_twiddle_count(N);
 
     // Out: slot s holds element t + P out_m(s)
     static __device__ __forceinline__ constexpr int out_m(int s)
@@ -137,7 +142,7 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) {
         const int slot = 8 * (k1 & 3) + (k1 >> 2);
-        const cplx<T> y = k1 ? ctw(x[slot], __ldg(tw + t * k1), INV) : x[slot];
+        const cplx<T> y = k1 ? ctw(x[slot], __ldg(tw + G::TWT + k1 * G::P + t), INV) : x[slot];
         Sc[k1 * G::ROW + t] = y;
     }
     __syncthreads();
@@ -173,8 +178,8 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
 // CTAs per SM the column passes are built for (registers <= 65536 / (128 x
 // this)).  512 points: 5 for the single-transform passes (96 registers), 4 for
 // the fused one (at 96 it spills, and measured no faster).  1024 points: 3
-// (168 registers; the 32-point second stage keeps more values live, and at 4
-// CTAs every variant spills).
+// (168 registers; the 32-point second stage keeps more values live; at 4
+// CTAs every variant spills, and the fused pass measured 1 % slower).
 constexpr int r32_col_min_blocks(int n, bool fused)
 {
     return n == 512 ? (fused ? 4 : 5) : 3;
@@ -197,7 +202,7 @@ __global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N, ZIN && ZOUT
     const int tile = blockIdx.x, other = blockIdx.y;
     const int col = tile * W + c;
     const bool cv = col < a.ncols;
-    const cplx<T> *twp = a.tw;  // tw[j] = exp(-2 pi i j / N)
+    const cplx<T> *twp = a.tw;  // twiddles<T>(N): see R32<N>::TWT
     cplx<T> x[32];
     {
         const cplx<T> *in = a.in + (long long)other * a.in_other + (long long)col * a.col_stride;

@@ -511,10 +511,10 @@ template <typename T> bool launch_rows_mix(const RowPassArgs<T> &a, bool forward
 
 // The power-of-two length whose packed table follows the n-entry twiddle
 // table: n itself, or N2 of n = N1 * N2 (N1 in {3, 5}, N2 >= 64); 0 if none.
-inline int packed_length(int n)
+constexpr int packed_length(int n)
 {
     if (n >= 8 && !(n & (n - 1))) return n;
-    for (int f : {3, 5})
+    for (int f = 3; f <= 5; f += 2)
         if (n % f == 0) {
             const int m = n / f;
             if (m >= 64 && !(m & (m - 1))) return m;
@@ -525,7 +525,7 @@ inline int packed_length(int n)
 // Size of the packed table appended to the n-entry twiddle table (0 when
 // packed_length(n) is 0); the host fills it in the order of P2Plan::twoff
 // for the length packed_length(n).
-inline int packed_twiddle_count(int n)
+constexpr int packed_twiddle_count(int n)
 {
     n = packed_length(n);
     if (!n) return 0;
