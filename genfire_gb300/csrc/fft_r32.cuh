@@ -177,12 +177,11 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
 
 // CTAs per SM the column passes are built for (registers <= 65536 / (128 x
 // this)).  512 points: 5 for the single-transform passes (96 registers), 4 for
-// the fused one (at 96 it spills, and measured no faster).  1024 points: 3
-// (168 registers; the 32-point second stage keeps more values live; at 4
-// CTAs every variant spills, and the fused pass measured 1 % slower).
+// the fused one (at 96 it spills, and measured no faster).  1024 points: 4
+// (128 registers, no spills; the 32-point second stage keeps more values live).
 constexpr int r32_col_min_blocks(int n, bool fused)
 {
-    return n == 512 ? (fused ? 4 : 5) : 3;
+    return n == 512 ? (fused ? 4 : 5) : 4;
 }
 
 // Column pass (the contract of k_colpass) for n = N.  ZIN: the input is the
