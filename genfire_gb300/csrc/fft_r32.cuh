@@ -127,22 +127,33 @@ __device__ __forceinline__ void dft32_regs(cplx<T> (&x)[32])
 
 // One N-point transform of the thread's 32 elements.  In: slot m holds
 // element t + P m.  Out: slot s holds element t + P out_m(s).  Uses the
-// CTA's exchange buffer (synchronises before and after writing it).  ZIN:
-// the elements of slots 8..23 are zero (the centred half of a box
-// transform: entries t + P m + N/4 mod N below N/2 lie in slots 0..7 and
-// 24..31).
+// CTA's exchange buffer (synchronises after writing it, and before unless
+// sync_in is false: no thread of the CTA has used the buffer yet).  ZIN: the
+// elements of slots 8..23 are zero (the centred half of a box transform:
+// entries t + P m + N/4 mod N below N/2 lie in slots 0..7 and 24..31).
 template <typename T, int N, bool INV, bool ZIN = false>
-__device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int t, const cplx<T> *__restrict__ tw)
+__device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int t, const cplx<T> *__restrict__ tw,
+                                        bool sync_in = true)
 {
     using G = R32<N>;
     dft32_regs<T, INV, ZIN>(x);
-    // WN^(t k1) and the exchange: S[k1][t]
-    __syncthreads();  // the buffer may still be read by the previous step
+    // WN^(t k1) and the exchange: S[k1][t].  The twiddles come from four
+    // loads, WN^(t b) for b = 1..3 and WN^(4t): k1 = 4a + b runs along the chain
+    // of b, one product by WN^(4t) per step (at most 7 products, a few units
+    // in the last place; 31 loads measured 3 % slower over the iteration)
+    if (sync_in) __syncthreads();  // the buffer may still be read by the previous step
     cplx<T> *Sc = S + c * G::CS;
+    const cplx<T> *tt = tw + G::TWT + t;  // tt[k1 P] = WN^(t k1)
+    cplx<T> cur[4] = {__ldg(tt + 4 * G::P), __ldg(tt + G::P), __ldg(tt + 2 * G::P), __ldg(tt + 3 * G::P)};
+    const cplx<T> w4 = cur[0];
 #pragma unroll
     for (int k1 = 0; k1 < 32; ++k1) {
-        const int slot = 8 * (k1 & 3) + (k1 >> 2);
-        const cplx<T> y = k1 ? ctw(x[slot], __ldg(tw + G::TWT + k1 * G::P + t), INV) : x[slot];
+        const int slot = 8 * (k1 & 3) + (k1 >> 2), b = k1 & 3;
+        cplx<T> y = x[slot];
+        if (k1) {
+            y = ctw(y, cur[b], INV);
+            if (k1 + 4 < 32) cur[b] = cmul(cur[b], w4);
+        }
         Sc[k1 * G::ROW + t] = y;
     }
     __syncthreads();
@@ -176,20 +187,18 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
 }
 
 // CTAs per SM the column passes are built for (registers <= 65536 / (128 x
-// this)).  512 points: 5 for the single-transform passes (96 registers), 4 for
-// the fused one (at 96 it spills, and measured no faster).  1024 points: 4
-// (128 registers, no spills; the 32-point second stage keeps more values live).
-constexpr int r32_col_min_blocks(int n, bool fused)
-{
-    return n == 512 ? (fused ? 4 : 5) : 4;
-}
+// this)).  512 points: 5 (96 registers; the fused pass spills 8 bytes there and
+// measured 5 % faster than at 4 CTAs).  1024 points: 4 (128 registers, no
+// spills; the 32-point second stage keeps more values live; 5 CTAs measured 3 %
+// slower over the iteration).
+constexpr int r32_col_min_blocks(int n) { return n == 512 ? 5 : 4; }
 
 // Column pass (the contract of k_colpass) for n = N.  ZIN: the input is the
 // centred half of a box (in_cnt N/2, in_c N/4) and the pass starts with a
 // forward transform; ZOUT: only the centred half is written (out_cnt N/2,
 // out_c N/4), so the final transform's other outputs are never formed.
 template <typename T, int N, bool ZIN, bool ZOUT>
-__global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N, ZIN && ZOUT)) k_col_r32(ColPassArgs<T> a)
+__global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N)) k_col_r32(ColPassArgs<T> a)
 {
     using G = R32<N>;
     constexpr int P = G::P, W = G::W;
@@ -224,7 +233,7 @@ __global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N, ZIN && ZOUT
     ErrAcc<T> err = 0;
     bool fwd_layout = false;  // slots in the output order of a transform
     if (a.mode & 1) {
-        r32_fft<T, N, false, ZIN>(x, s, c, t, twp);
+        r32_fft<T, N, false, ZIN>(x, s, c, t, twp, false);
         fwd_layout = true;
     }
     if (a.mode & 2) {
@@ -247,7 +256,7 @@ __global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N, ZIN && ZOUT
 #pragma unroll
             for (int m = 0; m < 32; ++m) x[m] = s[Lay::idx(t + P * m, c)];
         }
-        r32_fft<T, N, true>(x, s, c, t, twp);
+        r32_fft<T, N, true>(x, s, c, t, twp, (a.mode & 1) != 0);
         fwd_layout = true;
     }
     if (!fwd_layout || !cv) return;
@@ -330,7 +339,7 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
             x[m0 + i] = mk(va * (T)sa[i], vb * (T)sb[i]);
         }
     }
-    r32_fft<T, N, false, ZIN>(x, s, c, t, a.tw);
+    r32_fft<T, N, false, ZIN>(x, s, c, t, a.tw, false);
     __syncthreads();  // the exchange buffer becomes the natural-order tile
 #pragma unroll
     for (int sl = 0; sl < 32; ++sl) s[RowLay::idx(t + P * G::out_m(sl), c)] = x[sl];
