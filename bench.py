@@ -139,9 +139,10 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """dram bytes per launch of the dominant kernel from the committed ncu summary, if any."""
-    path = os.path.join(HERE, "profiles", "dr_iteration_euler256_traffic.txt")
+def committed_traffic(workload=WORKLOAD):
+    """dram bytes per launch of the dominant kernel from the committed ncu
+    summary of this workload's iteration, if any."""
+    path = os.path.join(HERE, "profiles", "dr_iteration_%s_traffic.txt" % workload)
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch"):
@@ -308,7 +309,8 @@ def run_ours(args, ws, rank, local, pg):
     k = int(np.argmax(ms))
     achieved = by[k] / (ms[k] * 1e-3) / 1e9
     roof = {"kernel": names[k], "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_kind": "of " + peak_kind, "traffic": committed_traffic(),
+            "frac": achieved / peak, "peak_kind": "of " + peak_kind,
+            "traffic": None if args.quick else committed_traffic(args.workload),
             "algorithmic_bytes_per_launch": by[k], "ms_per_launch": ms[k],
             "per_kernel": [{"kernel": names[i], "ms": ms[i], "bytes": by[i],
                             "GB/s": (by[i] / (ms[i] * 1e-3) / 1e9) if ms[i] > 0 else None} for i in range(len(ms))]}
