@@ -353,7 +353,7 @@ def run_ours(args, ws, rank, local, pg):
         "fft_pass_variants": {"F2": tuned[0], "F3": tuned[1], "I2": tuned[2],
                               "legend": "autotuned at setup: 0 generic shared-memory engine, 1 radix-8 register "
                                         "engine one column per thread, 2 the same with two columns per thread, "
-                                        "3 mixed-radix engine, 4 radix-32 x 16 engine (512 points, one exchange)"},
+                                        "3 mixed-radix engine, 4 radix-32 engine (512 or 1024 points, one exchange)"},
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": len(ms) * K,

@@ -483,7 +483,7 @@ class Recon:
 
     def tuning(self):
         """Autotuned FFT-pass variants (F2, F3, I2): 0 generic, 1 / 2 radix-8 register engine with 1 / 2
-        columns per thread, 3 mixed radix, 4 radix 32 x 16 (512 complex64 points)."""
+        columns per thread, 3 mixed radix, 4 radix-32 engine (512 or 1024 complex64 points)."""
         v = np.zeros(3, dtype=np.int32)
         self.ctx.check(load().genfire_recon_tuning(self._h, ptr(v, C.c_int32)))
         return [int(x) for x in v]

@@ -232,8 +232,9 @@ genfire_status genfire_recon_batch_destroy(genfire_recon_batch *b);
  * the dim-2 forward, the fused dim-3 and the dim-2 inverse pass; 0 = generic
  * shared-memory engine, 1 = register-resident radix 8, one column per thread,
  * 2 = the same with two columns per thread, 3 = mixed radix (3 or 5 times a
- * power of two), 4 = radix 32 x 16 for 512 complex64 points (one shared-memory
- * exchange per transform), -1 = built-in choice.  GENFIRE_COL_VARIANT=<v>
+ * power of two), 4 = radix 32 x 16 or 32 x 32 for 512 or 1024 complex64
+ * points (one shared-memory exchange per transform), -1 = built-in choice.
+ * GENFIRE_COL_VARIANT=<v>
  * forces variant v wherever it is valid. */
 genfire_status genfire_recon_tuning(genfire_recon *r, int32_t *variants);
 
