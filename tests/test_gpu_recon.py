@@ -35,6 +35,8 @@ CASES = [
     (8, 8, 2.0, 3, 1, 1, 12), (8, 8, 2.0, 1, 1, 1, 30), (8, 8, 2.0, 2, 1, 1, 30), (9, 9, 2.0, 3, 1, 1, 10),
     (8, 10, 2.0, 3, 1, 1, 10), (7, 7, 3.0, 3, 0, 1, 10), (8, 8, 2.0, 3, 1, 0, 8), (10, 8, 2.5, 3, 0, 0, 8),
     (16, 16, 2.0, 3, 1, 1, 20), (12, 12, 2.0, 1, 1, 1, 27),
+    # the longest transforms: n1 = 1024 (register engine) and 2048 (shared-memory engine) on thin grids
+    (512, 4, 2.0, 3, 1, 1, 3), (1024, 3, 2.0, 3, 1, 1, 2),
 ]
 
 

@@ -35,7 +35,7 @@ def test_iffshift3_ind_exact(ctx, oracle, size):
 
 
 @pytest.mark.parametrize("shape", [(8, 6, 10), (12, 15, 7), (16, 16, 16), (9, 25, 14), (64, 1, 3), (96, 40, 28),
-                                   (512, 2, 2), (1, 1, 7)])
+                                   (512, 2, 2), (1, 1, 7), (1024, 2, 3), (2, 2048, 2)])
 def test_fftn_fp64(lib, ctx, shape):
     rng = np.random.default_rng(sum(shape))
     a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
@@ -43,7 +43,8 @@ def test_fftn_fp64(lib, ctx, shape):
     assert rel(ctx.fftn(a, inverse=True), np.fft.ifftn(a)) < 1e-13
 
 
-@pytest.mark.parametrize("shape", [(8, 6, 10), (16, 16, 16), (9, 25, 14), (96, 40, 28), (1024, 2, 2)])
+@pytest.mark.parametrize("shape", [(8, 6, 10), (16, 16, 16), (9, 25, 14), (96, 40, 28), (1024, 2, 2), (2048, 2, 2),
+                                   (2, 2048, 3), (3, 2, 2048)])
 def test_fftn_complex64(lib, ctx, shape):
     rng = np.random.default_rng(sum(shape))
     a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
