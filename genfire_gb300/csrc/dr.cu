@@ -37,7 +37,7 @@ namespace gf {
 // twiddle tables, one per (device, n, precision), kept for the process: the
 // n entries exp(-2 pi i t / n), then (power-of-two n) the packed per-stage
 // table of the register-resident passes (P2Plan::twoff), copied from them,
-// then (n = 512, 1024) the radix-32 engines' table W_n^(t k1) ordered by k1
+// then (n = 128 .. 1024) the radix-32 engines' table W_n^(t k1) ordered by k1
 // then t (R32<n>::TWT)
 // ===========================================================================
 template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
@@ -51,7 +51,8 @@ template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
     auto it = cache.find(key);
     if (it != cache.end()) return static_cast<const cplx<T> *>(it->second);
     const int np = packed_twiddle_count(n);
-    const int nr = (n == 512 || n == 1024) ? 32 * (n / 32) : 0;  // radix-32 table: k1 < 32, t < n / 32
+    const bool r32 = n == 128 || n == 256 || n == 512 || n == 1024;
+    const int nr = r32 ? 32 * (n / 32) : 0;  // radix-32 table: k1 < 32, t < n / 32
     std::vector<cplx<T>> h((size_t)n + np + nr);
     const double pi = 3.14159265358979323846;
     for (int t = 0; t < n; ++t) {
@@ -78,7 +79,8 @@ template <typename T> const cplx<T> *twiddles(int n, cudaStream_t s)
     }
     if (nr) {
         const int P = n / 32;
-        const size_t o = (size_t)(n == 512 ? R32<512>::TWT : R32<1024>::TWT);
+        const size_t o = (size_t)(n == 128 ? R32<128>::TWT : n == 256 ? R32<256>::TWT
+                                  : n == 512 ? R32<512>::TWT : R32<1024>::TWT);
         if (o != (size_t)n + np) fail(GENFIRE_ERR_STATE, "internal: radix-32 twiddle table offset.");
         for (int k1 = 0; k1 < 32; ++k1)
             for (int t = 0; t < P; ++t) h[o + (size_t)k1 * P + t] = h[(size_t)t * k1];
@@ -213,12 +215,23 @@ template <typename T> static void ensure_smem_attrs()
     done.insert(dev);
 }
 
+// columns per CTA of the radix-32 engine for length n, 0 when it has none
+static int r32_width(int n)
+{
+    switch (n) {
+    case 128: return R32<128>::W;
+    case 256: return R32<256>::W;
+    case 512: return R32<512>::W;
+    case 1024: return R32<1024>::W;
+    default: return 0;
+    }
+}
+
 template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
 {
     if (v == kColGeneric) return true;
     if (v == kColR32)
-        return sizeof(T) == 4 && (a.pl.n == 512 || a.pl.n == 1024) && span_ok(a) &&
-               (!(a.mode & 4) || a.W == (a.pl.n == 512 ? R32<512>::W : R32<1024>::W));
+        return sizeof(T) == 4 && r32_width(a.pl.n) > 0 && span_ok(a) && (!(a.mode & 4) || a.W == r32_width(a.pl.n));
     if (v == kColMix) return span_ok(a) && mix_capable<T>(a.pl.n);
     if (!reg_capable(a)) return false;
     return v == kColReg1 || (v == kColReg2 && pair_capable(a));
@@ -234,13 +247,16 @@ template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
 // other lengths.
 template <typename T> static int default_col_variant(const ColPassArgs<T> &a)
 {
-    if (col_variant_ok(a, kColR32)) return kColR32;
+    // below 512 points the radix-32 engine is a candidate of the autotuner, not
+    // the built-in choice (at 256 points it took the 128^3 workload from 11.4 k
+    // to 12.8 k iterations/s; as the default it cost the batched problems 1.5 %)
+    if (a.pl.n >= 512 && col_variant_ok(a, kColR32)) return kColR32;
     if (reg_capable(a)) return ((a.mode & 3) == 3 && pair_capable(a)) ? kColReg2 : kColReg1;
     if (col_variant_ok(a, kColMix)) return kColMix;
     return kColGeneric;
 }
 
-// The radix-32 engines (512 or 1024 complex64 points), with compile-time
+// The radix-32 engines (128 to 1024 complex64 points), with compile-time
 // pruning when the pass reads / writes the centred half of a box.  Input
 // pruning only with output pruning (the fused dim-3 pass): the forward-only
 // 512-point variant with it takes 128 registers and measured 3 % slower.
@@ -251,9 +267,9 @@ template <typename T, int N> static void col_r32(const ColPassArgs<T> &a, int ot
     const bool zout = a.out_cnt == N / 2 && a.out_c == N / 4;
     const dim3 grid(cdiv(a.ncols, G::W), other);
     const size_t sm = G::template smem<T>();
-    if (zin && zout) k_col_r32<T, N, true, true><<<grid, kR32Threads, sm, st>>>(a);
-    else if (zout) k_col_r32<T, N, false, true><<<grid, kR32Threads, sm, st>>>(a);
-    else k_col_r32<T, N, false, false><<<grid, kR32Threads, sm, st>>>(a);
+    if (zin && zout) k_col_r32<T, N, true, true><<<grid, G::THREADS, sm, st>>>(a);
+    else if (zout) k_col_r32<T, N, false, true><<<grid, G::THREADS, sm, st>>>(a);
+    else k_col_r32<T, N, false, false><<<grid, G::THREADS, sm, st>>>(a);
 }
 template <typename T, int N> static void rows_r32(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
 {
@@ -262,11 +278,11 @@ template <typename T, int N> static void rows_r32(const RowPassArgs<T> &a, bool 
     const size_t sm = G::template smem<T>();
     const bool half = a.B1 == N / 2 && a.c1 == N / 4;  // the centred half of the row
     if (forward) {
-        if (half) k_row_r2c_r32<T, N, true><<<grid, kR32Threads, sm, st>>>(a);
-        else k_row_r2c_r32<T, N, false><<<grid, kR32Threads, sm, st>>>(a);
+        if (half) k_row_r2c_r32<T, N, true><<<grid, G::THREADS, sm, st>>>(a);
+        else k_row_r2c_r32<T, N, false><<<grid, G::THREADS, sm, st>>>(a);
     } else {
-        if (half) k_row_c2r_r32<T, N, true><<<grid, kR32Threads, sm, st>>>(a);
-        else k_row_c2r_r32<T, N, false><<<grid, kR32Threads, sm, st>>>(a);
+        if (half) k_row_c2r_r32<T, N, true><<<grid, G::THREADS, sm, st>>>(a);
+        else k_row_c2r_r32<T, N, false><<<grid, G::THREADS, sm, st>>>(a);
     }
 }
 
@@ -278,8 +294,12 @@ template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cu
     if (variant == kColAuto || !col_variant_ok(a, variant)) variant = default_col_variant(a);
     if (variant == kColR32) {
         if constexpr (sizeof(T) == 4) {
-            if (a.pl.n == 512) col_r32<T, 512>(a, other, st);
-            else col_r32<T, 1024>(a, other, st);
+            switch (a.pl.n) {
+            case 128: col_r32<T, 128>(a, other, st); break;
+            case 256: col_r32<T, 256>(a, other, st); break;
+            case 512: col_r32<T, 512>(a, other, st); break;
+            default: col_r32<T, 1024>(a, other, st); break;
+            }
         }
     } else if (variant == kColMix) {
         if (!launch_col_mix<T>(a, other, st)) fail(GENFIRE_ERR_STATE, "internal: mixed-radix pass not available.");

@@ -1,6 +1,6 @@
-// fft_r32.cuh -- 512- and 1024-point passes with 32 elements per thread.
+// fft_r32.cuh -- 128- to 1024-point passes with 32 elements per thread.
 //
-// An N-point transform (N = 32 * P, P = 16 or 32 threads per column) as one
+// An N-point transform (N = 32 * P, P = 4 .. 32 threads per column) as one
 // radix-32 stage and one radix-P stage with a single shared-memory exchange
 // between them; the radix-8 engine of fft_reg.cuh needs two (three at 1024),
 // and its exchanges are what bound those passes.  Thread t (0..P-1) of a
@@ -9,26 +9,26 @@
 //            (m = 8a + b: radix 4 over a, rotation W32^(b k1'), radix 8 over b),
 //            then times WN^(t k1) from the twiddle table;
 //   exchange: S[k1][t] = Y_t[k1];
-//   stage 2: X[k1 + 32 k2] = sum_t S[k1][t] WP^(t k2): for N = 512 the two
-//            16-point DFTs (radix 4 x 4) of k1 = t and t + 16, for N = 1024
-//            the 32-point DFT of k1 = t (the stage-1 schedule again); either
-//            way the thread ends with the elements t + P m' again.
+//   stage 2: X[k1 + 32 k2] = sum_t S[k1][t] WP^(t k2) for k1 = t + P h,
+//            h < 32 / P: the 4- or 8-point DFTs (N = 128, 256), the two
+//            16-point DFTs (radix 4 x 4, N = 512), or the 32-point DFT (the
+//            stage-1 schedule again, N = 1024); either way the thread ends
+//            with the elements t + P m' again.
 // The radix-4 and radix-8 butterflies are the packed-pair (f32x2) ones of
-// fft.cuh for complex64.  Every CTA has 128 threads: 8 columns of 16 threads
-// (N = 512) or 4 columns of 32 (N = 1024) -- the constraint table's tile
-// width for those lengths -- with the column fastest within a warp.
+// fft.cuh for complex64.  A CTA holds W columns of P threads -- W the
+// constraint table's tile width, 8 up to 512 points and 4 at 1024 -- with
+// the column fastest within a warp: 32, 64 or 128 threads.
 #pragma once
 
 #include "fft_reg.cuh"
 
 namespace gf {
 
-constexpr int kR32Threads = 128;
-
 template <int N> struct R32 {
-    static_assert(N == 512 || N == 1024, "radix-32 engines: 512 or 1024 points");
+    static_assert(N == 128 || N == 256 || N == 512 || N == 1024, "radix-32 engines: 128 to 1024 points");
     static constexpr int P = N / 32;                 // threads per column
-    static constexpr int W = kR32Threads / P;        // columns per CTA (8 or 4)
+    static constexpr int W = N <= 512 ? 8 : 4;       // columns per CTA
+    static constexpr int THREADS = P * W;
     static constexpr int ROW = P + 1;                // S[k1][t] row stride (odd: conflict-free reads)
     // column stride of the exchange buffer, 16 / W modulo 16: the W columns x
     // 16 / W threads of a half-warp hit 16 distinct 8-byte bank pairs
@@ -47,7 +47,9 @@ template <int N> struct R32 {
     // Out: slot s holds element t + P out_m(s)
     static __device__ __forceinline__ constexpr int out_m(int s)
     {
-        if constexpr (N == 512) return (s >> 4) + 2 * (((s & 15) >> 2) + 4 * (s & 3));
+        if constexpr (N == 128) return (s >> 2) + 8 * (s & 3);
+        else if constexpr (N == 256) return (s >> 3) + 4 * (s & 7);
+        else if constexpr (N == 512) return (s >> 4) + 2 * (((s & 15) >> 2) + 4 * (s & 3));
         else return 4 * (s & 7) + (s >> 3);
     }
     // slots of a transform's output that the centred half of a box keeps:
@@ -157,7 +159,16 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
         Sc[k1 * G::ROW + t] = y;
     }
     __syncthreads();
-    if constexpr (N == 512) {
+    if constexpr (N <= 256) {
+        // stage 2 for k1 = t + P h: slot P h + t' <- S[k1][t'], then the P-point
+        // DFT of each group (X[k1 + 32 k2] in slot P h + k2)
+#pragma unroll
+        for (int h = 0; h < 32 / G::P; ++h)
+#pragma unroll
+            for (int tp = 0; tp < G::P; ++tp) x[G::P * h + tp] = Sc[(t + G::P * h) * G::ROW + tp];
+#pragma unroll
+        for (int h = 0; h < 32 / G::P; ++h) Dft<G::P, T>::run(&x[G::P * h], INV, nullptr, G::P);
+    } else if constexpr (N == 512) {
         // stage 2 for k1 = t + 16 h: slot 16 h + t' <- S[k1][t']
 #pragma unroll
         for (int h = 0; h < 2; ++h)
@@ -186,12 +197,12 @@ __device__ __forceinline__ void r32_fft(cplx<T> (&x)[32], cplx<T> *S, int c, int
     }
 }
 
-// CTAs per SM the column passes are built for (registers <= 65536 / (128 x
+// CTAs per SM the column passes are built for (registers <= 65536 / (threads x
 // this)).  512 points: 5 (96 registers; the fused pass spills 8 bytes there and
 // measured 5 % faster than at 4 CTAs).  1024 points: 4 (128 registers, no
 // spills; the 32-point second stage keeps more values live; 5 CTAs measured 3 %
-// slower over the iteration).
-constexpr int r32_col_min_blocks(int n) { return n == 512 ? 5 : 4; }
+// slower over the iteration).  128 and 256 points: 128 registers.
+constexpr int r32_col_min_blocks(int n) { return n == 512 ? 5 : n == 1024 ? 4 : 2048 / n; }
 
 // L2 prefetch distance (blocks) of the single-transform 512-point column
 // passes: 380 took F2 and I2 from 0.080 / 0.082 to 0.076 / 0.078 ms at 512^3;
@@ -204,7 +215,7 @@ constexpr int r32_prefetch_ahead(int n, bool fused) { return (n == 512 && !fused
 // forward transform; ZOUT: only the centred half is written (out_cnt N/2,
 // out_c N/4), so the final transform's other outputs are never formed.
 template <typename T, int N, bool ZIN, bool ZOUT>
-__global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N)) k_col_r32(ColPassArgs<T> a)
+__global__ void __launch_bounds__(R32<N>::THREADS, r32_col_min_blocks(N)) k_col_r32(ColPassArgs<T> a)
 {
     using G = R32<N>;
     constexpr int P = G::P, W = G::W;
@@ -227,7 +238,7 @@ __global__ void __launch_bounds__(kR32Threads, r32_col_min_blocks(N)) k_col_r32(
         if (fb < nb && a.col_stride == 1) {
             const int ftile = (int)(fb % gridDim.x), fother = (int)(fb / gridDim.x);
             const cplx<T> *fin = a.in + (long long)fother * a.in_other + (long long)ftile * W;
-            for (int r = threadIdx.x; r < a.in_cnt; r += kR32Threads)
+            for (int r = threadIdx.x; r < a.in_cnt; r += G::THREADS)
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(fin + (long long)r * a.in_dim));
         }
     }
@@ -305,7 +316,7 @@ constexpr int kRowLoadGroup = 8;
 
 // ZIN: the rows are the centred half of the transform (B1 N/2, c1 N/4)
 template <typename T, int N, bool ZIN>
-__global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
+__global__ void __launch_bounds__(R32<N>::THREADS) k_row_r2c_r32(RowPassArgs<T> a)
 {
     using G = R32<N>;
     constexpr int P = G::P, W = G::W;
@@ -376,7 +387,7 @@ __global__ void __launch_bounds__(kR32Threads) k_row_r2c_r32(RowPassArgs<T> a)
 
 // ZOUT: only the centred half of each row is written (B1 N/2, c1 N/4)
 template <typename T, int N, bool ZOUT>
-__global__ void __launch_bounds__(kR32Threads) k_row_c2r_r32(RowPassArgs<T> a)
+__global__ void __launch_bounds__(R32<N>::THREADS) k_row_c2r_r32(RowPassArgs<T> a)
 {
     using G = R32<N>;
     constexpr int P = G::P, W = G::W;

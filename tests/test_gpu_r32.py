@@ -1,5 +1,5 @@
-"""The radix-32 engines (n = 512 as 32 x 16 and n = 1024 as 32 x 32,
-complex64; one shared-memory exchange per transform), forced with
+"""The radix-32 engines (n = 128 .. 1024 as 32 x 4 .. 32 x 32, complex64; one
+shared-memory exchange per transform), forced with
 GENFIRE_COL_VARIANT=4 wherever they are valid: transforms against numpy, and
 the fused dim-3 pass (constraint table, errK, Rfree capture), the dim-2
 passes and the row passes of a reconstruction against the oracle.  Bar: 1e-5
@@ -19,7 +19,8 @@ def r32(monkeypatch):
 
 
 @pytest.mark.parametrize("shape", [(8, 4, 512), (6, 512, 3), (512, 3, 5), (16, 512, 512),
-                                   (8, 4, 1024), (6, 1024, 3), (1024, 3, 5), (4, 1024, 1024)])
+                                   (8, 4, 1024), (6, 1024, 3), (1024, 3, 5), (4, 1024, 1024),
+                                   (8, 4, 256), (6, 256, 3), (256, 3, 5), (5, 128, 128), (128, 7, 9)])
 @pytest.mark.parametrize("inverse", [False, True])
 def test_r32_transforms(lib, ctx, r32, shape, inverse):
     rng = np.random.default_rng(sum(shape) + inverse)
@@ -39,7 +40,8 @@ def _measured(seed, D1, D2, os_, keep=0.5):
 
 
 @pytest.mark.parametrize("D1,D2,mode,os_", [(256, 4, 3, 2.0), (4, 256, 1, 2.0), (256, 4, 2, 2.0),
-                                           (512, 4, 3, 2.0), (4, 512, 1, 2.0), (400, 3, 3, 2.56)])
+                                           (512, 4, 3, 2.0), (4, 512, 1, 2.0), (400, 3, 3, 2.56),
+                                           (128, 4, 3, 2.0), (4, 128, 1, 2.0), (64, 5, 3, 2.0), (100, 3, 2, 2.56)])
 def test_r32_reconstruct_mixed(lib, ctx, oracle, r32, D1, D2, mode, os_):
     """n1 = 512 or 1024 puts the fused dim-3 pass (forward, constraint, errK,
     inverse) on the engine; n2 = 512 or 1024 the dim-2 forward and inverse
@@ -59,7 +61,7 @@ def test_r32_reconstruct_mixed(lib, ctx, oracle, r32, D1, D2, mode, os_):
     assert rel(rec, reco) < 1e-4
 
 
-@pytest.mark.parametrize("D1", [256, 512])
+@pytest.mark.parametrize("D1", [64, 128, 256, 512])
 def test_r32_rfree_capture(lib, ctx, oracle, r32, D1):
     D2, os_, N, nb = 4, 2.0, 3, 3
     M = _measured(5, D1, D2, os_)
