@@ -7,7 +7,7 @@
 // column holds the elements t + P m (m = 0..31) before and after a transform:
 //   stage 1: Y_t[k1] = sum_m x[t + P m] W32^(m k1) in registers
 //            (m = 8a + b: radix 4 over a, rotation W32^(b k1'), radix 8 over b),
-//            then times WN^(t k1) from the twiddle table;
+//            then times WN^(t k1) (four table entries and multiply chains);
 //   exchange: S[k1][t] = Y_t[k1];
 //   stage 2: X[k1 + 32 k2] = sum_t S[k1][t] WP^(t k2) for k1 = t + P h,
 //            h < 32 / P: the 4- or 8-point DFTs (N = 128, 256), the two
