@@ -63,3 +63,16 @@ def test_reference_arm_rank0_only():
         quick = True
         steps = 1
     assert bench.run_reference(A(), 2, 1) is None
+
+
+def test_committed_traffic_per_workload():
+    """The roofline's traffic comes from the committed capture of the
+    benchmarked workload's dominant kernel, and is absent for a workload
+    without one."""
+    sys.path.insert(0, ROOT)
+    import bench
+    t256 = bench.committed_traffic("euler256")
+    t512 = bench.committed_traffic("euler512")
+    assert t256 is not None and 4e8 < t256 < 7e8          # one 512^3 F3 launch (algorithmic 624 MB)
+    assert t512 is not None and 3e9 < t512 < 5e9          # one 1024^3 F3 launch (algorithmic 4.76 GB)
+    assert bench.committed_traffic("tilt64") is None
