@@ -279,3 +279,30 @@ def test_golden_turb3(oracle, golden):
     assert np.abs(flat[g["sample_idx"]] - g["sample_val"]).max() <= 1e-12 * np.abs(g["sample_val"]).max()
     assert np.count_nonzero(flat) == int(g["nnz"])
     assert np.allclose(rec[:, :, prm.Dim1 // 2], g["rec_slice"], rtol=0, atol=1e-12 * np.abs(g["rec_slice"]).max())
+
+
+def test_selection_randomized_against_numpy_restatement(oracle):
+    """Selection (plane distance, closest point, R \\ CP, box filter) of the C
+    oracle against the independent numpy restatement over random sizes,
+    oversampling ratios, cutoffs, both gridding extents, axis conventions and
+    angles, including right angles and the poles."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    angle = st.one_of(st.floats(-360, 360, allow_nan=False), st.sampled_from([0.0, 90.0, -90.0, 180.0, 45.0]))
+
+    @hyp.settings(max_examples=60, deadline=None, derandomize=True)
+    @hyp.given(D1=st.integers(3, 12), D2=st.integers(3, 12), os_=st.sampled_from([1.5, 2.0, 2.5, 3.0]),
+               cut=st.sampled_from([0.125, 0.3, 0.5, 0.7]), centro=st.sampled_from([0, 1]),
+               zyx=st.booleans(), phi=angle, theta=angle, psi=angle)
+    def check(D1, D2, os_, cut, centro, zyx, phi, theta, psi):
+        v3 = (1, 0, 0) if zyx else (0, 0, 1)
+        prm = oracle.make_params(D1, D2, 1, oversamplingRatio=os_, interpolationCutoffDistance=cut,
+                                 DFT_CentroSymmetricity=centro, vector3=v3)
+        n1, n2 = oracle.oversampled(D1, os_), oracle.oversampled(D2, os_)
+        Rf, nrm = oracle.proj_geometry(prm, phi, theta, psi)
+        a = oracle.select(n1, n2, centro, cut, Rf, nrm)
+        b = NR.select(n1, n2, centro, cut, Rf, nrm)
+        for x, y in zip(a[:4], b):
+            assert np.array_equal(x, y)
+
+    check()
