@@ -306,3 +306,34 @@ def test_selection_randomized_against_numpy_restatement(oracle):
             assert np.array_equal(x, y)
 
     check()
+
+
+def test_reconstruct_randomized_against_numpy_restatement(oracle):
+    """The loop of reconstruct.m in the C oracle against the numpy restatement
+    over random box shapes (odd and even, Dim1 != Dim2), oversampling ratios,
+    schedules, positivity and support switches, measured fractions and
+    iteration counts crossing the schedule's change points."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=25, deadline=None, derandomize=True)
+    @hyp.given(D1=st.integers(3, 9), D2=st.integers(3, 9), os_=st.sampled_from([2.0, 2.5, 3.0]),
+               mode=st.sampled_from([1, 2, 3]), pos=st.booleans(), sup_on=st.booleans(),
+               keep=st.sampled_from([0.2, 0.5, 0.9]), N=st.integers(1, 25), seed=st.integers(0, 2 ** 16))
+    def check(D1, D2, os_, mode, pos, sup_on, keep, N, seed):
+        rng = np.random.default_rng(seed)
+        n1, n2 = oracle.oversampled(D1, os_), oracle.oversampled(D2, os_)
+        sup = rng.random((D1, D2, D1)) < 0.8
+        vol = rng.random((D1, D2, D1)) * sup
+        M = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(NR.paddzero(vol, (n1, n2, n1)))))
+        M[rng.random(M.shape) > keep] = 0
+        M = np.asfortranarray(M)
+        prm = oracle.make_params(D1, D2, 1, oversamplingRatio=os_, numIterations=N, constraintEnforcementMode=mode,
+                                 constraintPositivity=int(pos), constraintSupport=int(sup_on))
+        r1, e1, _, _, _ = oracle.reconstruct(prm, M, support=sup)
+        r2, e2 = NR.reconstruct(M, N, sup, mode=mode, positivity=pos, use_support=sup_on)
+        scale = max(1.0, np.abs(r2).max())
+        assert np.abs(r1 - r2).max() <= 1e-12 * scale
+        assert np.allclose(e1, e2, rtol=0, atol=1e-12, equal_nan=True)
+
+    check()
