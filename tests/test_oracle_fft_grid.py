@@ -76,3 +76,36 @@ def test_grid_fft_dc_projection(oracle):
     M, _, _ = oracle.grid_fft(prm, projs, angles, allow_multiple=0, want_rec=False)
     m = D * os_
     assert abs(M[m // 2, m // 2, m // 2] - c * D * D) <= 1e-12 * c * D * D
+
+
+def test_grid_fft_randomized_against_numpy_restatement(oracle):
+    """FFT gridding of the C oracle against the numpy restatement over random
+    projection shapes, counts, oversampling ratios (integer cube sizes only),
+    cutoffs, both match rules and angles, including the zero and right-angle
+    poses that put samples exactly on voxels."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    angle = st.one_of(st.floats(-360, 360, allow_nan=False), st.sampled_from([0.0, 90.0, -90.0, 180.0]))
+
+    @hyp.settings(max_examples=30, deadline=None, derandomize=True)
+    @hyp.given(D2=st.integers(4, 12), dD1=st.integers(-2, 2), P=st.integers(1, 4), os_=st.sampled_from([1.5, 2.0, 3.0]),
+               cut=st.sampled_from([0.3, 0.7, 1.2]), am=st.sampled_from([0, 1]), seed=st.integers(0, 2 ** 16),
+               a0=st.tuples(angle, angle, angle))
+    def check(D2, dD1, P, os_, cut, am, seed, a0):
+        D1 = max(3, D2 + dD1)
+        if oracle.fft_grid_size(D2, os_) < 0 or oracle.fft_grid_size(D2, os_) < max(D1, D2):
+            return
+        rng = np.random.default_rng(seed)
+        projs = rng.random((D1, D2, P))
+        angles = np.stack([rng.uniform(0, 360, P), rng.uniform(-70, 70, P), rng.uniform(0, 360, P)], 1)
+        angles[0] = a0
+        prm = oracle.make_params(D1, D2, P, oversamplingRatio=os_, interpolationCutoffDistance=cut)
+        M, rec, n = oracle.grid_fft(prm, projs, angles, allow_multiple=am)
+        K, rec2, n2 = NR.fill_in_fourier_grid(projs, angles, os_, cut, am)
+        assert n == n2
+        assert np.array_equal(M != 0, K != 0)
+        scale = max(1.0, np.abs(K).max())
+        assert np.abs(M - K).max() <= 1e-12 * scale
+        assert np.abs(rec - rec2).max() <= 1e-12 * max(1.0, np.abs(rec2).max())
+
+    check()
