@@ -71,3 +71,25 @@ def test_rfactor_realspace(oracle):
         assert abs(R[q] - want) <= 1e-13 * want
         assert np.array_equal(simu[:, :, q], crop)
     assert abs(tot - R.mean()) <= 1e-15
+
+
+def test_projectors_randomized_against_numpy(oracle):
+    """Trilinear and cubic projectors of the C oracle against the numpy
+    restatements over random volume shapes (odd and even sides) and angles,
+    including right angles where samples fall on voxel faces."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+    angle = st.one_of(st.floats(-360, 360, allow_nan=False), st.sampled_from([0.0, 90.0, -90.0, 180.0]))
+
+    @hyp.settings(max_examples=30, deadline=None, derandomize=True)
+    @hyp.given(shape=st.tuples(st.integers(3, 9), st.integers(3, 9), st.integers(3, 9)), ang=st.tuples(angle, angle, angle),
+               seed=st.integers(0, 2 ** 16))
+    def check(shape, ang, seed):
+        vol = np.random.default_rng(seed).random(shape)
+        R = _rot(oracle, *ang)
+        for cubic, ref in ((False, NR.project), (True, NR.project_cubic)):
+            got = oracle.project_interp(vol, *ang, cubic=cubic)
+            want = ref(vol, R)
+            assert np.abs(got - want).max() <= 1e-12 * max(1.0, np.abs(want).max())
+
+    check()
