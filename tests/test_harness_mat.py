@@ -122,3 +122,40 @@ def test_reference_data_files(harness):
         assert info["name"] == name
         assert info["dims"] == "x".join(str(s) for s in arr.shape)
         assert float(info["sum"]) == _seq_sum(arr)
+
+
+def test_read_randomized(harness, tmp_path):
+    """Random shapes (including empty and large ones that compress into many
+    DEFLATE blocks), numeric classes, value ranges, names and compression,
+    written by scipy and read back by the harness's reader and inflater."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(shape=st.lists(st.integers(0, 40), min_size=2, max_size=4), dt=st.sampled_from(CLASSES),
+               compress=st.booleans(), scale=st.sampled_from([1.0, 100.0, 1e6]), runs=st.booleans(),
+               name=st.from_regex(r"[a-z][a-z0-9_]{0,30}", fullmatch=True), seed=st.integers(0, 2 ** 16))
+    def check(shape, dt, compress, scale, runs, name, seed):
+        rng = np.random.default_rng(seed)
+        n = int(np.prod(shape))
+        if runs:   # long runs of repeated values: back-references in the compressed stream
+            v = np.repeat(rng.random(max(1, n // 50 + 1)), 50)[:n]
+        else:
+            v = rng.random(n)
+        if np.issubdtype(dt, np.integer):
+            lo, hi = np.iinfo(dt).min, np.iinfo(dt).max
+            v = np.clip(np.round(v * scale * (1 if lo == 0 else 2) - (0 if lo == 0 else scale)), max(lo, -2 ** 52),
+                        min(hi, 2 ** 52))
+        else:
+            v = v * scale
+        a = np.asfortranarray(v.astype(dt).reshape(shape, order="F"))
+        f = str(tmp_path / "r.mat")
+        scipy_io.savemat(f, {name: a}, do_compression=compress)
+        d = {k: x for k, x in scipy_io.loadmat(f).items() if not k.startswith("__")}
+        (nm, arr), = d.items()
+        info = _info(harness, f)
+        assert info["name"] == nm
+        assert info["dims"] == "x".join(str(s) for s in arr.shape)
+        assert float(info["sum"]) == _seq_sum(arr)
+
+    check()
