@@ -159,3 +159,30 @@ def test_read_randomized(harness, tmp_path):
         assert float(info["sum"]) == _seq_sum(arr)
 
     check()
+
+
+def test_copy_randomized(harness, tmp_path):
+    """Random arrays of every numeric class through --mat-copy (reader, then
+    the Level-5 writer of double arrays): scipy reads back the same values."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=25, deadline=None, derandomize=True)
+    @hyp.given(shape=st.lists(st.integers(1, 30), min_size=2, max_size=4), dt=st.sampled_from(CLASSES),
+               compress=st.booleans(), seed=st.integers(0, 2 ** 16))
+    def check(shape, dt, compress, seed):
+        rng = np.random.default_rng(seed)
+        v = rng.standard_normal(int(np.prod(shape))) * 1000
+        if np.issubdtype(dt, np.integer):
+            v = np.abs(v) if np.iinfo(dt).min == 0 else v
+            v = np.clip(np.round(v), np.iinfo(dt).min, np.iinfo(dt).max)
+        a = np.asfortranarray(v.astype(dt).reshape(shape, order="F"))
+        src, dst = str(tmp_path / "s.mat"), str(tmp_path / "d.mat")
+        scipy_io.savemat(src, {"v": a}, do_compression=compress)
+        r = subprocess.run([harness, "--mat-copy", src, dst], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0, r.stderr
+        back = scipy_io.loadmat(dst)["v"]
+        want = scipy_io.loadmat(src)["v"].astype(np.float64)
+        assert back.shape == want.shape and np.array_equal(back.astype(np.float64), want)
+
+    check()
