@@ -337,3 +337,34 @@ def test_reconstruct_randomized_against_numpy_restatement(oracle):
         assert np.allclose(e1, e2, rtol=0, atol=1e-12, equal_nan=True)
 
     check()
+
+
+def test_symmetry_and_index_helpers_randomized(oracle):
+    """CentroSymmetricity, hermitianSymmetrize, make_Kspace_indices and the
+    pad / crop index ranges of the oracle against the numpy restatement over
+    random sizes of both parities."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(n1=st.integers(2, 13), n2=st.integers(2, 13), n3=st.integers(1, 11), seed=st.integers(0, 2 ** 16),
+               o=st.tuples(st.integers(1, 13), st.integers(1, 13), st.integers(1, 13)))
+    def check(n1, n2, n3, seed, o):
+        rng = np.random.default_rng(seed)
+        ext = oracle.grid_extent(n1, n2, 1)
+        FS = rng.standard_normal(tuple(ext[3:])) + 1j * rng.standard_normal(tuple(ext[3:]))
+        assert np.array_equal(oracle.centro(FS, n1, n1 // 2, n2), NR.centro(FS, n1, n1 // 2, n2))
+        x = rng.standard_normal((n1, n2, n3)) + 1j * rng.standard_normal((n1, n2, n3))
+        x[rng.random(x.shape) < 0.3] = 0
+        assert np.allclose(oracle.hermitian_symmetrize(x), NR.hermitian_symmetrize(x), rtol=0, atol=1e-15)
+        assert np.allclose(oracle.make_kspace_indices((n1, n2, n3)), NR.make_kspace_indices((n1, n2, n3)),
+                           rtol=0, atol=1e-15)
+        big = (n1, n2, n3)
+        ori = tuple(min(a, b) for a, b in zip(o, big))
+        vi = oracle.volumn_index(big, ori)
+        for i in range(3):
+            assert (vi[i, 0], vi[i, 1]) == NR.crop_range(big[i], ori[i])
+        v = rng.random(ori)
+        assert np.array_equal(oracle.stripzero(oracle.paddzero(v, big), ori), v)
+
+    check()
