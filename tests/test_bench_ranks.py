@@ -76,3 +76,23 @@ def test_committed_traffic_per_workload():
     assert t256 is not None and 4e8 < t256 < 7e8          # one 512^3 F3 launch (algorithmic 624 MB)
     assert t512 is not None and 3e9 < t512 < 5e9          # one 1024^3 F3 launch (algorithmic 4.76 GB)
     assert bench.committed_traffic("tilt64") is None
+
+
+def test_reference_arm_json_contract():
+    """`bench.py --impl reference` on the CPU (the oracle on the host cores, the
+    small workload): one JSON line with the contract's keys, the reference's
+    own metric and an e2e without host-device copies."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--quick",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("{")][-1]
+    d = json.loads(line)
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["unit"] == "iters/s"
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["e2e"]["value"] == d["value"]
