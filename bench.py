@@ -39,7 +39,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=30, help="timed FP64 iterations")
-    ap.add_argument("--rfactor-iters", type=int, default=50, help="iterations for the equal-R-factor comparison")
+    ap.add_argument("--rfactor-iters", type=int, default=None,
+                    help="iterations for the equal-R-factor comparison (default: the workload's own count, "
+                         "1000 for the 256^3 headline)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-problems leg")
@@ -259,7 +261,7 @@ def run_ours(args, ws, rank, local, pg):
     rec64.close()
 
     # ---- equal-iteration R-factors (reconstruct.m:176 form, ZYZ projector at the input angles)
-    NR_ = args.rfactor_iters
+    NR_ = args.rfactor_iters if args.rfactor_iters else (50 if args.quick else w["iters"])
     out = {}
     for prec, dM in ((G.PREC_MIXED, d_M32), (G.PREC_FP64, d_M64)):
         pr = params_for(G, w, prec, NR_)

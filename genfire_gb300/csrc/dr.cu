@@ -1,8 +1,9 @@
 // dr.cu -- the Fourier-constraint iteration of reconstruct.m on the GPU, the
 // recIFFT of the gridding, and the test-facing 3-D FFT.
 //
-// One iteration (reconstruct.m:117-186) is five FFT passes and two tiny
-// control kernels, captured once as a CUDA graph:
+// One iteration (reconstruct.m:117-186) is five FFT passes (five launches; the
+// loop's control updates run inside CTA 0 of F1 and I2), captured once as a
+// CUDA graph:
 //   F1         rows along dim 1: positivity and support, real -> half spectrum;
 //              its CTA 0 also starts the iteration (iteration count,
 //              constraint change points, bestErr reset)

@@ -26,12 +26,15 @@
 //   the epilogue reads the accumulators with tcgen05.ld (one row per thread,
 //   four warps per 32-lane quadrant, each a quarter of the columns) and
 //   contracts them with E_v, two 16-column groups at a time.
-// Every mbarrier wait is bounded by a clock limit; on expiry the kernel records
-// an error flag, stops issuing work, waits (bounded) for its copies and MMAs,
-// frees its TMEM and returns.
+// Every mbarrier wait is bounded by a clock limit; on expiry the CTA decides
+// to stop at a barrier with a reduction (so all its threads leave together),
+// records an error flag, waits (bounded) for its copies and MMAs still in
+// flight, frees its TMEM and returns.
 #include "internal.h"
 
 #include <cuda_bf16.h>
+
+#include <cstdlib>
 
 namespace gf {
 
@@ -94,11 +97,11 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 // bounded wait; returns false on expiry
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = kWaitCycles)
 {
     const long long t0 = clock64();
     while (!mbar_try(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
@@ -247,6 +250,7 @@ struct MmaArgs {
     int npad_last;            // columns of the last N chunk, a multiple of 64
     int *err;                 // set to 1 when a bounded wait expires
     int *queue;               // next tile to take (starts at 0)
+    long long wait_cycles;    // limit of the main loop's waits (the drain always allows kWaitCycles)
 };
 
 template <bool POW2>
@@ -260,7 +264,6 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     uint64_t *bar_mma = bar_load + 2;
     uint64_t *bar_done = bar_mma + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_done + 1);
-    int *abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     float2 *red = reinterpret_cast<float2 *>(smem_raw + 2 * kStageBytes + 128);  // 3 x 128 partial F
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -270,7 +273,6 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
         mbar_init(&bar_mma[0], 1);
         mbar_init(&bar_mma[1], 1);
         mbar_init(bar_done, 1);
-        *abort_flag = 0;
         mbar_fence_init();
     }
     if (warp == 0) {
@@ -282,8 +284,14 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    uint32_t n_load[2] = {0, 0}, n_mma[2] = {0, 0}, n_done = 0;  // completions issued per barrier
-    uint32_t w_load[2] = {0, 0}, w_mma[2] = {0, 0}, w_done = 0;  // completions waited per barrier
+    // Completions issued per barrier, and completions this thread has seen.  A
+    // phase counts as seen only when its wait succeeded, so after an expired
+    // wait thread 0's drain still waits for every copy and MMA in flight.  Every
+    // decision to stop is taken by a barrier with a reduction
+    // (__syncthreads_or), so all threads of the CTA leave at the same point.
+    uint32_t n_load[2] = {0, 0}, n_mma[2] = {0, 0}, n_done = 0;
+    uint32_t w_load[2] = {0, 0}, w_mma[2] = {0, 0}, w_done = 0;
+    const long long lim = a.wait_cycles;
     const double inv1 = 1.0 / (double)a.n1, inv2 = 1.0 / (double)a.n2;
     const int amin = -(a.D1 / 2), bmin = -(a.D2 / 2);
     const int r = tid & (kM - 1), h = tid >> 7;  // A generation: row r, quarter h of the 32-wide chunk
@@ -320,12 +328,12 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                 __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(st);  // re_hi, re_lo, im_hi, im_lo
                 __nv_bfloat16 *Bs = Ah + 4 * kATile;                          // hi, lo
                 // the MMAs that last read this stage must be complete
+                bool expired = false;
                 if (w_mma[s] < n_mma[s]) {
-                    if (!mbar_wait(&bar_mma[s], w_mma[s] & 1)) { *abort_flag = 1; }
-                    ++w_mma[s];
+                    if (mbar_wait(&bar_mma[s], w_mma[s] & 1, lim)) ++w_mma[s];
+                    else expired = true;
                 }
-                __syncthreads();
-                if (*abort_flag) { ok = false; break; }
+                if (__syncthreads_or(expired)) { ok = false; break; }
                 if (tid == 0) {
                     mbar_expect_tx(&bar_load[s], 2 * kBTile * 2);
                     const __nv_bfloat16 *src = Bp + (size_t)kc * 2 * kBTile;
@@ -360,10 +368,10 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
                 }
                 fence_proxy_async();
                 __syncthreads();
-                if (!mbar_wait(&bar_load[s], w_load[s] & 1)) *abort_flag = 1;
-                ++w_load[s];
-                __syncthreads();
-                if (*abort_flag) { ok = false; break; }
+                expired = false;
+                if (mbar_wait(&bar_load[s], w_load[s] & 1, lim)) ++w_load[s];
+                else expired = true;
+                if (__syncthreads_or(expired)) { ok = false; break; }
                 if (tid == 0) {
                     tc_fence_after();
                     const uint32_t a_base = saddr(Ah), b_base = saddr(Bs);
@@ -389,11 +397,11 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
             // all MMAs of this N chunk done -> epilogue
             if (tid == 0) mma_commit(bar_done);
             ++n_done;
-            if (!mbar_wait(bar_done, w_done & 1)) *abort_flag = 1;
-            ++w_done;
+            bool expired = false;
+            if (mbar_wait(bar_done, w_done & 1, lim)) ++w_done;
+            else expired = true;
             tc_fence_after();
-            __syncthreads();
-            if (*abort_flag) { ok = false; break; }
+            if (__syncthreads_or(expired)) { ok = false; break; }
             {
                 // F_j += sum_b Q(j,b) E_v(j,b): per 16-column group g, Horner's rule in
                 // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g);
@@ -453,12 +461,14 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     }
 
     if (!ok && tid == 0) atomicExch(a.err, 1);
-    // drain: bounded waits for copies and MMAs still in flight, then free TMEM
+    // drain: waits (full limit) for copies, MMAs and commits still in flight, then
+    // free TMEM.  At most one phase per barrier can be outstanding here.
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) {
-            while (w_load[s] < n_load[s]) { mbar_wait(&bar_load[s], w_load[s] & 1); ++w_load[s]; }
-            while (w_mma[s] < n_mma[s]) { mbar_wait(&bar_mma[s], w_mma[s] & 1); ++w_mma[s]; }
+            while (w_load[s] < n_load[s] && mbar_wait(&bar_load[s], w_load[s] & 1)) ++w_load[s];
+            while (w_mma[s] < n_mma[s] && mbar_wait(&bar_mma[s], w_mma[s] & 1)) ++w_mma[s];
         }
+        while (w_done < n_done && mbar_wait(bar_done, w_done & 1)) ++w_done;
     }
     tc_fence_before();
     __syncthreads();
@@ -532,6 +542,16 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     a.nkc = nkc; a.nnc = nnc; a.npad_last = npad_last;
     a.err = derr.as<int>();
     a.queue = derr.as<int>() + 1;
+    // GENFIRE_DEBUG_DFT_WAIT_CYCLES (a positive count of clock cycles) shortens
+    // the main loop's waits so that a test can make one expire and exercise the
+    // kernel's error path on real work: the drain still waits with the full
+    // limit for the copies and MMAs in flight, so the call returns
+    // GENFIRE_ERR_TIMEOUT with the context intact.
+    a.wait_cycles = kWaitCycles;
+    if (const char *dbg = std::getenv("GENFIRE_DEBUG_DFT_WAIT_CYCLES")) {
+        const long long v = std::atoll(dbg);
+        if (v > 0 && v < kWaitCycles) a.wait_cycles = v;
+    }
     const size_t smem = 2 * (size_t)kStageBytes + 128 + 3 * kM * sizeof(float2);
     const bool pow2 = a.log2n1 >= 0 && a.log2n2 >= 0;
     const void *kern = pow2 ? (const void *)k_dft_tcgen05<true> : (const void *)k_dft_tcgen05<false>;

@@ -314,21 +314,18 @@ void rfactor_realspace(genfire_ctx *ctx, int precision, const void *d_model, int
 constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB
 static __device__ __align__(256) unsigned char g_rfactor_scratch[kNoAllocScratchBytes];
 
-// Device address of the array on the current device.  The first call on a
-// device looks it up (cudaGetSymbolAddress) and caches it.
-static unsigned char *noalloc_scratch(int device)
+// Device address of the array in the current context.  Looked up on every
+// call (cudaGetSymbolAddress allocates nothing and is cheap once the module is
+// loaded): an address cached across calls would go stale when the device is
+// reset (MATLAB's reset(gpuDevice), cudaDeviceReset in another library), and a
+// kernel given it would write to memory that is no longer mapped.
+static unsigned char *noalloc_scratch()
 {
-    static std::mutex mu;
-    static std::map<int, unsigned char *> addr;
-    std::lock_guard<std::mutex> lk(mu);
-    auto it = addr.find(device);
-    if (it != addr.end()) return it->second;
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_rfactor_scratch);
     if (e != cudaSuccess || !p)
         fail(GENFIRE_ERR_CUDA, std::string("cudaGetSymbolAddress of the R-factor scratch array failed: ") +
                                    cudaGetErrorString(e));
-    addr[device] = static_cast<unsigned char *>(p);
     return static_cast<unsigned char *>(p);
 }
 
@@ -351,7 +348,7 @@ void rfactor_noalloc(genfire_ctx *ctx, int precision, const void *d_vol, int n1,
         fail(GENFIRE_ERR_ARG, "rfactor_noalloc: the inputs need more than the 4 MiB static scratch "
                               "(fewer projections per call, or genfire_rfactor).");
     cudaStream_t st = ctx->stream;
-    unsigned char *base = noalloc_scratch(ctx->device);
+    unsigned char *base = noalloc_scratch();
     const unsigned nblk = cdiv((size_t)n1 * n2, kProjThreads);
     double *dR = reinterpret_cast<double *>(base);
     double *part = reinterpret_cast<double *>(base + (sizeof(double) * 9 * (size_t)P + 255) / 256 * 256);

@@ -11,7 +11,11 @@
  * hold one zlib stream (RFC 1950) of such an element.  The DEFLATE decoder
  * (RFC 1951: stored, fixed-Huffman and dynamic-Huffman blocks, canonical
  * codes decoded one bit at a time) is written here so the harness needs no
- * library beyond libgenfire and libc.  Hosts are little-endian (x86-64 and
+ * library beyond libgenfire and libc.  Its canonical-code decoder is the
+ * published bit-at-a-time method of RFC 1951 section 3.2.2 (codes of each length
+ * counted, symbols listed in code order, a running first code and index per
+ * length), the same method as Mark Adler's reference decoder puff.c in the
+ * zlib distribution.  Hosts are little-endian (x86-64 and
  * AArch64 Linux); big-endian files are rejected.
  */
 #include "matio.h"

@@ -42,8 +42,9 @@ _PROPS = dict(
     particleWindowSize=None,
     # constraints (:57-60)
     constraintEnforcementMode=1, constraintPositivity=1, constraintSupport=1,
-    # DFT related (:62-65)
-    DFT_CentroSymmetricity=1, DFT_doGPU=1, Vol_ind=None,
+    # DFT related (:62-65).  DFT_doGPU keeps the reference's default and is not
+    # read: this implementation grids on the GPU whatever its value.
+    DFT_CentroSymmetricity=1, DFT_doGPU=0, Vol_ind=None,
     # temp saves (:67-70)
     save_temp=0, save_loopLength=50, saveFilename="./results/temp_rec",
     # this build: arithmetic of the GPU path, 'fp64' (drop-in) or 'mixed'

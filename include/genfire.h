@@ -331,10 +331,18 @@ genfire_status genfire_rfactor(genfire_ctx *ctx, int32_t precision,
  * (rotation matrices and partial sums) is a 4 MiB static device array in the
  * library, so the call allocates nothing; inputs needing more than 4 MiB of
  * scratch (about 9 * num_proj + 4 * num_proj * (ceil(n1*n2/256) + 1) doubles)
- * are rejected with GENFIRE_ERR_ARG.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  Every call uses the same array: calls whose GPU work
- * overlaps (from two host threads, or on two streams) race on it. */
+ * are rejected with GENFIRE_ERR_ARG.  Every call looks up the array's device
+ * address in the current context (cudaGetSymbolAddress, which allocates
+ * nothing), so a device reset between calls (reset(gpuDevice) in MATLAB) leaves
+ * no stale address behind; the context itself must be recreated after a reset,
+ * as for every other call.  vol and measured are read on the context's stream
+ * (genfire_stream), with no ordering against the stream that wrote them: the
+ * caller finishes writing them first (synchronize, or produce them on that
+ * stream).  The call copies the rotation matrices in and the sums out and
+ * waits for them, so it must not be called while any stream of the device is
+ * being captured into a CUDA graph.  Every call uses the same array: calls
+ * whose GPU work overlaps (from two host threads, or on two streams) race on
+ * it. */
 genfire_status genfire_rfactor_noalloc(genfire_ctx *ctx, int32_t precision, const void *d_vol, int32_t n1,
                                        int32_t n2, int32_t n3, int32_t num_proj, const double *angles,
                                        const double *vectors, const double *d_measured, double *Rarr,

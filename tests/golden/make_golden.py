@@ -54,8 +54,12 @@ def turb3_oracle(projs, angles):
                 errK=errK, recon_slice=recon[:, :, prm.Dim1 // 2].copy(), recon_l2=np.linalg.norm(recon))
 
 
-def main(ref="/root/reference"):
+def main(ref=None):
+    """ref: the reference tree (argument, or the GENFIRE_REFERENCE environment variable)."""
     import scipy.io
+    ref = ref or os.environ.get("GENFIRE_REFERENCE")
+    if not ref:
+        raise SystemExit("usage: make_golden.py <reference tree>  (or set GENFIRE_REFERENCE)")
     pj = scipy.io.loadmat(os.path.join(ref, "data_turb3", "pj_new_Turbu3_1015.mat"))["pj_new_Turbu3_1015"]
     an = scipy.io.loadmat(os.path.join(ref, "data_turb3", "angles_usedin_refine_1015.mat"))["euler_angles"]
     projs = np.asfortranarray(pj[:, :, ::4], dtype=np.float64)

@@ -106,10 +106,12 @@ def test_rejects_bad_files(harness, tmp_path):
     assert r.returncode == 1
 
 
-REF_DATA = "/root/reference/data_turb3"
+# the reference's data_turb3 folder, found through GENFIRE_REFERENCE (the reference tree)
+REF_DATA = os.path.join(os.environ.get("GENFIRE_REFERENCE", ""), "data_turb3")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_DATA), reason="the reference's data files are not on this machine")
+@pytest.mark.skipif(not os.environ.get("GENFIRE_REFERENCE") or not os.path.isdir(REF_DATA),
+                    reason="GENFIRE_REFERENCE does not name a reference tree with data_turb3 on this machine")
 def test_reference_data_files(harness):
     """The reference's own compressed MAT files read as scipy reads them."""
     for fn in sorted(os.listdir(REF_DATA)):

@@ -48,22 +48,48 @@ def _dev(a, dtype):
     return torch.from_numpy(flat).cuda()
 
 
-@pytest.mark.parametrize("precision_name", ["fp64", "mixed"])
-def test_noalloc_matches_rfactor_twice(lib, ctx, precision_name):
+CASES = [
+    (1, (40, 36, 32), 7, None),
+    (2, (24, 24, 24), 13, ((0, 0, 1), (0, 1, 0), (1, 0, 0))),
+    # more than one 64-projection chunk of the host-side staging (rotations up, sums back)
+    (4, (40, 36, 20), 100, None),
+]
+
+
+def _check_twice(lib, ctx, precision, cases):
     import torch
-    precision = lib.PREC_FP64 if precision_name == "fp64" else lib.PREC_MIXED
     rdt = np.float64 if precision == lib.PREC_FP64 else np.float32
-    for seed, shape, P, vectors in [(1, (40, 36, 32), 7, None), (2, (24, 24, 24), 13, ((0, 0, 1), (0, 1, 0), (1, 0, 0)))]:
+    for seed, shape, P, vectors in cases:
         vol, angles, meas = _case(seed, shape, P)
         d_vol, d_meas = _dev(vol, rdt), _dev(meas, np.float64)
         torch.cuda.synchronize()
         ref_errR, ref_R1, ref_R2 = ctx.rfactor(vol.astype(rdt), angles, meas, vectors=vectors, precision=precision)
-        for _ in range(2):
+        for call in range(2):
+            # the second call must not change the device's free memory: the
+            # first one has loaded everything the call needs
+            free0 = torch.cuda.mem_get_info()[0] if call == 1 else None
             st, errR, R1, R2 = _call(lib, ctx, precision, d_vol.data_ptr(), shape, angles, d_meas.data_ptr(), vectors)
+            if call == 1:
+                assert torch.cuda.mem_get_info()[0] == free0
             assert st == 0, lib._lib.load().genfire_last_error(ctx.handle)
             assert abs(errR - ref_errR) <= TOL * abs(ref_errR)
             assert np.abs(R1 - ref_R1).max() <= TOL * np.abs(ref_R1).max()
             assert np.abs(R2 - ref_R2).max() <= TOL * np.abs(ref_R2).max()
+
+
+@pytest.mark.parametrize("precision_name", ["fp64", "mixed"])
+def test_noalloc_matches_rfactor_twice(lib, ctx, precision_name):
+    precision = lib.PREC_FP64 if precision_name == "fp64" else lib.PREC_MIXED
+    _check_twice(lib, ctx, precision, CASES)
+
+
+def test_noalloc_cubic_matches_rfactor_twice(lib, ctx):
+    # the cubic-convolution projector through the same static scratch
+    assert lib._lib.load().genfire_set_projector_interpolation(ctx.handle, lib.INTERP_CUBIC) == 0
+    try:
+        _check_twice(lib, ctx, lib.PREC_FP64, [CASES[0], CASES[2]])
+    finally:
+        lib._lib.load().genfire_set_projector_interpolation(ctx.handle, lib.INTERP_TRILINEAR)
 
 
 def test_noalloc_rejects_oversized_inputs(lib, ctx):
