@@ -96,10 +96,30 @@ __device__ __forceinline__ bool mbar_try(uint64_t *bar, uint32_t parity)
         : "memory");
     return ok != 0;
 }
-// bounded wait; returns false on expiry
+// non-blocking test of a phase
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; returns false on expiry.  try_wait may suspend the thread for a
+// time the hardware chooses before it reports failure, so a limit shorter than
+// the default (the error-path test) polls with test_wait, which never suspends.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long limit = kWaitCycles)
 {
     const long long t0 = clock64();
+    if (limit < kWaitCycles) {
+        while (!mbar_test(bar, parity))
+            if (clock64() - t0 > limit) return false;
+        return true;
+    }
     while (!mbar_try(bar, parity))
         if (clock64() - t0 > limit) return false;
     return true;

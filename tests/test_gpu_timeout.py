@@ -1,8 +1,9 @@
 """The tensor-core gridding kernel's bounded waits, made to expire on real work.
 
 Every mbarrier wait of k_dft_tcgen05 has a clock limit.  GENFIRE_DEBUG_DFT_WAIT_CYCLES
-shortens the main loop's limit to one cycle, so a wait for a bulk copy or for
-the MMAs just issued expires while they are still in flight.  The kernel must
+shortens the main loop's limit to one cycle (polled with the non-blocking
+mbarrier.test_wait), so a wait for a bulk copy or for the MMAs just issued
+expires while they are still in flight.  The kernel must
 then stop at one barrier for the whole CTA, wait (with the full limit) for
 everything in flight, free its TMEM and return; the call reports
 GENFIRE_ERR_TIMEOUT.  The same context must then grid normally and match the
