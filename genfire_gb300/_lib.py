@@ -23,6 +23,7 @@ GENFIRE_ERR_STATE = 6
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_FP16_SCALED = 2
 
 PROFILE_KERNELS = 5   # GENFIRE_PROFILE_KERNELS: kernels of one iteration
 

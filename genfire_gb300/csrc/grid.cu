@@ -143,8 +143,8 @@ void check_params(const genfire_params &p, bool need_projs)
     if (!(p.oversamplingRatio >= 1.0) || p.oversamplingRatio > 64.0)
         fail(GENFIRE_ERR_ARG, "oversamplingRatio must be in [1, 64].");
     if (!(p.interpolationCutoffDistance > 0.0)) fail(GENFIRE_ERR_ARG, "interpolationCutoffDistance must be positive.");
-    if (p.precision != GENFIRE_PREC_FP64 && p.precision != GENFIRE_PREC_MIXED)
-        fail(GENFIRE_ERR_ARG, "precision must be GENFIRE_PREC_FP64 or GENFIRE_PREC_MIXED.");
+    if (p.precision != GENFIRE_PREC_FP64 && p.precision != GENFIRE_PREC_MIXED && p.precision != GENFIRE_PREC_FP16_SCALED)
+        fail(GENFIRE_ERR_ARG, "precision must be GENFIRE_PREC_FP64, GENFIRE_PREC_MIXED or GENFIRE_PREC_FP16_SCALED.");
     for (const double *v : {p.vector1, p.vector2, p.vector3})
         if (v[0] == 0 && v[1] == 0 && v[2] == 0) fail(GENFIRE_ERR_ARG, "rotation axis vectors must be non-zero.");
     int n1 = oversampled(p.Dim1, p.oversamplingRatio), n2 = oversampled(p.Dim2, p.oversamplingRatio);
@@ -759,9 +759,10 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     DevBuf F(sizeof(cplx<T>) * (size_t)std::max<long long>(sel.total, 1), st);
     double dft_kernel_ms = 0;
     if (sizeof(T) == sizeof(float)) {
-        // MIXED: split-BF16 tensor-core DFT (grid_mma.cu)
+        // MIXED / FP16_SCALED: split-BF16 / split-FP16 tensor-core DFT (grid_mma.cu)
         dft_tcgen05(ctx, d_proj, D1, D2, n1, n2, P, sel.nk, sel.off, sel.u.as<float>(), sel.v.as<float>(),
-                    reinterpret_cast<float2 *>(F.p), stage_ms ? &dft_kernel_ms : nullptr);
+                    reinterpret_cast<float2 *>(F.p), stage_ms ? &dft_kernel_ms : nullptr,
+                    p.precision == GENFIRE_PREC_FP16_SCALED);
     } else {
         // FP64: kDftJ consecutive points of one projection per CTA
         std::vector<DftTile> tiles;

@@ -1,38 +1,55 @@
-// grid_mma.cu -- the MIXED-precision gridding DFT on the 5th-generation tensor
-// cores (tcgen05, sm_103a).
+// grid_mma.cu -- the reduced-precision gridding DFT on the 5th-generation
+// tensor cores (tcgen05, sm_103a).
 //
 // For one projection P (D1 x D2) and a tile of 128 selected K-points j:
 //   Q(j, b) = sum_a E_u(j, a) P(a, b),  E_u(j, a) = exp(-2 pi i a u_j / n1)
 //   F_j     = sum_b Q(j, b) E_v(j, b),  E_v(j, b) = exp(-2 pi i b v_j / n2)
 // (fillInFourierGrid_DFT.m:243).  Q is a GEMM with M = 128 K-points, N = D2
-// (256-column chunks), K = D1 (32-wide chunks).  Operands are split into BF16
-// hi + lo parts and multiplied as hi*hi + hi*lo + lo*hi (FP32 accumulation),
-// which keeps ~16 significant bits of each operand:
-//   Re Q += Re(E_u)_hi P_hi + Re(E_u)_hi P_lo + Re(E_u)_lo P_hi   (TMEM cols   0..255)
-//   Im Q += Im(E_u)_hi P_hi + Im(E_u)_hi P_lo + Im(E_u)_lo P_hi   (TMEM cols 256..511)
-// * B (P, hi and lo) is pre-split once per projection into the canonical
-//   no-swizzle K-major layout and fed per K-chunk by cp.async.bulk (the TMA
-//   engine) into shared memory, completing on an mbarrier.
-// * A (E_u) is generated on the fly by the CTA's threads: per row, anchor
-//   phases are reduced exactly in FP64 (a*u is exact, the fractional part is
-//   taken before sincospi) and advanced by FP32 rotations within 16-element
-//   blocks, then split into BF16 hi/lo and stored in the same layout.
-// * Persistent: one CTA per SM drains the tiles of all projections from a
-//   device work queue (an atomic counter).
-// * One elected thread issues tcgen05.mma (M = 128, N = 256, K = 16) and
-//   tcgen05.commit; shared-memory stages are double buffered so the next
-//   chunk is generated while the tensor core works on the current one.
-// * 16 warps: each thread generates 8 consecutive k of one row of A per chunk;
-//   the epilogue reads the accumulators with tcgen05.ld (one row per thread,
-//   four warps per 32-lane quadrant, each a quarter of the columns) and
-//   contracts them with E_v, two 16-column groups at a time.
-// Every mbarrier wait is bounded by a clock limit; on expiry the CTA decides
-// to stop at a barrier with a reduction (so all its threads leave together),
-// records an error flag, waits (bounded) for its copies and MMAs still in
-// flight, frees its TMEM and returns.
+// and K = D1.  Operands are split into hi + lo parts of a 16-bit type and
+// multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation:
+//   Re Q += Re(E_u)_hi P_hi + Re(E_u)_hi P_lo + Re(E_u)_lo P_hi
+//   Im Q += Im(E_u)_hi P_hi + Im(E_u)_hi P_lo + Im(E_u)_lo P_hi
+// The 16-bit type is BF16 (GENFIRE_PREC_MIXED: ~16 significant bits per
+// operand) or FP16 (GENFIRE_PREC_FP16_SCALED: ~22 bits, with each projection
+// scaled by a power of two so that its largest value sits just below 2^14 and
+// the lo parts stay in FP16's normal range; the scale is undone exactly in the
+// epilogue).
+//
+// Work decomposition.  P is pre-split once into blocks of 128 columns (b) by
+// 256 rows (a) in the canonical no-swizzle K-major layout (128 KB per block,
+// hi and lo).  A unit of work is (tile of 128 points, block): the tile's
+// partial Q over the block's rows and columns, contracted with E_v over the
+// block's columns, gives a partial F; the partials of a point (one per block
+// of its projection, two for 256 x 256 projections) are summed in block order
+// afterwards.  Units are ordered by projection, block, tile, and each CTA
+// (one per SM) takes a contiguous range of them, so it keeps one block
+// resident in shared memory across many tiles and reloads it (one bulk copy)
+// only a few times.
+//
+// Warp roles in each CTA:
+//   warps 0-3   epilogue: thread = TMEM lane = point; tcgen05.ld of the Re and
+//               Im accumulators, Horner's rule in E_v(1) per 16-column group
+//               times an exact anchor E_v(b_g), partial F stored;
+//   warp 4      one thread loads blocks (cp.async.bulk into shared memory,
+//               completing on an mbarrier) and issues tcgen05.mma (M = 128,
+//               N <= 128, K = 16), committing to mbarriers;
+//   warps 5-12  A producers: per 32-wide K chunk, each thread forms 16
+//               consecutive E_u(j, a) of one point from an exact anchor and
+//               FP32 rotations, splits them into hi/lo and stores them in the
+//               K-major layout; three A stages.
+// The accumulator (Re and Im, 2 x 128 columns) is double buffered in TMEM, so
+// the epilogue of one unit overlaps the MMAs of the next.
+//
+// Every mbarrier wait is bounded by a clock limit.  A role whose wait expires
+// sets a shared abort flag; the other roles see it in their own waits and
+// stop.  The issuing thread then waits (full limit) for its MMAs (one final
+// tcgen05.commit) and its block copy in flight, every thread meets at one
+// barrier, TMEM is freed and the CTA returns; the host reports
+// GENFIRE_ERR_TIMEOUT.
 #include "internal.h"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cstdlib>
 
@@ -40,14 +57,8 @@ namespace gf {
 
 namespace umma {
 
-constexpr int kThreads = 512;      // 16 warps
-constexpr int kM = 128;            // rows per tile
+constexpr int kM = 128;            // rows (points) per tile
 constexpr int kKC = 32;            // K per chunk (two MMA k-steps of 16)
-constexpr int kNC = 256;           // N per chunk (columns of one accumulator)
-constexpr int kATile = kM * kKC;   // bf16 elements of one A array (8 KB)
-constexpr int kBTile = kNC * kKC;  // bf16 elements of one B array (16 KB)
-// stage: A re_hi, re_lo, im_hi, im_lo (4 x 8 KB) then B hi, lo (2 x 16 KB)
-constexpr int kStageBytes = 4 * kATile * 2 + 2 * kBTile * 2;  // 64 KB
 constexpr long long kWaitCycles = 4000000000LL;               // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -251,51 +262,129 @@ __device__ __forceinline__ float bf16_hi_f(uint32_t w) { return __uint_as_float(
 
 }  // namespace umma
 
-// One work item: a tile of up to 128 consecutive selected points of one projection.
-struct MmaTile {
+namespace umma {
+
+constexpr int kN = 128;                        // columns of one block (N of the MMAs)
+constexpr int kKR = 256;                       // rows of one block (its K range)
+constexpr int kKCB = kKR / kKC;                // K chunks per block (8)
+constexpr int kABytes = kM * kKC * 2;          // one A array of a chunk (8 KB)
+constexpr int kAStage = 4 * kABytes;           // re_hi, re_lo, im_hi, im_lo (32 KB)
+constexpr int kStages = 3;
+constexpr int kBArr = kN * kKC;                // elements of one B array of a chunk
+constexpr int kBChunk = 2 * kBArr * 2;         // hi + lo of one chunk (16 KB)
+constexpr int kBBytes = kKCB * kBChunk;        // one block (128 KB)
+constexpr int kEpiWarps = 4, kMmaWarp = 4, kProdWarp0 = 5, kProdWarps = 8;
+constexpr int kProdThreads = 32 * kProdWarps;
+constexpr int kWsThreads = 32 * (kProdWarp0 + kProdWarps);  // 416
+constexpr int kNBars = 2 * kStages + 4 + 3;    // afull, aempty, tfull x2, tempty x2, bfull, bdone, drain
+constexpr size_t kWsSmem = (size_t)kBBytes + kStages * kAStage + 8 * kNBars + 16;
+
+// kind::f16 instruction descriptor: FP32 accumulator, FP16 A and B, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+
+// Bounded wait that also stops when another role of the CTA has given up
+// (abort flag); an expired wait sets the flag.
+__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, long long limit, volatile int *abort_flag)
+{
+    const long long t0 = clock64();
+    const bool poll = limit < kWaitCycles;
+    for (;;) {
+        if (poll ? mbar_test(bar, parity) : mbar_try(bar, parity)) return true;
+        if (*abort_flag) return false;
+        if (clock64() - t0 > limit) {
+            *abort_flag = 1;
+            return false;
+        }
+    }
+}
+
+// two floats rounded to a packed pair of the 16-bit operand type (first at the
+// lower address), and the halves of such a pair back as floats (exact)
+template <bool F16> __device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    if constexpr (F16) {
+        __half2 t = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&t);
+    } else {
+        return pack_bf16(a, b);
+    }
+}
+template <bool F16> __device__ __forceinline__ float half_lo(uint32_t w)
+{
+    if constexpr (F16) return __half2float(__ushort_as_half((unsigned short)(w & 0xFFFFu)));
+    else return bf16_lo_f(w);
+}
+template <bool F16> __device__ __forceinline__ float half_hi(uint32_t w)
+{
+    if constexpr (F16) return __half2float(__ushort_as_half((unsigned short)(w >> 16)));
+    else return bf16_hi_f(w);
+}
+
+}  // namespace umma
+
+// One unit of work: a tile of up to 128 consecutive selected points of one
+// projection against one block (128 columns x 256 rows) of that projection.
+struct WsUnit {
+    long long j0;  // first point
     int proj;
-    int nj;
-    long long j0;
+    int blk;       // block index (proj * nnc + nc) * nkr + kr
+    int nj;        // points in the tile (<= 128)
+    int pad;
 };
 
-struct MmaArgs {
-    const __nv_bfloat16 *B;   // pre-split projections: [proj][nchunk][kchunk][hi|lo][256 x 32]
-    const MmaTile *tiles;
-    int ntiles;
+struct WsArgs {
+    const uint16_t *B;        // pre-split blocks: [blk][K chunk][hi|lo][128 x 32], 16-bit words
+    const WsUnit *units;
+    int nunits;
     const float *u, *v;
-    float2 *F;
-    int D1, D2, n1, n2;
-    int log2n1, log2n2;       // log2 of n1, n2 when powers of two, else -1
-    int nkc, nnc;             // K chunks (32 wide), N chunks (256 wide)
-    int npad_last;            // columns of the last N chunk, a multiple of 64
-    int *err;                 // set to 1 when a bounded wait expires
-    int *queue;               // next tile to take (starts at 0)
-    long long wait_cycles;    // limit of the main loop's waits (the drain always allows kWaitCycles)
+    const float *inv_scale;   // per projection (1 for BF16)
+    float2 *F;                // partial F: [part][ntot], part = nc * nkr + kr
+    long long ntot;
+    int D1, D2, D1p, D2p;     // D1p: D1 rounded up to 32; D2p: D2 rounded up to 16
+    int n1, n2, log2n1, log2n2;
+    int nnc, nkr;
+    int *err;                 // set to 1 when a bounded wait expired
+    long long wait_cycles;    // limit of the pipeline's waits (the drain always allows kWaitCycles)
 };
 
-template <bool POW2>
-__global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
+template <bool F16, bool POW2>
+__global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
 {
     using namespace umma;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // carve: [stage 0][stage 1] (64 KB each), then barriers and scratch
-    unsigned char *stage_base = smem_raw;
-    uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem_raw + 2 * kStageBytes);
-    uint64_t *bar_mma = bar_load + 2;
-    uint64_t *bar_done = bar_mma + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_done + 1);
-    float2 *red = reinterpret_cast<float2 *>(smem_raw + 2 * kStageBytes + 128);  // 3 x 128 partial F
+    unsigned char *sB = smem_raw;
+    unsigned char *sA = smem_raw + kBBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kBBytes + kStages * kAStage);
+    uint64_t *afull = bars, *aempty = bars + kStages, *tfull = bars + 2 * kStages, *tempty = tfull + 2;
+    uint64_t *bfull = tempty + 2, *bdone = bfull + 1, *drain = bdone + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + kNBars);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
-        mbar_init(&bar_load[0], 1);
-        mbar_init(&bar_load[1], 1);
-        mbar_init(&bar_mma[0], 1);
-        mbar_init(&bar_mma[1], 1);
-        mbar_init(bar_done, 1);
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&afull[s], kProdThreads);
+            mbar_init(&aempty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 32 * kEpiWarps);
+        }
+        mbar_init(bfull, 1);
+        mbar_init(bdone, 1);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
         mbar_fence_init();
     }
-    if (warp == 0) {
+    if (warp == kMmaWarp) {
         tmem_alloc(tmem_slot, 512);
         tmem_relinquish();
     }
@@ -304,266 +393,327 @@ __global__ void __launch_bounds__(umma::kThreads, 1) k_dft_tcgen05(MmaArgs a)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // Completions issued per barrier, and completions this thread has seen.  A
-    // phase counts as seen only when its wait succeeded, so after an expired
-    // wait thread 0's drain still waits for every copy and MMA in flight.  Every
-    // decision to stop is taken by a barrier with a reduction
-    // (__syncthreads_or), so all threads of the CTA leave at the same point.
-    uint32_t n_load[2] = {0, 0}, n_mma[2] = {0, 0}, n_done = 0;
-    uint32_t w_load[2] = {0, 0}, w_mma[2] = {0, 0}, w_done = 0;
+    // this CTA's contiguous range of units
+    const int u0 = (int)((long long)a.nunits * blockIdx.x / gridDim.x);
+    const int u1 = (int)((long long)a.nunits * (blockIdx.x + 1) / gridDim.x);
     const long long lim = a.wait_cycles;
-    const double inv1 = 1.0 / (double)a.n1, inv2 = 1.0 / (double)a.n2;
-    const int amin = -(a.D1 / 2), bmin = -(a.D2 / 2);
-    const int r = tid & (kM - 1), h = tid >> 7;  // A generation: row r, quarter h of the 32-wide chunk
-    bool ok = true;
+    const int nparts = a.nnc * a.nkr;
 
-    // tiles are drained from a device work queue: each CTA takes the next
-    // unclaimed tile when it finishes one
-    __shared__ int s_item;
-    for (;;) {
-        if (tid == 0) s_item = atomicAdd(a.queue, 1);
-        __syncthreads();
-        const int item = s_item;
-        __syncthreads();
-        if (item >= a.ntiles) break;
-        const MmaTile tl = a.tiles[item];
-        const bool row_ok = r < tl.nj;
-        const float uj = row_ok ? a.u[tl.j0 + r] : 0.f;
-        // epilogue row and column quarter
-        const int erow = (warp & 3) * 32 + lane, equart = warp >> 2;
-        const bool erow_ok = erow < tl.nj;
-        const float vj = erow_ok ? a.v[tl.j0 + erow] : 0.f;
-        float2 Fsum = make_float2(0.f, 0.f);
-
-        for (int nc = 0; nc < a.nnc && ok; ++nc) {
-            const int N = (nc == a.nnc - 1) ? a.npad_last : kNC;
-            const uint32_t idesc = idesc_bf16(kM, N);
-            // A anchors for this thread: S = E_u(amin + 8h), rotations by 1 and by 32
-            float2 S = row_ok ? phase_any<POW2>(amin + 8 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
-            const float2 w1 = phase_any<POW2>(1, uj, a.log2n1, inv1), w32 = phase_any<POW2>(32, uj, a.log2n1, inv1);
-            const __nv_bfloat16 *Bp = a.B + ((size_t)(tl.proj * a.nnc + nc) * a.nkc) * 2 * kBTile;
-            for (int kc = 0; kc < a.nkc; ++kc) {
-                const int s = kc & 1;
-                unsigned char *st = stage_base + s * kStageBytes;
-                __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(st);  // re_hi, re_lo, im_hi, im_lo
-                __nv_bfloat16 *Bs = Ah + 4 * kATile;                          // hi, lo
-                // the MMAs that last read this stage must be complete
-                bool expired = false;
-                if (w_mma[s] < n_mma[s]) {
-                    if (mbar_wait(&bar_mma[s], w_mma[s] & 1, lim)) ++w_mma[s];
-                    else expired = true;
-                }
-                if (__syncthreads_or(expired)) { ok = false; break; }
-                if (tid == 0) {
-                    mbar_expect_tx(&bar_load[s], 2 * kBTile * 2);
-                    const __nv_bfloat16 *src = Bp + (size_t)kc * 2 * kBTile;
-                    bulk_g2s(Bs, src, kBTile * 2, &bar_load[s]);
-                    bulk_g2s(Bs + kBTile, src + kBTile, kBTile * 2, &bar_load[s]);
-                }
-                ++n_load[s];
-                // A: 8 consecutive k for row r: k = 8h .. 8h+7 of this chunk
-                {
-                    float2 e = S;
-                    uint32_t rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        float2 e0 = e;
-                        e = cmulf(e, w1);
-                        float2 e1 = e;
-                        e = cmulf(e, w1);
-                        // hi: both values rounded in one conversion; lo from the
-                        // exact float values of the packed halves
-                        rh[q] = pack_bf16(e0.x, e1.x);
-                        ih[q] = pack_bf16(e0.y, e1.y);
-                        rl[q] = pack_bf16(e0.x - bf16_lo_f(rh[q]), e1.x - bf16_hi_f(rh[q]));
-                        il[q] = pack_bf16(e0.y - bf16_lo_f(ih[q]), e1.y - bf16_hi_f(ih[q]));
+    if (warp == kMmaWarp) {
+        if (lane == 0) {
+            // ---------------------------------------------------------------- MMA issue
+            int cur_blk = -1;
+            uint32_t g = 0, nbf = 0, nbd = 0;  // A chunks consumed; bfull / bdone phases seen
+            bool b_pending = false;             // a block copy issued but not seen complete
+            for (int i = u0; i < u1; ++i) {
+                const WsUnit un = a.units[i];
+                const int part = un.blk % nparts, nc = part / a.nkr, kr = part % a.nkr;
+                const int Nc = min(kN, a.D2p - kN * nc);
+                const int nkc = min(kKCB, (a.D1p - kKR * kr) / kKC);
+                bool ok = true;
+                if (un.blk != cur_blk) {
+                    if (cur_blk >= 0) {  // the MMAs that read the resident block must be complete
+                        mma_commit(bdone);
+                        if (!ws_wait(bdone, nbd & 1, lim, abort_flag)) break;
+                        ++nbd;
                     }
-                    S = cmulf(S, w32);
-                    // one 16-byte core-matrix row (k = 8h..8h+7) per array
-                    const int idx = kmaj_index(r, 8 * h);
-                    *reinterpret_cast<uint4 *>(Ah + 0 * kATile + idx) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-                    *reinterpret_cast<uint4 *>(Ah + 1 * kATile + idx) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-                    *reinterpret_cast<uint4 *>(Ah + 2 * kATile + idx) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-                    *reinterpret_cast<uint4 *>(Ah + 3 * kATile + idx) = make_uint4(il[0], il[1], il[2], il[3]);
+                    mbar_expect_tx(bfull, (uint32_t)(nkc * kBChunk));
+                    const unsigned char *src = reinterpret_cast<const unsigned char *>(a.B) + (size_t)un.blk * kBBytes;
+                    for (int c = 0; c < nkc; ++c) bulk_g2s(sB + c * kBChunk, src + (size_t)c * kBChunk, kBChunk, bfull);
+                    b_pending = true;
+                    if (!ws_wait(bfull, nbf & 1, lim, abort_flag)) break;
+                    ++nbf;
+                    b_pending = false;
+                    cur_blk = un.blk;
                 }
-                fence_proxy_async();
-                __syncthreads();
-                expired = false;
-                if (mbar_wait(&bar_load[s], w_load[s] & 1, lim)) ++w_load[s];
-                else expired = true;
-                if (__syncthreads_or(expired)) { ok = false; break; }
-                if (tid == 0) {
+                const int li = i - u0, buf = li & 1;
+                if (li >= 2 && !ws_wait(&tempty[buf], ((li >> 1) - 1) & 1, lim, abort_flag)) break;
+                tc_fence_after();
+                const uint32_t idesc = F16 ? idesc_f16(kM, Nc) : idesc_bf16(kM, Nc);
+                const uint32_t dre = tmem + (uint32_t)(buf * 256), dim = dre + 128;
+                for (int kc = 0; kc < nkc; ++kc, ++g) {
+                    const int s = (int)(g % kStages);
+                    if (!ws_wait(&afull[s], (g / kStages) & 1, lim, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
                     tc_fence_after();
-                    const uint32_t a_base = saddr(Ah), b_base = saddr(Bs);
+                    const uint32_t a_base = saddr(sA + s * kAStage), b_base = saddr(sB + kc * kBChunk);
 #pragma unroll
                     for (int ks = 0; ks < 2; ++ks) {
                         const uint32_t ko = ks * 16 * 16;  // 16 k = two core matrices = 256 bytes
-                        const uint64_t b_hi = sdesc(b_base + ko), b_lo = sdesc(b_base + kBTile * 2 + ko);
-                        const uint64_t a_rh = sdesc(a_base + ko), a_rl = sdesc(a_base + kATile * 2 + ko);
-                        const uint64_t a_ih = sdesc(a_base + 2 * kATile * 2 + ko), a_il = sdesc(a_base + 3 * kATile * 2 + ko);
+                        const uint64_t b_hi = sdesc(b_base + ko), b_lo = sdesc(b_base + kBArr * 2 + ko);
+                        const uint64_t a_rh = sdesc(a_base + ko), a_rl = sdesc(a_base + kABytes + ko);
+                        const uint64_t a_ih = sdesc(a_base + 2 * kABytes + ko), a_il = sdesc(a_base + 3 * kABytes + ko);
                         const uint32_t first = (kc == 0 && ks == 0) ? 0u : 1u;
-                        mma_bf16(tmem, a_rh, b_hi, idesc, first);
-                        mma_bf16(tmem, a_rh, b_lo, idesc, 1u);
-                        mma_bf16(tmem, a_rl, b_hi, idesc, 1u);
-                        mma_bf16(tmem + 256, a_ih, b_hi, idesc, first);
-                        mma_bf16(tmem + 256, a_ih, b_lo, idesc, 1u);
-                        mma_bf16(tmem + 256, a_il, b_hi, idesc, 1u);
+                        mma_bf16(dre, a_rh, b_hi, idesc, first);
+                        mma_bf16(dre, a_rh, b_lo, idesc, 1u);
+                        mma_bf16(dre, a_rl, b_hi, idesc, 1u);
+                        mma_bf16(dim, a_ih, b_hi, idesc, first);
+                        mma_bf16(dim, a_ih, b_lo, idesc, 1u);
+                        mma_bf16(dim, a_il, b_hi, idesc, 1u);
                     }
-                    mma_commit(&bar_mma[s]);
+                    mma_commit(&aempty[s]);  // the stage is free once these MMAs have read it
                 }
-                ++n_mma[s];
+                if (!ok) break;
+                mma_commit(&tfull[buf]);  // the unit's accumulator is complete
             }
-            if (!ok) break;
-            // all MMAs of this N chunk done -> epilogue
-            if (tid == 0) mma_commit(bar_done);
-            ++n_done;
-            bool expired = false;
-            if (mbar_wait(bar_done, w_done & 1, lim)) ++w_done;
-            else expired = true;
+            // drain: every MMA this thread issued, then a block copy still in flight
+            mma_commit(drain);
+            mbar_wait(drain, 0);
+            if (b_pending) mbar_wait(bfull, nbf & 1);
+        }
+    } else if (warp >= kProdWarp0) {
+        // -------------------------------------------------------------------- A producers
+        const int q = tid - kProdWarp0 * 32;
+        const int r = q & (kM - 1), h = q >> 7;  // point (row) and half of the 32-wide chunk
+        const double inv1 = 1.0 / (double)a.n1;
+        const int amin = -(a.D1 / 2);
+        uint32_t g = 0;
+        bool ok = true;
+        for (int i = u0; i < u1 && ok; ++i) {
+            const WsUnit un = a.units[i];
+            const int kr = (un.blk % nparts) % a.nkr;
+            const int nkc = min(kKCB, (a.D1p - kKR * kr) / kKC);
+            const bool row_ok = r < un.nj;
+            const float uj = row_ok ? a.u[un.j0 + r] : 0.f;
+            const float2 w1 = phase_any<POW2>(1, uj, a.log2n1, inv1);
+            for (int kc = 0; kc < nkc; ++kc, ++g) {
+                const int s = (int)(g % kStages);
+                if (g >= (uint32_t)kStages && !ws_wait(&aempty[s], ((g / kStages) - 1) & 1, lim, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                // 16 consecutive k of row r: a = amin + kr*256 + kc*32 + 16h + 0..15
+                float2 e = row_ok ? phase_any<POW2>(amin + kKR * kr + kKC * kc + 16 * h, uj, a.log2n1, inv1)
+                                  : make_float2(0.f, 0.f);
+                uint32_t rh[8], rl[8], ih[8], il[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float2 e0 = e;
+                    e = cmulf(e, w1);
+                    const float2 e1 = e;
+                    if (t < 7) e = cmulf(e, w1);
+                    // hi: both values rounded in one conversion; lo from the exact
+                    // float values of the packed halves
+                    rh[t] = pack2<F16>(e0.x, e1.x);
+                    ih[t] = pack2<F16>(e0.y, e1.y);
+                    rl[t] = pack2<F16>(e0.x - half_lo<F16>(rh[t]), e1.x - half_hi<F16>(rh[t]));
+                    il[t] = pack2<F16>(e0.y - half_lo<F16>(ih[t]), e1.y - half_hi<F16>(ih[t]));
+                }
+                uint16_t *As = reinterpret_cast<uint16_t *>(sA + s * kAStage);
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const int idx = kmaj_index(r, 16 * h + 8 * c);  // one 16-byte core-matrix row
+                    *reinterpret_cast<uint4 *>(As + 0 * (kABytes / 2) + idx) = make_uint4(rh[4 * c], rh[4 * c + 1], rh[4 * c + 2], rh[4 * c + 3]);
+                    *reinterpret_cast<uint4 *>(As + 1 * (kABytes / 2) + idx) = make_uint4(rl[4 * c], rl[4 * c + 1], rl[4 * c + 2], rl[4 * c + 3]);
+                    *reinterpret_cast<uint4 *>(As + 2 * (kABytes / 2) + idx) = make_uint4(ih[4 * c], ih[4 * c + 1], ih[4 * c + 2], ih[4 * c + 3]);
+                    *reinterpret_cast<uint4 *>(As + 3 * (kABytes / 2) + idx) = make_uint4(il[4 * c], il[4 * c + 1], il[4 * c + 2], il[4 * c + 3]);
+                }
+                fence_proxy_async();  // the stores are visible to the tensor core
+                mbar_arrive(&afull[s]);
+            }
+        }
+    } else {
+        // -------------------------------------------------------------------- epilogue
+        const int row = warp * 32 + lane;  // TMEM lane of this warp's quadrant
+        const double inv2 = 1.0 / (double)a.n2;
+        const int bmin = -(a.D2 / 2);
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int i = u0; i < u1; ++i) {
+            const WsUnit un = a.units[i];
+            const int part = un.blk % nparts, nc = part / a.nkr;
+            const int Nc = min(kN, a.D2p - kN * nc);
+            const int li = i - u0, buf = li & 1;
+            if (!ws_wait(&tfull[buf], (li >> 1) & 1, lim, abort_flag)) break;
             tc_fence_after();
-            if (__syncthreads_or(expired)) { ok = false; break; }
-            {
-                // F_j += sum_b Q(j,b) E_v(j,b): per 16-column group g, Horner's rule in
-                // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g);
-                // two groups per step (independent chains, one wait for both loads)
-                const int quarter = N / 4;               // columns per warp quarter (multiple of 16)
-                const int c0 = equart * quarter;
-                const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-                const float2 v1 = phase_any<POW2>(1, vj, a.log2n2, inv2);
-                for (int c = 0; c < quarter; c += 32) {
-                    const bool two = c + 16 < quarter;   // warp-uniform
-                    uint32_t re0[16], im0[16], re1[16], im1[16];
-                    const uint32_t col = (uint32_t)(c0 + c);
-                    tmem_ld16(tmem + lane_base + col, re0);
-                    tmem_ld16(tmem + lane_base + 256u + col, im0);
-                    if (two) {
-                        tmem_ld16(tmem + lane_base + col + 16u, re1);
-                        tmem_ld16(tmem + lane_base + 256u + col + 16u, im1);
-                    }
-                    const int b0 = bmin + nc * kNC + c0 + c;
-                    const float2 an0 = erow_ok ? phase_any<POW2>(b0, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
-                    const float2 an1 = (erow_ok && two) ? phase_any<POW2>(b0 + 16, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
-                    tmem_wait_ld();
-                    float2 h0 = make_float2(__uint_as_float(re0[15]), __uint_as_float(im0[15]));
+            const bool row_ok = row < un.nj;
+            const float vj = row_ok ? a.v[un.j0 + row] : 0.f;
+            const float2 v1 = phase_any<POW2>(1, vj, a.log2n2, inv2);
+            const uint32_t cre = tmem + lane_base + (uint32_t)(buf * 256), cim = cre + 128;
+            float2 Fsum = make_float2(0.f, 0.f);
+            // F += sum_b Q(j,b) E_v(j,b): per 16-column group, Horner's rule in
+            // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g);
+            // two groups per step (independent chains, one wait for both loads)
+            for (int c = 0; c < Nc; c += 32) {
+                const bool two = c + 16 < Nc;  // warp-uniform
+                uint32_t re0[16], im0[16], re1[16], im1[16];
+                tmem_ld16(cre + (uint32_t)c, re0);
+                tmem_ld16(cim + (uint32_t)c, im0);
+                if (two) {
+                    tmem_ld16(cre + (uint32_t)(c + 16), re1);
+                    tmem_ld16(cim + (uint32_t)(c + 16), im1);
+                }
+                const int b0 = bmin + kN * nc + c;
+                const float2 an0 = row_ok ? phase_any<POW2>(b0, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
+                const float2 an1 = (row_ok && two) ? phase_any<POW2>(b0 + 16, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
+                tmem_wait_ld();
+                float2 h0 = make_float2(__uint_as_float(re0[15]), __uint_as_float(im0[15]));
 #pragma unroll
-                    for (int i = 14; i >= 0; --i) {
-                        const float2 t = cmulf(h0, v1);
-                        h0 = make_float2(t.x + __uint_as_float(re0[i]), t.y + __uint_as_float(im0[i]));
-                    }
-                    const float2 p0 = cmulf(h0, an0);
-                    Fsum.x += p0.x;
-                    Fsum.y += p0.y;
-                    if (two) {
-                        float2 h1 = make_float2(__uint_as_float(re1[15]), __uint_as_float(im1[15]));
+                for (int t = 14; t >= 0; --t) {
+                    const float2 m = cmulf(h0, v1);
+                    h0 = make_float2(m.x + __uint_as_float(re0[t]), m.y + __uint_as_float(im0[t]));
+                }
+                const float2 p0 = cmulf(h0, an0);
+                Fsum.x += p0.x;
+                Fsum.y += p0.y;
+                if (two) {
+                    float2 h1 = make_float2(__uint_as_float(re1[15]), __uint_as_float(im1[15]));
 #pragma unroll
-                        for (int i = 14; i >= 0; --i) {
-                            const float2 t = cmulf(h1, v1);
-                            h1 = make_float2(t.x + __uint_as_float(re1[i]), t.y + __uint_as_float(im1[i]));
-                        }
-                        const float2 p1 = cmulf(h1, an1);
-                        Fsum.x += p1.x;
-                        Fsum.y += p1.y;
+                    for (int t = 14; t >= 0; --t) {
+                        const float2 m = cmulf(h1, v1);
+                        h1 = make_float2(m.x + __uint_as_float(re1[t]), m.y + __uint_as_float(im1[t]));
                     }
+                    const float2 p1 = cmulf(h1, an1);
+                    Fsum.x += p1.x;
+                    Fsum.y += p1.y;
                 }
             }
             tc_fence_before();
-            __syncthreads();  // TMEM reads finished before the next MMAs overwrite it
+            mbar_arrive(&tempty[buf]);  // this thread's TMEM reads of the buffer are complete
+            if (row_ok) {
+                const float sc = a.inv_scale[un.proj];
+                a.F[(size_t)part * a.ntot + un.j0 + row] = make_float2(Fsum.x * sc, Fsum.y * sc);
+            }
         }
-        if (!ok) break;
-        // combine the four column quarters of each row and store
-        if (equart > 0) red[(equart - 1) * kM + erow] = Fsum;
-        __syncthreads();
-        if (equart == 0 && erow_ok) {
-            const float2 o1 = red[erow], o2 = red[kM + erow], o3 = red[2 * kM + erow];
-            a.F[tl.j0 + erow] = make_float2(((Fsum.x + o1.x) + o2.x) + o3.x, ((Fsum.y + o1.y) + o2.y) + o3.y);
-        }
-        __syncthreads();
     }
 
-    if (!ok && tid == 0) atomicExch(a.err, 1);
-    // drain: waits (full limit) for copies, MMAs and commits still in flight, then
-    // free TMEM.  At most one phase per barrier can be outstanding here.
-    if (tid == 0) {
-        for (int s = 0; s < 2; ++s) {
-            while (w_load[s] < n_load[s] && mbar_wait(&bar_load[s], w_load[s] & 1)) ++w_load[s];
-            while (w_mma[s] < n_mma[s] && mbar_wait(&bar_mma[s], w_mma[s] & 1)) ++w_mma[s];
-        }
-        while (w_done < n_done && mbar_wait(bar_done, w_done & 1)) ++w_done;
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 512);
+    if (tid == 0 && *abort_flag) atomicExch(a.err, 1);
+    if (warp == kMmaWarp) tmem_dealloc(tmem, 512);
 }
 
-// Pre-split projections into BF16 hi/lo in the B layout (one 16 KB array per
-// (projection, N chunk, K chunk, hi|lo)); zero beyond D1 x D2.
-// Grid: x = (projection, N chunk, K chunk) block of B, y = 1024-element slice
-// of its kBTile elements (four per thread).
-constexpr int kSplitSlice = 1024;
-__global__ void __launch_bounds__(256) k_split_projections(const double *__restrict__ proj, int D1, int D2, int nkc,
-                                                           int nnc, __nv_bfloat16 *__restrict__ B)
+// Per-projection power-of-two scales for FP16 operands: 2^(14 - e) with
+// max|P| < 2^e, so that the largest scaled value is below 2^14; inv = 2^(e - 14).
+__global__ void __launch_bounds__(256) k_proj_scale(const double *__restrict__ proj, long long per, float *scale,
+                                                    float *inv_scale)
+{
+    const double *src = proj + (long long)blockIdx.x * per;
+    float m = 0.f;
+    for (long long i = threadIdx.x; i < per; i += 256) m = fmaxf(m, fabsf((float)src[i]));
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ float wm[8];
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) m = fmaxf(m, wm[w]);
+        m = fmaxf(m, wm[0]);
+        int e = 0;
+        if (m > 0.f) frexpf(m, &e);
+        const int sh = max(-100, min(100, 14 - e));
+        scale[blockIdx.x] = m > 0.f ? ldexpf(1.f, sh) : 1.f;
+        inv_scale[blockIdx.x] = m > 0.f ? ldexpf(1.f, -sh) : 1.f;
+    }
+}
+
+// Pre-split (scaled) projections into hi/lo blocks in the B layout: block
+// (p, nc, kr) holds columns b = 128 nc + (0..127) and rows a = 256 kr + (0..255)
+// as 8 K chunks of [hi | lo][128 x 32]; zero beyond D1 x D2.
+// Grid: x = block, y = K chunk; each thread converts 16 elements.
+template <bool F16>
+__global__ void __launch_bounds__(256) k_split_projections(const double *__restrict__ proj, int D1, int D2, int nnc,
+                                                           int nkr, const float *__restrict__ scale,
+                                                           uint16_t *__restrict__ B)
 {
     using namespace umma;
-    const int blk = blockIdx.x;  // (p * nnc + nc) * nkc + kc
-    const int kc = blk % nkc, nc = (blk / nkc) % nnc, p = blk / (nkc * nnc);
+    const int blk = blockIdx.x, kc = blockIdx.y;
+    const int kr = blk % nkr, nc = (blk / nkr) % nnc, p = blk / (nkr * nnc);
     const double *src = proj + (long long)p * D1 * D2;
-    __nv_bfloat16 *dst = B + (long long)blk * 2 * kBTile;
-#pragma unroll
-    for (int i = 0; i < kSplitSlice / 256; ++i) {
-        const int e = blockIdx.y * kSplitSlice + i * 256 + threadIdx.x;
+    const float sc = scale[p];
+    uint16_t *dst = B + (size_t)blk * (kBBytes / 2) + (size_t)kc * (2 * kBArr);
+    for (int e = threadIdx.x; e < kBArr; e += 256) {
         // e is the linear position in the layout: invert kmaj_index
         const int rg = e >> 8, kg = (e >> 6) & 3, rr = (e >> 3) & 7, kk = e & 7;
-        const int b = nc * kNC + rg * 8 + rr, aa = kc * kKC + kg * 8 + kk;
-        const float xf = (b < D2 && aa < D1) ? (float)src[aa + (long long)D1 * b] : 0.f;
-        const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-        dst[e] = hi;
-        dst[kBTile + e] = __float2bfloat16_rn(xf - __bfloat162float(hi));
+        const int b = nc * kN + rg * 8 + rr, aa = kr * kKR + kc * kKC + kg * 8 + kk;
+        const float xf = (b < D2 && aa < D1) ? (float)src[aa + (long long)D1 * b] * sc : 0.f;
+        if constexpr (F16) {
+            const __half hi = __float2half_rn(xf);
+            dst[e] = __half_as_ushort(hi);
+            dst[kBArr + e] = __half_as_ushort(__float2half_rn(xf - __half2float(hi)));
+        } else {
+            const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+            dst[e] = __bfloat16_as_ushort(hi);
+            dst[kBArr + e] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
+        }
+    }
+}
+
+// F[j] = sum over the parts of partial F (in part order).
+__global__ void k_sum_parts(const float2 *__restrict__ Fp, int nparts, long long ntot, float2 *__restrict__ F)
+{
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < ntot; j += (long long)gridDim.x * blockDim.x) {
+        float2 s = Fp[j];
+        for (int q = 1; q < nparts; ++q) {
+            const float2 t = Fp[(size_t)q * ntot + j];
+            s.x += t.x;
+            s.y += t.y;
+        }
+        F[j] = s;
     }
 }
 
 // Host: F (float2, one per selected point) for all projections.
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
                  const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
-                 const float *d_v, float2 *d_F, double *kernel_ms)
+                 const float *d_v, float2 *d_F, double *kernel_ms, bool fp16)
 {
     using namespace umma;
     cudaStream_t st = ctx->stream;
-    const int nkc = (D1 + kKC - 1) / kKC;
-    const int nnc = (D2 + kNC - 1) / kNC;
-    const int last = D2 - (nnc - 1) * kNC;
-    const int npad_last = (last + 63) / 64 * 64;  // four epilogue quarters of whole 16-column groups
-    const size_t nB = (size_t)P * nnc * nkc * 2 * kBTile;
-    DevBuf B(nB * sizeof(__nv_bfloat16), st);
-    {
-        static_assert(kBTile % kSplitSlice == 0, "split slices");
-        k_split_projections<<<dim3((unsigned)(P * nnc * nkc), kBTile / kSplitSlice), 256, 0, st>>>(
-            d_proj, D1, D2, nkc, nnc, B.as<__nv_bfloat16>());
+    const int D1p = (D1 + kKC - 1) / kKC * kKC, D2p = (D2 + 15) / 16 * 16;
+    const int nnc = (D2p + kN - 1) / kN, nkr = (D1p + kKR - 1) / kKR;
+    const int nparts = nnc * nkr;
+    const int nblk = P * nnc * nkr;
+    long long ntot = 0;
+    for (int p = 0; p < P; ++p) ntot += nk[p];
+    if (ntot == 0) return;
+
+    DevBuf B((size_t)nblk * kBBytes, st), scl(2 * sizeof(float) * P, st);
+    float *d_scale = scl.as<float>(), *d_inv = d_scale + P;
+    if (fp16) {
+        k_proj_scale<<<P, 256, 0, st>>>(d_proj, (long long)D1 * D2, d_scale, d_inv);
         GF_CHECK_LAUNCH();
+    } else {
+        std::vector<float> ones(2 * (size_t)P, 1.f);
+        GF_CUDA(cudaMemcpyAsync(d_scale, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, st));
+        GF_CUDA(cudaStreamSynchronize(st));  // the staging vector goes out of scope below
     }
-    std::vector<MmaTile> tiles;
+    if (fp16)
+        k_split_projections<true><<<dim3((unsigned)nblk, kKCB), 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, B.as<uint16_t>());
+    else
+        k_split_projections<false><<<dim3((unsigned)nblk, kKCB), 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, B.as<uint16_t>());
+    GF_CHECK_LAUNCH();
+
+    // units ordered by projection, block, tile
+    std::vector<WsUnit> units;
     for (int p = 0; p < P; ++p)
-        for (long long j = 0; j < nk[p]; j += kM)
-            tiles.push_back(MmaTile{p, (int)std::min<long long>(kM, nk[p] - j), off[p] + j});
-    if (tiles.empty()) return;
-    DevBuf dt(sizeof(MmaTile) * tiles.size(), st), derr(2 * sizeof(int), st);
-    GF_CUDA(cudaMemcpyAsync(dt.p, tiles.data(), sizeof(MmaTile) * tiles.size(), cudaMemcpyHostToDevice, st));
-    GF_CUDA(cudaMemsetAsync(derr.p, 0, 2 * sizeof(int), st));
-    MmaArgs a;
-    a.B = B.as<__nv_bfloat16>();
-    a.tiles = dt.as<MmaTile>();
-    a.ntiles = (int)tiles.size();
+        for (int nc = 0; nc < nnc; ++nc)
+            for (int kr = 0; kr < nkr; ++kr)
+                for (long long j = 0; j < nk[p]; j += kM)
+                    units.push_back(WsUnit{off[p] + j, p, (p * nnc + nc) * nkr + kr,
+                                           (int)std::min<long long>(kM, nk[p] - j), 0});
+    DevBuf du(sizeof(WsUnit) * units.size(), st), derr(sizeof(int), st);
+    DevBuf Fp(nparts > 1 ? sizeof(float2) * (size_t)nparts * ntot : 0, st);
+    GF_CUDA(cudaMemcpyAsync(du.p, units.data(), sizeof(WsUnit) * units.size(), cudaMemcpyHostToDevice, st));
+    GF_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), st));
+    WsArgs a;
+    a.B = B.as<uint16_t>();
+    a.units = du.as<WsUnit>();
+    a.nunits = (int)units.size();
     a.u = d_u;
     a.v = d_v;
-    a.F = d_F;
-    a.D1 = D1; a.D2 = D2; a.n1 = n1; a.n2 = n2;
+    a.inv_scale = d_inv;
+    a.F = nparts > 1 ? Fp.as<float2>() : d_F;
+    a.ntot = ntot;
+    a.D1 = D1; a.D2 = D2; a.D1p = D1p; a.D2p = D2p;
+    a.n1 = n1; a.n2 = n2;
     auto lg = [](int n) { int t = 0; while ((1 << t) < n) ++t; return (1 << t) == n ? t : -1; };
     a.log2n1 = lg(n1); a.log2n2 = lg(n2);
-    a.nkc = nkc; a.nnc = nnc; a.npad_last = npad_last;
+    a.nnc = nnc; a.nkr = nkr;
     a.err = derr.as<int>();
-    a.queue = derr.as<int>() + 1;
     // GENFIRE_DEBUG_DFT_WAIT_CYCLES (a positive count of clock cycles) shortens
-    // the main loop's waits so that a test can make one expire and exercise the
+    // the pipeline's waits so that a test can make one expire and exercise the
     // kernel's error path on real work: the drain still waits with the full
     // limit for the copies and MMAs in flight, so the call returns
     // GENFIRE_ERR_TIMEOUT with the context intact.
@@ -572,21 +722,31 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
         const long long v = std::atoll(dbg);
         if (v > 0 && v < kWaitCycles) a.wait_cycles = v;
     }
-    const size_t smem = 2 * (size_t)kStageBytes + 128 + 3 * kM * sizeof(float2);
     const bool pow2 = a.log2n1 >= 0 && a.log2n2 >= 0;
-    const void *kern = pow2 ? (const void *)k_dft_tcgen05<true> : (const void *)k_dft_tcgen05<false>;
-    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = (int)std::min<size_t>(tiles.size(), (size_t)ctx->sm_count);
+    const void *kern = fp16 ? (pow2 ? (const void *)k_dft_tcgen05<true, true> : (const void *)k_dft_tcgen05<true, false>)
+                            : (pow2 ? (const void *)k_dft_tcgen05<false, true> : (const void *)k_dft_tcgen05<false, false>);
+    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsSmem));
+    const int grid = (int)std::min<size_t>(units.size(), (size_t)ctx->sm_count);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (kernel_ms) {
         GF_CUDA(cudaEventCreate(&e0));
         GF_CUDA(cudaEventCreate(&e1));
         GF_CUDA(cudaEventRecord(e0, st));
     }
-    if (pow2) k_dft_tcgen05<true><<<grid, kThreads, smem, st>>>(a);
-    else k_dft_tcgen05<false><<<grid, kThreads, smem, st>>>(a);
+    if (fp16) {
+        if (pow2) k_dft_tcgen05<true, true><<<grid, kWsThreads, kWsSmem, st>>>(a);
+        else k_dft_tcgen05<true, false><<<grid, kWsThreads, kWsSmem, st>>>(a);
+    } else {
+        if (pow2) k_dft_tcgen05<false, true><<<grid, kWsThreads, kWsSmem, st>>>(a);
+        else k_dft_tcgen05<false, false><<<grid, kWsThreads, kWsSmem, st>>>(a);
+    }
     GF_CHECK_LAUNCH();
     if (kernel_ms) GF_CUDA(cudaEventRecord(e1, st));
+    if (nparts > 1) {
+        k_sum_parts<<<(unsigned)std::min<long long>((ntot + 255) / 256, 16LL * ctx->sm_count), 256, 0, st>>>(
+            Fp.as<float2>(), nparts, ntot, d_F);
+        GF_CHECK_LAUNCH();
+    }
     int herr = 0;
     GF_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     GF_CUDA(cudaStreamSynchronize(st));

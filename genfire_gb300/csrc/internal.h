@@ -80,11 +80,13 @@ int fft_grid_size(int Dim2, double ratio);
 void grid_fft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, const double *angles,
               void *d_M, void *d_rec, int64_t *npairs);
 
-// MIXED DFT of all selected points on the tensor cores (grid_mma.cu): F[j]
-// (complex64) for the points of every projection (counts nk, offsets off).
+// Reduced-precision DFT of all selected points on the tensor cores
+// (grid_mma.cu): F[j] (complex64) for the points of every projection (counts
+// nk, offsets off); split-BF16 operands, or split-FP16 operands with
+// per-projection power-of-two scaling when fp16.
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
                  const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
-                 const float *d_v, float2 *d_F, double *kernel_ms = nullptr);
+                 const float *d_v, float2 *d_F, double *kernel_ms, bool fp16);
 
 // Selection of one projection into host arrays (test entry point).
 long long select_one(genfire_ctx *ctx, const genfire_params &p, double phi, double theta, double psi,

@@ -12,7 +12,7 @@
  *               [--iterations 50] [--cutoff 0.7] [--gridding 1|2] [--mode 1|2|3]
  *               [--positivity 0|1] [--support-constraint 0|1]
  *               [--multiple-matches 0|1] [--centro 0|1] [--vector1 x,y,z]
- *               [--vector2 x,y,z] [--vector3 x,y,z] [--precision fp64|mixed]
+ *               [--vector2 x,y,z] [--vector3 x,y,z] [--precision fp64|mixed|fp16_scaled]
  *               [--no-rfactor] [--save-temp L [--save-prefix results/temp_rec]]
  *               [--rfree NBINS [--rfree-percent 0.05] [--seed S]]
  *   (defaults: the class defaults of GENFIRE_Reconstructor.m:30-70)
@@ -203,7 +203,7 @@ static int staged(genfire_ctx *ctx, const genfire_params *p, const void *M, cons
                   const double *projs, const double *angles, int n1, int n2, int save_every, const char *prefix,
                   int nbins, double pct, long long seed, void *rec, double *errK, double **rfree_out)
 {
-    const size_t N = (size_t)n1 * n2 * n1, es = p->precision == GENFIRE_PREC_MIXED ? sizeof(float) : sizeof(double);
+    const size_t N = (size_t)n1 * n2 * n1, es = p->precision != GENFIRE_PREC_FP64 ? sizeof(float) : sizeof(double);
     uint8_t *mask = NULL;
     int64_t *counts = NULL, *ind = NULL, *wcounts = NULL, *wind = NULL;
     if (nbins > 0) {
@@ -314,7 +314,8 @@ int main(int argc, char **argv)
         else if (!strcmp(k, "--vector1") && !vec3(v, p.vector1)) {}
         else if (!strcmp(k, "--vector2") && !vec3(v, p.vector2)) {}
         else if (!strcmp(k, "--vector3") && !vec3(v, p.vector3)) {}
-        else if (!strcmp(k, "--precision")) p.precision = !strcmp(v, "mixed") ? GENFIRE_PREC_MIXED : GENFIRE_PREC_FP64;
+        else if (!strcmp(k, "--precision")) p.precision = !strcmp(v, "mixed") ? GENFIRE_PREC_MIXED
+                                                           : !strcmp(v, "fp16_scaled") ? GENFIRE_PREC_FP16_SCALED : GENFIRE_PREC_FP64;
         else if (!strcmp(k, "--save-temp")) save_every = atoi(v);
         else if (!strcmp(k, "--save-prefix")) save_prefix = v;
         else if (!strcmp(k, "--rfree")) nbins = atoi(v);
@@ -354,7 +355,7 @@ int main(int argc, char **argv)
         return 1;
     }
     if (p.griddingMethod > 2) { fprintf(stderr, "GENFIRE: Unrecognized gridding method.\n"); return 1; }
-    const int mixed = p.precision == GENFIRE_PREC_MIXED;
+    const int mixed = p.precision != GENFIRE_PREC_FP64;
     const size_t es = mixed ? sizeof(float) : sizeof(double);
     uint8_t *support = malloc(nv);
     for (size_t i = 0; i < nv; ++i) support[i] = sp.re ? sp.re[i] != 0 : 1;

@@ -18,7 +18,7 @@ import os
 import numpy as np
 
 from . import _lib
-from ._lib import GenfireError, PREC_FP64, PREC_MIXED
+from ._lib import GenfireError, PREC_FP16_SCALED, PREC_FP64, PREC_MIXED
 
 _PROPS = dict(
     # internal variables (GENFIRE_Reconstructor.m:6-28)
@@ -93,7 +93,9 @@ class GENFIRE_Reconstructor:
             return PREC_FP64
         if self.precision in ("mixed", PREC_MIXED):
             return PREC_MIXED
-        raise GenfireError(_lib.GENFIRE_ERR_ARG, "GENFIRE: precision must be 'fp64' or 'mixed'.")
+        if self.precision in ("fp16_scaled", PREC_FP16_SCALED):
+            return PREC_FP16_SCALED
+        raise GenfireError(_lib.GENFIRE_ERR_ARG, "GENFIRE: precision must be 'fp64', 'mixed' or 'fp16_scaled'.")
 
     def params(self):
         """The genfire_params of the current properties."""
@@ -191,7 +193,7 @@ class GENFIRE_Reconstructor:
             self.fillInFourierGrid()
         if self.griddingMethod == 2:
             self.fillInFourierGrid_DFT()
-        if self._prec() == PREC_MIXED:
+        if self._prec() != PREC_FP64:
             self.measuredK = np.asfortranarray(self.measuredK, dtype=np.complex64)
         self.measuredK_mask = self.measuredK != 0
         self.Vol_ind = _lib.volumn_index(self.measuredK.shape, [self.Dim1, self.Dim2, self.Dim1])

@@ -46,9 +46,17 @@ typedef enum genfire_status {
     GENFIRE_ERR_STATE = 6         /* handle used out of order */
 } genfire_status;
 
+/* Arithmetic of a call.  FP64 is the drop-in (complex128 throughout).  MIXED
+ * and FP16_SCALED iterate in complex64 with FP64 error, weight and phase sums;
+ * they differ only in the gridding DFT's tensor-core operands: split BF16
+ * (hi*hi + hi*lo + lo*hi, ~16 bits per operand) for MIXED, split FP16 (~22
+ * bits per operand, each projection scaled by a power of two so its largest
+ * value sits below 2^14) for FP16_SCALED.  Wherever a call takes a real
+ * volume or grid, FP16_SCALED means float, as MIXED does. */
 typedef enum genfire_precision {
     GENFIRE_PREC_FP64 = 0,
-    GENFIRE_PREC_MIXED = 1
+    GENFIRE_PREC_MIXED = 1,
+    GENFIRE_PREC_FP16_SCALED = 2
 } genfire_precision;
 
 /* The GENFIRE_Reconstructor properties read by the hot path

@@ -51,7 +51,7 @@ def params(G, D1, D2, P, **kw):
         if k in ("vector1", "vector2", "vector3"):
             getattr(p, k)[:] = [float(x) for x in v]
         elif k == "precision":
-            p.precision = G.PREC_MIXED if v == "mixed" else G.PREC_FP64
+            p.precision = {"mixed": G.PREC_MIXED, "fp16": G.PREC_FP16_SCALED}.get(v, G.PREC_FP64)
         else:
             setattr(p, k, v)
     return p

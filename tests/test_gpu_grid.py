@@ -73,11 +73,12 @@ def test_grid_dft_fp64_parity(lib, ctx, oracle, D1, D2, P, os_, cut, centro):
     assert rel(rec, reco) < FP64_TOL
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp16"])
 @pytest.mark.parametrize("D1,D2,P,os_,cut,centro", GRID_CASES[:5])
-def test_grid_dft_mixed_tolerance(lib, ctx, oracle, D1, D2, P, os_, cut, centro):
+def test_grid_dft_mixed_tolerance(lib, ctx, oracle, D1, D2, P, os_, cut, centro, prec):
     projs, angles = _random_case(D1 * 11 + P, D1, D2, P)
     kw = dict(oversamplingRatio=os_, interpolationCutoffDistance=cut, DFT_CentroSymmetricity=centro)
-    M, rec, nk = ctx.grid_dft(params(lib, D1, D2, P, precision="mixed", **kw), projs, angles)
+    M, rec, nk = ctx.grid_dft(params(lib, D1, D2, P, precision=prec, **kw), projs, angles)
     Mo, reco, nko = oracle.grid_dft(oracle.make_params(D1, D2, P, **kw), projs, angles)
     assert M.dtype == np.complex64 and rec.dtype == np.float32
     assert np.array_equal(nk, nko)
@@ -151,16 +152,51 @@ def test_grid_dft_rejects_bad_parameters(lib, ctx, field, value, status):
     assert str(e.value).startswith("GENFIRE:")
 
 
+@pytest.mark.parametrize("prec", ["mixed", "fp16"])
 @pytest.mark.parametrize("D1,D2,P,os_,cut", [(64, 64, 12, 2.0, 0.125), (40, 300, 3, 2.0, 0.3), (100, 72, 4, 2.0, 0.2),
-                                             (128, 128, 3, 2.0, 0.125)])
-def test_grid_dft_mixed_tensor_core_shapes(lib, ctx, oracle, D1, D2, P, os_, cut):
-    """Split-BF16 tensor-core DFT: several 128-point tiles, K (D1) not a multiple of 32,
-    N (D2) above 256 (two accumulator chunks)."""
+                                             (128, 128, 3, 2.0, 0.125), (300, 40, 2, 2.0, 0.3),
+                                             (280, 144, 2, 2.0, 0.2)])
+def test_grid_dft_mixed_tensor_core_shapes(lib, ctx, oracle, D1, D2, P, os_, cut, prec):
+    """Tensor-core DFT (split BF16 and split FP16): several 128-point tiles, K (D1)
+    not a multiple of 32 and above 256 (two resident blocks along K), N (D2) not a
+    multiple of 16 and above 128 (several 128-column blocks), a non-power-of-two
+    grid (FP64 phase reduction)."""
     projs, angles = _random_case(D1 + D2 + P, D1, D2, P)
     kw = dict(oversamplingRatio=os_, interpolationCutoffDistance=cut, vector3=(0, 0, 1))
-    M, rec, nk = ctx.grid_dft(params(lib, D1, D2, P, precision="mixed", **kw), projs, angles)
+    M, rec, nk = ctx.grid_dft(params(lib, D1, D2, P, precision=prec, **kw), projs, angles)
     Mo, reco, nko = oracle.grid_dft(oracle.make_params(D1, D2, P, **kw), projs, angles)
     assert np.array_equal(nk, nko)
     assert np.array_equal(M != 0, Mo != 0)
     assert rel(M, Mo) < MIXED_TOL
     assert rel(rec, reco) < MIXED_TOL
+
+
+def test_fp16_scaled_is_more_accurate_than_bf16(lib, ctx, oracle):
+    """Split FP16 keeps ~22 bits per operand against split BF16's ~16: on the same
+    projections its gridding error is well below the BF16 one (both below 1e-4)."""
+    D, P = 64, 8
+    projs, angles = _random_case(4242, D, D, P)
+    kw = dict(oversamplingRatio=2.0, interpolationCutoffDistance=0.125)
+    Mo, _, _ = oracle.grid_dft(oracle.make_params(D, D, P, **kw), projs, angles, want_rec=False)
+    e = {}
+    for prec in ("mixed", "fp16"):
+        M, _, _ = ctx.grid_dft(params(lib, D, D, P, precision=prec, **kw), projs, angles, want_rec=False)
+        e[prec] = rel(M, Mo)
+    assert e["mixed"] < MIXED_TOL and e["fp16"] < 1e-5
+    assert e["fp16"] < 0.25 * e["mixed"], e
+
+
+@pytest.mark.parametrize("amp", [1e-7, 1e7])
+def test_fp16_scaled_per_projection_scaling(lib, ctx, oracle, amp):
+    """Amplitudes far outside FP16's range (1e-7 would underflow, 1e7 overflow)
+    grid within 1e-5 of the oracle: each projection is scaled by a power of two
+    before the split and the scale is undone exactly."""
+    D, P = 32, 3
+    projs, angles = _random_case(99, D, D, P)
+    projs = np.asfortranarray(projs * amp * np.array([1.0, 3.0, 0.5]))
+    kw = dict(oversamplingRatio=2.0, interpolationCutoffDistance=0.3)
+    M, _, nk = ctx.grid_dft(params(lib, D, D, P, precision="fp16", **kw), projs, angles, want_rec=False)
+    Mo, _, nko = oracle.grid_dft(oracle.make_params(D, D, P, **kw), projs, angles, want_rec=False)
+    assert np.array_equal(nk, nko)
+    assert np.all(np.isfinite(M))
+    assert rel(M, Mo) < 1e-5
