@@ -28,15 +28,20 @@
 //
 // Warp roles in each CTA:
 //   warps 0-3   epilogue: thread = TMEM lane = point; tcgen05.ld of the Re and
-//               Im accumulators, Horner's rule in E_v(1) per 16-column group
-//               times an exact anchor E_v(b_g), partial F stored;
+//               Im accumulators, per 16-column group Horner's rule in E_v(2)
+//               over its even and odd columns at once (packed FP32 pairs),
+//               times an anchor E_v(b_g) (exact every 64 columns), partial F
+//               stored;
 //   warp 4      one thread loads blocks (cp.async.bulk into shared memory,
 //               completing on an mbarrier) and issues tcgen05.mma (M = 128,
 //               N <= 128, K = 16), committing to mbarriers;
 //   warps 5-12  A producers: per 32-wide K chunk, each thread forms 16
-//               consecutive E_u(j, a) of one point from an exact anchor and
-//               FP32 rotations, splits them into hi/lo and stores them in the
-//               K-major layout; three A stages.
+//               consecutive E_u(j, a) of one point as packed FP32 pairs
+//               (real parts of two neighbours in one register pair, imaginary
+//               parts in another) by four independent chains of packed
+//               rotations from an anchor (exact every 4 chunks), splits them
+//               into hi/lo (one packed subtraction per pair) and stores them in
+//               the K-major layout; three A stages.
 // The accumulator (Re and Im, 2 x 128 columns) is double buffered in TMEM, so
 // the epilogue of one unit overlaps the MMAs of the next.
 //
@@ -328,6 +333,57 @@ template <bool F16> __device__ __forceinline__ float half_hi(uint32_t w)
     else return bf16_hi_f(w);
 }
 
+// Packed FP32 pairs (add/sub/mul/fma.rn.f32x2: one instruction for both
+// halves; each half rounds as the scalar operation would).
+typedef unsigned long long f2x_t;
+__device__ __forceinline__ f2x_t pk(float lo, float hi)
+{
+    f2x_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 upk(f2x_t r)
+{
+    float2 a;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+    return a;
+}
+__device__ __forceinline__ f2x_t sub_x2(f2x_t a, f2x_t b)
+{
+    f2x_t r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x_t mul_x2(f2x_t a, f2x_t b)
+{
+    f2x_t r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x_t fma_x2(f2x_t a, f2x_t b, f2x_t c)
+{
+    f2x_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// Two complex values held as (X, Y) = ((re0, re1), (im0, im1)), both rotated
+// by the complex w given as the pairs (w.x, w.x), (w.y, w.y), (-w.y, -w.y).
+__device__ __forceinline__ void rot_x2(f2x_t &X, f2x_t &Y, f2x_t wx, f2x_t wy, f2x_t nwy)
+{
+    const f2x_t x = fma_x2(Y, nwy, mul_x2(X, wx));
+    Y = fma_x2(Y, wx, mul_x2(X, wy));
+    X = x;
+}
+// hi/lo split of a pair: hi = the pair rounded to the 16-bit type (packed),
+// lo = (pair - hi) rounded (packed); the residual is one packed subtraction
+template <bool F16> __device__ __forceinline__ void split_x2(f2x_t v, uint32_t &hi, uint32_t &lo)
+{
+    const float2 f = upk(v);
+    hi = pack2<F16>(f.x, f.y);
+    const float2 r = upk(sub_x2(v, pk(half_lo<F16>(hi), half_hi<F16>(hi))));
+    lo = pack2<F16>(r.x, r.y);
+}
+
 }  // namespace umma
 
 // One unit of work: a tile of up to 128 consecutive selected points of one
@@ -477,38 +533,63 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
             const int nkc = min(kKCB, (a.D1p - kKR * kr) / kKC);
             const bool row_ok = r < un.nj;
             const float uj = row_ok ? a.u[un.j0 + r] : 0.f;
+            // rotations of the row: by 1 (odd elements), 2 (chain step), 4, 8, 12 (chain
+            // starts) and 32 (next chunk); the packed ones as ((x, x), (y, y), (-y, -y))
             const float2 w1 = phase_any<POW2>(1, uj, a.log2n1, inv1);
+            const float2 w4 = phase_any<POW2>(4, uj, a.log2n1, inv1);
+            const float2 w2 = cmulf(w1, w1), w8 = cmulf(w4, w4), w12 = cmulf(w8, w4);
+            const float2 w32 = cmulf(cmulf(w8, w8), cmulf(w8, w8));
+            const f2x_t w2x = pk(w2.x, w2.x), w2y = pk(w2.y, w2.y), w2n = pk(-w2.y, -w2.y);
+            const f2x_t w4x = pk(w4.x, w4.x), w4y = pk(w4.y, w4.y), w4n = pk(-w4.y, -w4.y);
+            const f2x_t w8x = pk(w8.x, w8.x), w8y = pk(w8.y, w8.y), w8n = pk(-w8.y, -w8.y);
+            const f2x_t wcx = pk(w12.x, w12.x), wcy = pk(w12.y, w12.y), wcn = pk(-w12.y, -w12.y);
+            float2 anchor = make_float2(0.f, 0.f);
             for (int kc = 0; kc < nkc; ++kc, ++g) {
                 const int s = (int)(g % kStages);
                 if (g >= (uint32_t)kStages && !ws_wait(&aempty[s], ((g / kStages) - 1) & 1, lim, abort_flag)) {
                     ok = false;
                     break;
                 }
-                // 16 consecutive k of row r: a = amin + kr*256 + kc*32 + 16h + 0..15
-                float2 e = row_ok ? phase_any<POW2>(amin + kKR * kr + kKC * kc + 16 * h, uj, a.log2n1, inv1)
-                                  : make_float2(0.f, 0.f);
+                // 16 consecutive k of row r: a = amin + kr*256 + kc*32 + 16h + 0..15.  The
+                // anchor E_u(a) is exact every 4 chunks and one rotation by 32 from the
+                // previous chunk's otherwise.  The values are held as 8 pairs (2p, 2p+1),
+                // each pair's real parts and imaginary parts packed: pair 0 from the
+                // anchor, pairs 2, 4, 6 rotated from it by 4, 8, 12 and every odd pair
+                // from the one before it by 2 (four independent chains of packed
+                // rotations, at most three rotations from the anchor)
+                if ((kc & 3) == 0)
+                    anchor = row_ok ? phase_any<POW2>(amin + kKR * kr + kKC * kc + 16 * h, uj, a.log2n1, inv1)
+                                    : make_float2(0.f, 0.f);
+                else
+                    anchor = cmulf(anchor, w32);
+                const float2 e1 = cmulf(anchor, w1);
+                f2x_t X[8], Y[8];
+                X[0] = pk(anchor.x, e1.x);
+                Y[0] = pk(anchor.y, e1.y);
+                X[2] = X[0]; Y[2] = Y[0]; rot_x2(X[2], Y[2], w4x, w4y, w4n);
+                X[4] = X[0]; Y[4] = Y[0]; rot_x2(X[4], Y[4], w8x, w8y, w8n);
+                X[6] = X[0]; Y[6] = Y[0]; rot_x2(X[6], Y[6], wcx, wcy, wcn);
+#pragma unroll
+                for (int m = 0; m < 8; m += 2) {
+                    X[m + 1] = X[m];
+                    Y[m + 1] = Y[m];
+                    rot_x2(X[m + 1], Y[m + 1], w2x, w2y, w2n);
+                }
                 uint32_t rh[8], rl[8], ih[8], il[8];
 #pragma unroll
-                for (int t = 0; t < 8; ++t) {
-                    const float2 e0 = e;
-                    e = cmulf(e, w1);
-                    const float2 e1 = e;
-                    if (t < 7) e = cmulf(e, w1);
-                    // hi: both values rounded in one conversion; lo from the exact
-                    // float values of the packed halves
-                    rh[t] = pack2<F16>(e0.x, e1.x);
-                    ih[t] = pack2<F16>(e0.y, e1.y);
-                    rl[t] = pack2<F16>(e0.x - half_lo<F16>(rh[t]), e1.x - half_hi<F16>(rh[t]));
-                    il[t] = pack2<F16>(e0.y - half_lo<F16>(ih[t]), e1.y - half_hi<F16>(ih[t]));
+                for (int m = 0; m < 8; ++m) {
+                    split_x2<F16>(X[m], rh[m], rl[m]);
+                    split_x2<F16>(Y[m], ih[m], il[m]);
                 }
                 uint16_t *As = reinterpret_cast<uint16_t *>(sA + s * kAStage);
 #pragma unroll
-                for (int c = 0; c < 2; ++c) {
-                    const int idx = kmaj_index(r, 16 * h + 8 * c);  // one 16-byte core-matrix row
-                    *reinterpret_cast<uint4 *>(As + 0 * (kABytes / 2) + idx) = make_uint4(rh[4 * c], rh[4 * c + 1], rh[4 * c + 2], rh[4 * c + 3]);
-                    *reinterpret_cast<uint4 *>(As + 1 * (kABytes / 2) + idx) = make_uint4(rl[4 * c], rl[4 * c + 1], rl[4 * c + 2], rl[4 * c + 3]);
-                    *reinterpret_cast<uint4 *>(As + 2 * (kABytes / 2) + idx) = make_uint4(ih[4 * c], ih[4 * c + 1], ih[4 * c + 2], ih[4 * c + 3]);
-                    *reinterpret_cast<uint4 *>(As + 3 * (kABytes / 2) + idx) = make_uint4(il[4 * c], il[4 * c + 1], il[4 * c + 2], il[4 * c + 3]);
+                for (int c8 = 0; c8 < 2; ++c8) {
+                    const int idx = kmaj_index(r, 16 * h + 8 * c8);  // one 16-byte core-matrix row
+                    const int k0 = 4 * c8;
+                    *reinterpret_cast<uint4 *>(As + 0 * (kABytes / 2) + idx) = make_uint4(rh[k0], rh[k0 + 1], rh[k0 + 2], rh[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 1 * (kABytes / 2) + idx) = make_uint4(rl[k0], rl[k0 + 1], rl[k0 + 2], rl[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 2 * (kABytes / 2) + idx) = make_uint4(ih[k0], ih[k0 + 1], ih[k0 + 2], ih[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 3 * (kABytes / 2) + idx) = make_uint4(il[k0], il[k0 + 1], il[k0 + 2], il[k0 + 3]);
                 }
                 fence_proxy_async();  // the stores are visible to the tensor core
                 mbar_arrive(&afull[s]);
@@ -530,11 +611,35 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
             const bool row_ok = row < un.nj;
             const float vj = row_ok ? a.v[un.j0 + row] : 0.f;
             const float2 v1 = phase_any<POW2>(1, vj, a.log2n2, inv2);
+            const float2 v16 = phase_any<POW2>(16, vj, a.log2n2, inv2);
+            const float2 v2 = cmulf(v1, v1);
+            const f2x_t v2x = pk(v2.x, v2.x), v2y = pk(v2.y, v2.y), v2n = pk(-v2.y, -v2.y);
             const uint32_t cre = tmem + lane_base + (uint32_t)(buf * 256), cim = cre + 128;
-            float2 Fsum = make_float2(0.f, 0.f);
-            // F += sum_b Q(j,b) E_v(j,b): per 16-column group, Horner's rule in
-            // w = E_v(1) gives sum_i Q_{16g+i} w^i, times the exact anchor E_v(b_g);
-            // two groups per step (independent chains, one wait for both loads)
+            float2 Fsum = make_float2(0.f, 0.f), an = make_float2(0.f, 0.f);
+            // F += sum_b Q(j,b) E_v(j,b) over 16-column groups: with w = E_v(1), a group's
+            // sum_i Q_i w^i is A(w^2) + w B(w^2), A and B the polynomials of its even and
+            // odd columns, both evaluated by Horner's rule in one packed chain (the pair
+            // (A, B) of real parts and the pair of imaginary parts), then multiplied by
+            // the group's anchor E_v(b_g) (exact every 64 columns, one rotation by 16
+            // from the previous group otherwise); two groups per step (independent
+            // chains, one wait for both loads)
+            auto group = [&](const uint32_t(&re)[16], const uint32_t(&im)[16], float2 anc) {
+                f2x_t H = pk(__uint_as_float(re[14]), __uint_as_float(re[15]));
+                f2x_t G = pk(__uint_as_float(im[14]), __uint_as_float(im[15]));
+#pragma unroll
+                for (int t = 6; t >= 0; --t) {
+                    const f2x_t qr = pk(__uint_as_float(re[2 * t]), __uint_as_float(re[2 * t + 1]));
+                    const f2x_t qi = pk(__uint_as_float(im[2 * t]), __uint_as_float(im[2 * t + 1]));
+                    const f2x_t h2 = fma_x2(H, v2x, fma_x2(G, v2n, qr));
+                    G = fma_x2(H, v2y, fma_x2(G, v2x, qi));
+                    H = h2;
+                }
+                const float2 hr = upk(H), hi = upk(G);  // (A.re, B.re), (A.im, B.im)
+                const float2 sB = cmulf(make_float2(hr.y, hi.y), v1);
+                const float2 p = cmulf(make_float2(hr.x + sB.x, hi.x + sB.y), anc);
+                Fsum.x += p.x;
+                Fsum.y += p.y;
+            };
             for (int c = 0; c < Nc; c += 32) {
                 const bool two = c + 16 < Nc;  // warp-uniform
                 uint32_t re0[16], im0[16], re1[16], im1[16];
@@ -544,30 +649,13 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
                     tmem_ld16(cre + (uint32_t)(c + 16), re1);
                     tmem_ld16(cim + (uint32_t)(c + 16), im1);
                 }
-                const int b0 = bmin + kN * nc + c;
-                const float2 an0 = row_ok ? phase_any<POW2>(b0, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
-                const float2 an1 = (row_ok && two) ? phase_any<POW2>(b0 + 16, vj, a.log2n2, inv2) : make_float2(0.f, 0.f);
+                const float2 an0 = (c & 63) == 0 ? (row_ok ? phase_any<POW2>(bmin + kN * nc + c, vj, a.log2n2, inv2)
+                                                          : make_float2(0.f, 0.f))
+                                                 : cmulf(an, v16);
+                an = cmulf(an0, v16);  // the second group's anchor
                 tmem_wait_ld();
-                float2 h0 = make_float2(__uint_as_float(re0[15]), __uint_as_float(im0[15]));
-#pragma unroll
-                for (int t = 14; t >= 0; --t) {
-                    const float2 m = cmulf(h0, v1);
-                    h0 = make_float2(m.x + __uint_as_float(re0[t]), m.y + __uint_as_float(im0[t]));
-                }
-                const float2 p0 = cmulf(h0, an0);
-                Fsum.x += p0.x;
-                Fsum.y += p0.y;
-                if (two) {
-                    float2 h1 = make_float2(__uint_as_float(re1[15]), __uint_as_float(im1[15]));
-#pragma unroll
-                    for (int t = 14; t >= 0; --t) {
-                        const float2 m = cmulf(h1, v1);
-                        h1 = make_float2(m.x + __uint_as_float(re1[t]), m.y + __uint_as_float(im1[t]));
-                    }
-                    const float2 p1 = cmulf(h1, an1);
-                    Fsum.x += p1.x;
-                    Fsum.y += p1.y;
-                }
+                group(re0, im0, an0);
+                if (two) group(re1, im1, an);
             }
             tc_fence_before();
             mbar_arrive(&tempty[buf]);  // this thread's TMEM reads of the buffer are complete

@@ -1,8 +1,9 @@
-"""A gridding case for profilers (ncu): one MIXED fillInFourierGrid_DFT call of
-the benchmark's shape (90 random-Euler projections of 256 x 256, oversampling
-2, cutoff 0.125) on random projection data.
+"""A gridding case for profilers (ncu): fillInFourierGrid_DFT calls of the
+benchmark's shape (90 random-Euler projections of 256 x 256, oversampling 2,
+cutoff 0.125) on random projection data, in MIXED (split-BF16) or
+FP16_SCALED (split-FP16) precision.
 
-    python -m genfire_gb300.profile_grid_case [calls]
+    python -m genfire_gb300.profile_grid_case [calls] [mixed|fp16]
 """
 import os
 import sys
@@ -17,6 +18,7 @@ def main(argv):
     ge.build()
     import genfire_gb300 as G
     calls = int(argv[0]) if argv else 1
+    prec = argv[1] if len(argv) > 1 else "mixed"
     rng = np.random.default_rng(0)
     D, P = 256, 90
     projs = np.asfortranarray(rng.random((D, D, P)))
@@ -28,7 +30,7 @@ def main(argv):
     p.interpolationCutoffDistance = 0.125
     p.vector3[0] = 0
     p.vector3[2] = 1
-    p.precision = G.PREC_MIXED
+    p.precision = G.PREC_FP16_SCALED if prec == "fp16" else G.PREC_MIXED
     ctx = G.Context(0)
     for _ in range(calls):
         t0 = time.time()
