@@ -19,6 +19,8 @@
 // the next iteration and never observed (the result and the R-factor read
 // the same centred box), so the forward passes skip the zero rows and the
 // inverse passes only produce the box.
+#include <cub/cub.cuh>
+
 #include "fft.cuh"
 #include "fft_reg.cuh"
 #include "fft_r32.cuh"
@@ -586,37 +588,53 @@ __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const u
     return true;
 }
 
+// The table is built per (column, segment of kTabSeg consecutive q3): counts
+// (and |M| sums) per segment, one ordered exclusive scan over (column,
+// segment) with the segment fastest, then each segment writes its entries at
+// its offset, so a column's entries stay in q3 order.  Grid: x = 128
+// consecutive columns (q1 fastest: coalesced reads of M), y = segment.
+constexpr int kTabSeg = 32;
+
 template <typename T>
-__global__ void k_tab_count(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask, TabGeom g,
+__global__ void k_tab_count(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask, TabGeom g, int nseg,
                             int *__restrict__ counts, double *__restrict__ colsum)
 {
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= g.h1 * g.n2) return;
-    const int q1 = col % g.h1, q2 = col / g.h1;
+    const int q1 = col % g.h1, q2 = col / g.h1, seg = blockIdx.y;
+    const int e3 = min(g.n1, (seg + 1) * kTabSeg);
     int cnt = 0;
     double s = 0;
-    for (int q3 = 0; q3 < g.n1; ++q3) {
+    for (int q3 = seg * kTabSeg; q3 < e3; ++q3) {
         TabEntry<T> e;
         double am;
         if (tab_point<T>(M, mask, g, q1, q2, q3, e, am)) { ++cnt; s += am; }
     }
-    counts[col] = cnt;
-    colsum[col] = s;
+    counts[(long long)col * nseg + seg] = cnt;
+    colsum[(long long)col * nseg + seg] = s;
 }
 
 template <typename T>
-__global__ void k_tab_write(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask, TabGeom g,
-                            const int *__restrict__ off, TabEntry<T> *__restrict__ tab)
+__global__ void k_tab_write(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask, TabGeom g, int nseg,
+                            const int *__restrict__ segoff, TabEntry<T> *__restrict__ tab)
 {
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= g.h1 * g.n2) return;
-    const int q1 = col % g.h1, q2 = col / g.h1;
-    int o = off[col];
-    for (int q3 = 0; q3 < g.n1; ++q3) {
+    const int q1 = col % g.h1, q2 = col / g.h1, seg = blockIdx.y;
+    const int e3 = min(g.n1, (seg + 1) * kTabSeg);
+    int o = segoff[(long long)col * nseg + seg];
+    for (int q3 = seg * kTabSeg; q3 < e3; ++q3) {
         TabEntry<T> e;
         double am;
         if (tab_point<T>(M, mask, g, q1, q2, q3, e, am)) tab[o++] = e;
     }
+}
+
+// column offsets of the table (CSR) from the segment offsets
+__global__ void k_tab_coloff(const int *__restrict__ segoff, int ncol, int nseg, int *__restrict__ taboff)
+{
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col <= ncol) taboff[col] = segoff[(long long)col * nseg];
 }
 
 // exclusive scan of n ints (single CTA) and the total in off[n]; also the
@@ -914,19 +932,33 @@ template <typename T> struct ReconT : ReconBase {
         TabGeom g;
         g.n1 = n1; g.n2 = n2; g.h1 = h1; g.W3 = W3; g.m = m;
         for (int k = 0; k < 32; ++k) g.delay[k] = k < m ? delay[k] : 0.0;
-        const int ncol = h1 * n2;
-        DevBuf counts(sizeof(int) * ncol, st), colsum(sizeof(double) * ncol, st), dtot(sizeof(double), st);
+        const int ncol = h1 * n2, nseg = (int)cdiv(n1, kTabSeg);
+        const long long nsc = (long long)ncol * nseg;
+        DevBuf counts(sizeof(int) * nsc, st), colsum(sizeof(double) * nsc, st), dtot(sizeof(double), st);
+        DevBuf segoff(sizeof(int) * (nsc + 1), st);
         taboff.alloc(sizeof(int) * (ncol + 1), st);
-        k_tab_count<T><<<cdiv(ncol, 128), 128, 0, st>>>(M.as<cplx<T>>(), mask.as<uint8_t>(), g, counts.as<int>(), colsum.as<double>());
+        const dim3 tgrid((unsigned)cdiv(ncol, 128), (unsigned)nseg);
+        k_tab_count<T><<<tgrid, 128, 0, st>>>(M.as<cplx<T>>(), mask.as<uint8_t>(), g, nseg, counts.as<int>(), colsum.as<double>());
         GF_CHECK_LAUNCH();
-        k_scan_cols<<<1, 1024, 0, st>>>(counts.as<int>(), colsum.as<double>(), ncol, taboff.as<int>(), dtot.as<double>());
+        {
+            // segment offsets: segoff[0] = 0, segoff[i + 1] = counts[0] + ... + counts[i];
+            // denom = the sum of the segments' |M| sums (device-wide reduction)
+            GF_CUDA(cudaMemsetAsync(segoff.p, 0, sizeof(int), st));
+            size_t tb1 = 0, tb2 = 0;
+            GF_CUDA(cub::DeviceScan::InclusiveSum(nullptr, tb1, counts.as<int>(), segoff.as<int>() + 1, (int)nsc, st));
+            GF_CUDA(cub::DeviceReduce::Sum(nullptr, tb2, colsum.as<double>(), dtot.as<double>(), (int)nsc, st));
+            DevBuf tmp(std::max(tb1, tb2), st);
+            GF_CUDA(cub::DeviceScan::InclusiveSum(tmp.p, tb1, counts.as<int>(), segoff.as<int>() + 1, (int)nsc, st));
+            GF_CUDA(cub::DeviceReduce::Sum(tmp.p, tb2, colsum.as<double>(), dtot.as<double>(), (int)nsc, st));
+        }
+        k_tab_coloff<<<cdiv(ncol + 1, 256), 256, 0, st>>>(segoff.as<int>(), ncol, nseg, taboff.as<int>());
         GF_CHECK_LAUNCH();
         ntab = 0;
         GF_CUDA(cudaMemcpyAsync(&ntab, taboff.as<int>() + ncol, sizeof(int), cudaMemcpyDeviceToHost, st));
         GF_CUDA(cudaMemcpyAsync(&denom, dtot.p, sizeof(double), cudaMemcpyDeviceToHost, st));
         GF_CUDA(cudaStreamSynchronize(st));
         tab.alloc(sizeof(TabEntry<T>) * (size_t)std::max(ntab, 1), st);
-        k_tab_write<T><<<cdiv(ncol, 128), 128, 0, st>>>(M.as<cplx<T>>(), mask.as<uint8_t>(), g, taboff.as<int>(), tab.as<TabEntry<T>>());
+        k_tab_write<T><<<tgrid, 128, 0, st>>>(M.as<cplx<T>>(), mask.as<uint8_t>(), g, nseg, segoff.as<int>(), tab.as<TabEntry<T>>());
         GF_CHECK_LAUNCH();
 
         // object buffers, support

@@ -25,12 +25,6 @@ template <> struct Coord<double> {
         return __dadd_rn(__dadd_rn(__dmul_rn(a, x), __dmul_rn(b, y)), __dmul_rn(c, z));
     }
 };
-template <> struct Coord<float> {
-    static __device__ __forceinline__ float lin(double a, double x, double b, double y, double c, double z)
-    {
-        return (float)fma(c, z, fma(b, y, a * x));
-    }
-};
 
 template <typename T>
 __device__ __forceinline__ T trilinear(const T *__restrict__ V, int n1, int n2, int n3, long long vs1, long long vs2,
@@ -139,13 +133,28 @@ __global__ void __launch_bounds__(kProjThreads)
         const double X = i - c1, Y = j - c2;
         double acc = 0;
         T part_acc = 0;
-        for (int k = 0; k < n3; ++k) {
-            const double Z = k - c3;
-            const T rx = Coord<T>::lin(R[0], X, R[3], Y, R[6], Z);
-            const T ry = Coord<T>::lin(R[1], X, R[4], Y, R[7], Z);
-            const T rz = Coord<T>::lin(R[2], X, R[5], Y, R[8], Z);
-            part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, rx + (T)c1, ry + (T)c2, rz + (T)c3);
-            if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+        if constexpr (sizeof(T) == sizeof(double)) {
+            // FP64: the oracle's operation order, ((R0 X + R3 Y) + R6 Z), each rounded
+            for (int k = 0; k < n3; ++k) {
+                const double Z = k - c3;
+                const T rx = Coord<T>::lin(R[0], X, R[3], Y, R[6], Z);
+                const T ry = Coord<T>::lin(R[1], X, R[4], Y, R[7], Z);
+                const T rz = Coord<T>::lin(R[2], X, R[5], Y, R[8], Z);
+                part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, rx + (T)c1, ry + (T)c2, rz + (T)c3);
+                if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+            }
+        } else {
+            // FP32: the pixel's part R0 X + R3 Y (+ the centre) once in FP64, rounded
+            // to float; per sample one FP32 fma with the third column (this part runs
+            // FP64 at 2 operations per clock per SM, so the loop stays FP32)
+            const float bx = (float)(R[0] * X + R[3] * Y + c1), by = (float)(R[1] * X + R[4] * Y + c2),
+                        bz = (float)(R[2] * X + R[5] * Y + c3);
+            const float r6 = (float)R[6], r7 = (float)R[7], r8 = (float)R[8];
+            for (int k = 0; k < n3; ++k) {
+                const float Z = (float)(k - c3);
+                part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, fmaf(Z, r6, bx), fmaf(Z, r7, by), fmaf(Z, r8, bz));
+                if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+            }
         }
         acc += (double)part_acc;
         if (proj) proj[(long long)p * npix + pix] = (T)acc;
