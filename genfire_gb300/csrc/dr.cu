@@ -533,6 +533,10 @@ void fftn_device(genfire_ctx *ctx, int precision, void *d_data, int n1, int n2, 
 // (E = measuredK ~= 0 & mask, reconstruct.m:99), grouped by column q1 + h1*q2.
 struct TabGeom {
     int n1, n2, h1, W3, m;
+    // delay indices whose test 1 - Q > delay holds at every point: make_Kspace_indices'
+    // coordinates lie in [-1, 1], so Q <= sqrt(3) and 1 - Q > -0.7321 everywhere; a
+    // delay below -0.75 (mode 3's -999, the -10 of modes 1 and 2) needs no Q
+    uint32_t always;
     double delay[32];
 };
 
@@ -550,7 +554,15 @@ __device__ __forceinline__ double kspace_k(int n, int i)
     return (double)(i - r) / (double)r;
 }
 
-template <typename T>
+// |M| of one measured value, summed in FP64 by the caller: complex64 values in
+// FP32 (the iteration's own precision), complex128 in FP64
+__device__ __forceinline__ double abs_val(float2 v) { return (double)sqrtf(fmaf(v.x, v.x, v.y * v.y)); }
+__device__ __forceinline__ double abs_val(double2 v) { return sqrt(v.x * v.x + v.y * v.y); }
+
+// One half-spectrum point q of the constraint table.  MASKS: also the
+// per-delay masks (the counting pass needs only whether q is an entry and the
+// |M| it contributes).
+template <typename T, bool MASKS>
 __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const uint8_t *__restrict__ mask,
                                           const TabGeom &g, int q1, int q2, int q3, TabEntry<T> &e, double &absM)
 {
@@ -570,16 +582,29 @@ __device__ __forceinline__ bool tab_point(const cplx<T> *__restrict__ M, const u
     e.eflags = (inEq ? 1u : 0u) | ((inEm && !mate_stored) ? 2u : 0u);
     // constraintIndicators = 1 - Q (reconstruct.m:36-42, make_Kspace_indices.m)
     auto kv = [](int n, int i) -> double { return kspace_k(n, i); };
+    const uint32_t all = g.m >= 32 ? 0xFFFFFFFFu : ((1u << g.m) - 1u);
     uint32_t cq = 0, cm = 0;
     if (inEq) {
-        const double ci = 1.0 - q_radius(kv(n2, c2), kv(n1, c1), kv(n1, c3));
-        for (int k = 0; k < g.m; ++k) cq |= (ci > g.delay[k]) ? (1u << k) : 0u;
-        absM += sqrt((double)Ma.x * Ma.x + (double)Ma.y * Ma.y);
+        if constexpr (MASKS) {
+            cq = g.always;
+            if (cq != all) {
+                const double ci = 1.0 - q_radius(kv(n2, c2), kv(n1, c1), kv(n1, c3));
+                for (int k = 0; k < g.m; ++k) cq |= (ci > g.delay[k]) ? (1u << k) : 0u;
+            }
+        } else {
+            absM += abs_val(Ma);
+        }
     }
     if (inEm) {
-        const double ci = 1.0 - q_radius(kv(n2, d2), kv(n1, d1), kv(n1, d3));
-        for (int k = 0; k < g.m; ++k) cm |= (ci > g.delay[k]) ? (1u << k) : 0u;
-        if (!mate_stored) absM += sqrt((double)Mb.x * Mb.x + (double)Mb.y * Mb.y);
+        if constexpr (MASKS) {
+            cm = g.always;
+            if (cm != all) {
+                const double ci = 1.0 - q_radius(kv(n2, d2), kv(n1, d1), kv(n1, d3));
+                for (int k = 0; k < g.m; ++k) cm |= (ci > g.delay[k]) ? (1u << k) : 0u;
+            }
+        } else if (!mate_stored) {
+            absM += abs_val(Mb);
+        }
     }
     e.cq = cq;
     e.cmq = cm;
@@ -608,7 +633,7 @@ __global__ void k_tab_count(const cplx<T> *__restrict__ M, const uint8_t *__rest
     for (int q3 = seg * kTabSeg; q3 < e3; ++q3) {
         TabEntry<T> e;
         double am;
-        if (tab_point<T>(M, mask, g, q1, q2, q3, e, am)) { ++cnt; s += am; }
+        if (tab_point<T, false>(M, mask, g, q1, q2, q3, e, am)) { ++cnt; s += am; }
     }
     counts[(long long)col * nseg + seg] = cnt;
     colsum[(long long)col * nseg + seg] = s;
@@ -626,7 +651,7 @@ __global__ void k_tab_write(const cplx<T> *__restrict__ M, const uint8_t *__rest
     for (int q3 = seg * kTabSeg; q3 < e3; ++q3) {
         TabEntry<T> e;
         double am;
-        if (tab_point<T>(M, mask, g, q1, q2, q3, e, am)) tab[o++] = e;
+        if (tab_point<T, true>(M, mask, g, q1, q2, q3, e, am)) tab[o++] = e;
     }
 }
 
@@ -931,7 +956,11 @@ template <typename T> struct ReconT : ReconBase {
         // constraint table
         TabGeom g;
         g.n1 = n1; g.n2 = n2; g.h1 = h1; g.W3 = W3; g.m = m;
-        for (int k = 0; k < 32; ++k) g.delay[k] = k < m ? delay[k] : 0.0;
+        g.always = 0;
+        for (int k = 0; k < 32; ++k) {
+            g.delay[k] = k < m ? delay[k] : 0.0;
+            if (k < m && delay[k] < -0.75) g.always |= 1u << k;
+        }
         const int ncol = h1 * n2, nseg = (int)cdiv(n1, kTabSeg);
         const long long nsc = (long long)ncol * nseg;
         DevBuf counts(sizeof(int) * nsc, st), colsum(sizeof(double) * nsc, st), dtot(sizeof(double), st);

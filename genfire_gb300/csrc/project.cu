@@ -26,13 +26,17 @@ template <> struct Coord<double> {
     }
 };
 
+// floor in the argument's own precision (the float path must not round through FP64)
+__device__ __forceinline__ float floor_t(float x) { return floorf(x); }
+__device__ __forceinline__ double floor_t(double x) { return floor(x); }
+
 template <typename T>
 __device__ __forceinline__ T trilinear(const T *__restrict__ V, int n1, int n2, int n3, long long vs1, long long vs2,
                                        T x, T y, T z)
 {
     if (!(x >= (T)0 && y >= (T)0 && z >= (T)0 && x <= (T)(n1 - 1) && y <= (T)(n2 - 1) && z <= (T)(n3 - 1)))
         return (T)0;
-    int i = (int)floor(x), j = (int)floor(y), k = (int)floor(z);
+    int i = (int)floor_t(x), j = (int)floor_t(y), k = (int)floor_t(z);
     i = min(i, n1 - 2); j = min(j, n2 - 2); k = min(k, n3 - 2);
     i = max(i, 0); j = max(j, 0); k = max(k, 0);
     const T fx = x - (T)i, fy = y - (T)j, fz = z - (T)k;
@@ -61,7 +65,7 @@ __device__ __forceinline__ T trilinear(const T *__restrict__ V, int n1, int n2, 
 // boundary rule folded in.
 template <typename T> __device__ __forceinline__ void keys_taps(T x, int n, int &s, T (&e)[4])
 {
-    int i = (int)floor(x);
+    int i = (int)floor_t(x);
     i = min(max(i, 0), n - 2);
     const T t = x - (T)i, t2 = t * t, t3 = t2 * t;
     const T wm = (T)0.5 * (-t3 + (T)2 * t2 - t);            // index i - 1
@@ -104,6 +108,45 @@ __device__ __forceinline__ T tricubic(const T *__restrict__ V, int n1, int n2, i
         acc += ez[c] * accy;
     }
     return acc;
+}
+
+// Trilinear sample of a float volume with no conversion instructions (this
+// part routes float<->int conversions and rounding to a narrow pipe): for
+// 0 <= x < 2^22, t = x + 1.5*2^23 holds round-to-nearest(x) in its low mantissa
+// bits, one step down where that exceeds x gives floor(x) and its integer; the
+// result equals trilinear<float> bit for bit.
+__device__ __forceinline__ void floor_split(float x, float hi, int &i, float &f)
+{
+    const float t = __fadd_rn(x, 12582912.0f);
+    float fl = __fsub_rn(t, 12582912.0f);
+    int n = __float_as_int(t) - 0x4B400000;
+    if (fl > x) { fl -= 1.0f; n -= 1; }
+    if (fl > hi) { fl = hi; n = __float_as_int(__fadd_rn(hi, 12582912.0f)) - 0x4B400000; }  // clamp to n - 2
+    i = n;
+    f = x - fl;
+}
+__device__ __forceinline__ float trilinear_f(const float *__restrict__ V, float e1, float e2, float e3, float h1,
+                                             float h2, float h3, long long vs1, long long vs2, float x, float y,
+                                             float z)
+{
+    if (!(x >= 0.f && y >= 0.f && z >= 0.f && x <= e1 && y <= e2 && z <= e3)) return 0.f;
+    int i, j, k;
+    float fx, fy, fz;
+    floor_split(x, h1, i, fx);
+    floor_split(y, h2, j, fy);
+    floor_split(z, h3, k, fz);
+    const long long j0o = (long long)j * vs1, j1o = j0o + vs1, k0o = (long long)k * vs2, k1o = k0o + vs2;
+    const float v000 = V[i + j0o + k0o], v100 = V[i + 1 + j0o + k0o];
+    const float v010 = V[i + j1o + k0o], v110 = V[i + 1 + j1o + k0o];
+    const float v001 = V[i + j0o + k1o], v101 = V[i + 1 + j0o + k1o];
+    const float v011 = V[i + j1o + k1o], v111 = V[i + 1 + j1o + k1o];
+    const float c00 = v000 * (1.f - fx) + v100 * fx;
+    const float c10 = v010 * (1.f - fx) + v110 * fx;
+    const float c01 = v001 * (1.f - fx) + v101 * fx;
+    const float c11 = v011 * (1.f - fx) + v111 * fx;
+    const float c0 = c00 * (1.f - fy) + c10 * fy;
+    const float c1 = c01 * (1.f - fy) + c11 * fy;
+    return c0 * (1.f - fz) + c1 * fz;
 }
 
 template <typename T, bool CUBIC>
@@ -150,10 +193,25 @@ __global__ void __launch_bounds__(kProjThreads)
             const float bx = (float)(R[0] * X + R[3] * Y + c1), by = (float)(R[1] * X + R[4] * Y + c2),
                         bz = (float)(R[2] * X + R[5] * Y + c3);
             const float r6 = (float)R[6], r7 = (float)R[7], r8 = (float)R[8];
-            for (int k = 0; k < n3; ++k) {
-                const float Z = (float)(k - c3);
-                part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, fmaf(Z, r6, bx), fmaf(Z, r7, by), fmaf(Z, r8, bz));
-                if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+            float Z = (float)(-c3);  // stepped by exact additions of 1
+            if constexpr (CUBIC) {
+                for (int k = 0; k < n3; ++k, Z += 1.f) {
+                    part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, fmaf(Z, r6, bx), fmaf(Z, r7, by), fmaf(Z, r8, bz));
+                    if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+                }
+            } else if (n1 >= 2 && n2 >= 2 && n3 >= 2) {
+                const float e1 = (float)(n1 - 1), e2 = (float)(n2 - 1), e3 = (float)(n3 - 1);
+                const float h1 = (float)(n1 - 2), h2 = (float)(n2 - 2), h3 = (float)(n3 - 2);
+                for (int k = 0; k < n3; ++k, Z += 1.f) {
+                    part_acc += trilinear_f(reinterpret_cast<const float *>(vol), e1, e2, e3, h1, h2, h3, vs1, vs2,
+                                            fmaf(Z, r6, bx), fmaf(Z, r7, by), fmaf(Z, r8, bz));
+                    if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+                }
+            } else {
+                for (int k = 0; k < n3; ++k, Z += 1.f) {
+                    part_acc += sample<T, CUBIC>(vol, n1, n2, n3, vs1, vs2, fmaf(Z, r6, bx), fmaf(Z, r7, by), fmaf(Z, r8, bz));
+                    if ((k & 15) == 15) { acc += (double)part_acc; part_acc = 0; }
+                }
             }
         }
         acc += (double)part_acc;
