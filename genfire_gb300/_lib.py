@@ -6,6 +6,7 @@ Arrays are passed in MATLAB layout: Fortran-ordered numpy arrays, complex
 data interleaved.
 """
 import ctypes as C
+import weakref
 import os
 
 import numpy as np
@@ -168,13 +169,21 @@ class Context:
             raise GenfireError(st, (msg or b"").decode() or "GENFIRE: could not create a context")
         self._h = h
         self.device = device
+        self._children = weakref.WeakSet()  # live Recon / ReconBatch objects of this context
 
     @property
     def handle(self):
         return self._h
 
+    def _adopt(self, child):
+        self._children.add(child)
+
     def close(self):
         if getattr(self, "_h", None):
+            # batches before their members, then the reconstructions, then the context
+            kids = list(getattr(self, "_children", []))
+            for k in [k for k in kids if isinstance(k, ReconBatch)] + [k for k in kids if not isinstance(k, ReconBatch)]:
+                k.close()
             load().genfire_destroy(self._h)
             self._h = None
 
@@ -436,6 +445,7 @@ class Recon:
                                              ptr(pj), ptr(an), 0, C.byref(h))
         ctx.check(st)
         self._h = h
+        ctx._adopt(self)
         self.done = 0
 
     def iterate(self, count):
@@ -496,7 +506,8 @@ class Recon:
 
     def close(self):
         if getattr(self, "_h", None):
-            load().genfire_recon_destroy(self._h)
+            if self.ctx.handle:  # a closed context has already freed it
+                load().genfire_recon_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -516,6 +527,7 @@ class ReconBatch:
         h = C.c_void_p()
         ctx.check(load().genfire_recon_batch_create(ctx.handle, len(self.members), arr, C.byref(h)))
         self._h = h
+        ctx._adopt(self)
 
     def iterate(self, count):
         self.ctx.check(load().genfire_recon_batch_iterate(self._h, count))
@@ -524,7 +536,8 @@ class ReconBatch:
 
     def close(self):
         if getattr(self, "_h", None):
-            load().genfire_recon_batch_destroy(self._h)
+            if self.ctx.handle:  # a closed context has already freed it
+                load().genfire_recon_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

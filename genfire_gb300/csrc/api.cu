@@ -134,6 +134,14 @@ genfire_status genfire_destroy(genfire_ctx *ctx)
 {
     if (!ctx) return GENFIRE_OK;
     cudaSetDevice(ctx->device);
+    // batches and reconstructions still alive use this context's stream: free them first
+    while (!ctx->batches.empty()) gf::recon_batch_destroy(*ctx->batches.begin());
+    while (!ctx->recons.empty()) {
+        genfire_recon *r = *ctx->recons.begin();
+        ctx->recons.erase(r);
+        delete r->impl;
+        delete r;
+    }
     if (ctx->stream) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);

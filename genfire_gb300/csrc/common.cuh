@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -101,11 +102,15 @@ inline double mround(double x) { return x < 0 ? -std::floor(-x + 0.5) : std::flo
 
 }  // namespace gf
 
-// The context behind genfire_ctx.
+// The context behind genfire_ctx.  It tracks the reconstructions and batches
+// created on it: genfire_destroy frees whatever is still alive before it
+// destroys the stream they use.
 struct genfire_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     int interp = GENFIRE_INTERP_TRILINEAR;  // projector interpolation (genfire_set_projector_interpolation)
     std::string last_error;
+    std::set<genfire_recon *> recons;
+    std::set<genfire_recon_batch *> batches;
 };

@@ -867,6 +867,12 @@ struct ReconBase {
     virtual void iterate(int count) = 0;
     // one iteration as a (not instantiated) graph, for batches
     virtual cudaGraph_t capture_iteration() = 0;
+    // one iteration's launches on st (for a caller's own capture), the kernel
+    // attributes that must be set before a capture, and the grid size (the
+    // batch orders members by it)
+    virtual void enqueue(cudaStream_t st) = 0;
+    virtual void prepare_capture() = 0;
+    virtual long long grid_points() const = 0;
     // iterations still allowed, and the bookkeeping after one batched iteration
     virtual int remaining() const = 0;
     virtual void advance() = 0;
@@ -1200,6 +1206,10 @@ template <typename T> struct ReconT : ReconBase {
         if (bytes) kernel_bytes(bytes);
     }
 
+    void enqueue(cudaStream_t st) override { enqueue_iteration(st); }
+    void prepare_capture() override { ensure_smem_attrs<T>(); }
+    long long grid_points() const override { return (long long)n1 * n2 * n1; }
+
     cudaGraph_t capture_iteration() override
     {
         cudaStream_t st = ctx->stream;
@@ -1402,7 +1412,9 @@ genfire_recon *recon_create(genfire_ctx *ctx, const genfire_params &p, const voi
         try { r->setup(M, mask, support, initial, projs, angles, on_device); } catch (...) { delete r; throw; }
         impl = r;
     }
-    return new genfire_recon{ctx, impl};
+    auto *h = new genfire_recon{ctx, impl};
+    ctx->recons.insert(h);
+    return h;
 }
 
 void recon_iterate(genfire_recon *r, int count) { r->impl->iterate(count); }
@@ -1419,6 +1431,10 @@ void recon_result(genfire_recon *r, void *rec, double *errK, double *errR, doubl
 }
 void recon_destroy(genfire_recon *r)
 {
+    for (genfire_recon_batch *b : r->ctx->batches)
+        for (genfire_recon *m : b->members)
+            if (m == r) fail(GENFIRE_ERR_STATE, "a reconstruction that belongs to a live batch: destroy the batch first.");
+    r->ctx->recons.erase(r);
     delete r->impl;
     delete r;
 }
@@ -1436,27 +1452,60 @@ genfire_recon_batch *recon_batch_create(genfire_ctx *ctx, genfire_recon *const *
         for (int j = 0; j < i; ++j)
             if (members[j] == members[i]) fail(GENFIRE_ERR_ARG, "batch: a reconstruction appears twice.");
     }
-    cudaGraph_t parent = nullptr;
-    GF_CUDA(cudaGraphCreate(&parent, 0));
-    cudaGraphExec_t exec = nullptr;
-    try {
-        for (int i = 0; i < count; ++i) {
-            cudaGraph_t g = members[i]->impl->capture_iteration();
-            cudaGraphNode_t node;
-            const cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, g);  // copies g
-            cudaGraphDestroy(g);
-            GF_CUDA(e);
-        }
-        GF_CUDA(cudaGraphInstantiate(&exec, parent, 0));
-    } catch (...) {
-        cudaGraphDestroy(parent);
-        throw;
-    }
-    cudaGraphDestroy(parent);
+    // One graph of one iteration of every member: a fork/join capture in which
+    // the members' launches go to up to 8 branch streams (largest grids first,
+    // dealt round-robin), so the graph holds parallel chains of kernels and small
+    // members run beside the large ones.
     auto *b = new genfire_recon_batch();
     b->ctx = ctx;
     b->members.assign(members, members + count);
-    b->exec = exec;
+    cudaGraph_t graph = nullptr;
+    try {
+        const int S = std::min(count, 8);
+        for (int k = 0; k < S; ++k) {
+            cudaStream_t s = nullptr;
+            GF_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            b->branches.push_back(s);
+        }
+        for (int k = 0; k < S + 1; ++k) {
+            cudaEvent_t e = nullptr;
+            GF_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            b->events.push_back(e);
+        }
+        std::vector<int> order(count);
+        for (int i = 0; i < count; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+            return members[x]->impl->grid_points() > members[y]->impl->grid_points();
+        });
+        for (int i = 0; i < count; ++i) members[i]->impl->prepare_capture();
+        cudaStream_t st = ctx->stream;
+        GF_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            GF_CUDA(cudaEventRecord(b->events[S], st));  // fork
+            for (int k = 0; k < S; ++k) GF_CUDA(cudaStreamWaitEvent(b->branches[k], b->events[S], 0));
+            for (int n = 0; n < count; ++n) members[order[n]]->impl->enqueue(b->branches[n % S]);
+            for (int k = 0; k < S; ++k) {  // join
+                GF_CUDA(cudaEventRecord(b->events[k], b->branches[k]));
+                GF_CUDA(cudaStreamWaitEvent(st, b->events[k], 0));
+            }
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            graph = nullptr;
+            throw;
+        }
+        GF_CUDA(cudaStreamEndCapture(st, &graph));
+        GF_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
+        cudaGraphDestroy(graph);
+    } catch (...) {
+        if (graph) cudaGraphDestroy(graph);
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        for (auto s : b->branches) cudaStreamDestroy(s);
+        for (auto e : b->events) cudaEventDestroy(e);
+        delete b;
+        throw;
+    }
+    ctx->batches.insert(b);
     return b;
 }
 
@@ -1476,8 +1525,11 @@ void recon_batch_iterate(genfire_recon_batch *b, int count)
 
 void recon_batch_destroy(genfire_recon_batch *b)
 {
-    if (b->exec) cudaGraphExecDestroy(b->exec);
     cudaStreamSynchronize(b->ctx->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    for (auto s : b->branches) cudaStreamDestroy(s);
+    for (auto e : b->events) cudaEventDestroy(e);
+    b->ctx->batches.erase(b);
     delete b;
 }
 

@@ -19,6 +19,8 @@ struct genfire_recon_batch {
     genfire_ctx *ctx;
     std::vector<genfire_recon *> members;
     cudaGraphExec_t exec = nullptr;
+    std::vector<cudaStream_t> branches;  // the capture's branch streams (kept for the graph's lifetime)
+    std::vector<cudaEvent_t> events;     // its fork and join events
 };
 
 namespace gf {

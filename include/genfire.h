@@ -110,6 +110,8 @@ genfire_status genfire_grid_size(const genfire_params *p, int32_t *n1, int32_t *
 /* ---- context ----------------------------------------------------------- */
 
 genfire_status genfire_create(int32_t device, genfire_ctx **out);
+/* Frees the context and, first, every reconstruction and batch still alive on
+ * it (their handles become invalid). */
 genfire_status genfire_destroy(genfire_ctx *ctx);
 const char *genfire_last_error(const genfire_ctx *ctx);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
@@ -210,6 +212,8 @@ genfire_status genfire_recon_iterate(genfire_recon *r, int32_t count);
 genfire_status genfire_recon_result(genfire_recon *r, void *reconstruction, double *errK,
                                     double *errR, double *Rarr, double *Rarr2,
                                     int32_t on_device);
+/* GENFIRE_ERR_STATE (nothing freed) while r is a member of a live batch:
+ * destroy the batch first. */
 genfire_status genfire_recon_destroy(genfire_recon *r);
 
 /* Batches of independent reconstructions (problems of different sizes,

@@ -76,3 +76,26 @@ def test_batch_refuses_overrun_and_foreign_members(lib, ctx):
     for r in (r1, r2, r3):
         r.close()
     other.close()
+
+
+def test_handle_lifetimes(lib, ctx):
+    """A member of a live batch cannot be destroyed (GENFIRE_ERR_STATE, nothing
+    freed), and genfire_destroy frees the reconstructions and batches still
+    alive on the context before its stream: their Python objects may be
+    collected afterwards without touching freed memory."""
+    r, _, _, _ = _make(lib, ctx, *PROBLEMS[0], seed=70)
+    b = lib.ReconBatch(ctx, [r])
+    assert lib._lib.load().genfire_recon_destroy(r._h) == 6
+    r.iterate(1)  # still usable
+    b.close()
+    r.close()
+    c2 = lib.Context(0)
+    r2, _, _, _ = _make(lib, c2, *PROBLEMS[3], seed=71)
+    b2 = lib.ReconBatch(c2, [r2])
+    b2.iterate(1)
+    c2._children.discard(r2)  # left to genfire_destroy
+    c2._children.discard(b2)
+    c2.close()
+    b2.close()  # no C call: the context freed them
+    r2.close()
+    assert r2._h is None and b2._h is None
