@@ -274,15 +274,15 @@ def run_ours(args, ws, rank, local, pg):
         K_e2e = K if args.quick else max(K, w["iters"])
         t_short, d2h = e2e_call(K)
         t_e2e, d2h = e2e_call(K_e2e) if K_e2e != K else (t_short, d2h)
-        # split: a plain copy of the same host bytes, then the staged calls
+        # split, from the staged calls: the setup alone (the same inputs already in
+        # device memory), then from host buffers (copies + setup), the iterations
+        # and the readback
+        pe = params_for(G, w, G.PREC_MIXED, K_e2e)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        tmpM = torch.from_numpy(hM.reshape(-1, order="F")).to("cuda")
-        tmpS = torch.from_numpy(hS.reshape(-1, order="F")).to("cuda")
-        torch.cuda.synchronize()
-        t_h2d = time.perf_counter() - t0
-        del tmpM, tmpS
-        pe = params_for(G, w, G.PREC_MIXED, K_e2e)
+        r = ctx.recon(pe, d_M32.data_ptr(), support=d_sup.data_ptr(), on_device=True)
+        t_setup = time.perf_counter() - t0
+        r.close()
         t0 = time.perf_counter()
         r = ctx.recon(pe, hM, support=hS)
         t_create = time.perf_counter() - t0
@@ -298,7 +298,7 @@ def run_ours(args, ws, rank, local, pg):
                "d2h_bytes_per_step": d2h / K_e2e,
                "at_timed_steps": {"steps": K, "value": K / t_short, "h2d_bytes_per_step": h2d / K,
                                   "d2h_bytes_per_step": d2h / K},
-               "split_ms": {"h2d_copy": t_h2d * 1e3, "setup": (t_create - t_h2d) * 1e3, "iterate": t_iter * 1e3,
+               "split_ms": {"h2d_copy": (t_create - t_setup) * 1e3, "setup": t_setup * 1e3, "iterate": t_iter * 1e3,
                             "d2h_result": t_d2h * 1e3, "staged_total": (t_create + t_iter + t_d2h) * 1e3},
                "note": "one genfire_reconstruct call of the configuration's %d iterations from host buffers: "
                        "measuredK (%d^3 complex64, pageable) and the support copied in, reconstruction and errK "
