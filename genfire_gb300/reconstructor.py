@@ -47,7 +47,8 @@ _PROPS = dict(
     DFT_CentroSymmetricity=1, DFT_doGPU=0, Vol_ind=None,
     # temp saves (:67-70)
     save_temp=0, save_loopLength=50, saveFilename="./results/temp_rec",
-    # this build: arithmetic of the GPU path, 'fp64' (drop-in) or 'mixed'
+    # this build: arithmetic of the GPU path, 'fp64' (drop-in), 'mixed' (split-BF16 gridding,
+    # complex64 iteration) or 'fp16_scaled' (split-FP16 gridding, complex64 iteration)
     precision="fp64", device=0,
 )
 

@@ -200,3 +200,26 @@ def test_fp16_scaled_per_projection_scaling(lib, ctx, oracle, amp):
     assert np.array_equal(nk, nko)
     assert np.all(np.isfinite(M))
     assert rel(M, Mo) < 1e-5
+
+
+def test_reconstructor_fp16_scaled_dft_gridding(lib, ctx, oracle, tmp_path):
+    """GENFIRE_Reconstructor(precision='fp16_scaled', griddingMethod=2): readFiles ->
+    CheckPrepareData -> runGridding (split-FP16 tensor-core DFT, single measuredK)
+    -> reconstruct, against the oracle's FP64 chain."""
+    from genfire_gb300 import GENFIRE_Reconstructor
+    D, P, iters = 32, 10, 20
+    projs, angles = _random_case(515, D, D, P)
+    np.save(tmp_path / "pj.npy", projs)
+    np.save(tmp_path / "ang.npy", angles)
+    G = GENFIRE_Reconstructor(filename_Projections=str(tmp_path / "pj.npy"), filename_Angles=str(tmp_path / "ang.npy"),
+                              oversamplingRatio=2, interpolationCutoffDistance=0.3, numIterations=iters,
+                              griddingMethod=2, constraintEnforcementMode=3, precision="fp16_scaled")
+    G = G.readFiles().CheckPrepareData().runGridding().reconstruct()
+    assert G.measuredK.dtype == np.complex64
+    prm = oracle.make_params(D, D, P, oversamplingRatio=2, interpolationCutoffDistance=0.3, numIterations=iters,
+                             constraintEnforcementMode=3)
+    Mo, _, _ = oracle.grid_dft(prm, projs, angles, want_rec=False)
+    assert rel(G.measuredK, Mo) < 1e-5
+    reco, errKo = oracle.reconstruct(prm, Mo)[:2]
+    assert rel(G.reconstruction, reco) < 1e-4
+    assert np.abs(np.asarray(G.errK).ravel() - np.asarray(errKo).ravel()).max() < 1e-4

@@ -41,20 +41,20 @@ def harness(lib):
     return build.HARNESS
 
 
-@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "fp16"])
 def test_harness_dft_equals_python(lib, ctx, harness, tmp_path, prec):
     pj, ang, fp, fa = _inputs(ctx, tmp_path)
     D, P, N = pj.shape[0], pj.shape[2], 12
     out = str(tmp_path / "res.mat")
     _run(harness, ["--projections", fp, "--angles", fa, "--results", out, "--gridding", "2", "--oversampling", "2",
                    "--cutoff", "0.3", "--iterations", str(N), "--mode", "3", "--vector3", "0,0,1",
-                   "--precision", prec])
+                   "--precision", {"fp16": "fp16_scaled"}.get(prec, prec)])
     res = scipy_io.loadmat(out)
     p = params(lib, D, D, P, oversamplingRatio=2.0, interpolationCutoffDistance=0.3, numIterations=N,
                constraintEnforcementMode=3, vector3=(0, 0, 1), precision=prec)
     M, _, _ = ctx.grid_dft(p, pj, ang)
     rec, errK, _, _, _ = ctx.reconstruct(p, M, support=np.ones((D, D, D), bool))
-    assert res["final_Rec"].dtype == (np.float32 if prec == "mixed" else np.float64)
+    assert res["final_Rec"].dtype == (np.float64 if prec == "fp64" else np.float32)
     assert np.array_equal(res["final_Rec"], rec)
     assert np.array_equal(res["final_errK"].ravel(), errK)
     assert res["final_Kfactor"].item() == errK.min()
