@@ -20,6 +20,7 @@
 // the same centred box), so the forward passes skip the zero rows and the
 // inverse passes only produce the box.
 #include <cub/cub.cuh>
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled_v12000
 
 #include "fft.cuh"
 #include "fft_reg.cuh"
@@ -122,9 +123,12 @@ template <typename T, int N> static void set_reg_attrs()
 // register-resident engine with one column per thread, or with two adjacent
 // float columns per thread (unit column stride and 16-byte aligned column
 // pairs: even strides, aligned bases; tiles start at even columns), the
-// mixed-radix engine, and the radix-32 engines for 512 and 1024 complex64
-// points (fft_r32.cuh: 32 x 16 and 32 x 32, one exchange per transform).
-enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3, kColR32 = 4 };
+// mixed-radix engine, the radix-32 engines for 512 and 1024 complex64 points
+// (fft_r32.cuh: 32 x 16 and 32 x 32, one exchange per transform), and for the
+// fused 512-point pass the persistent radix-32 pass fed by TMA tensor copies
+// (measured 6 % slower than variant 4 on the 512^3 iteration; an autotuner
+// candidate).
+enum ColVariant { kColAuto = -1, kColGeneric = 0, kColReg1 = 1, kColReg2 = 2, kColMix = 3, kColR32 = 4, kColR32Tma = 5 };
 
 // GENFIRE_COL_VARIANT=<v> forces variant v wherever it is valid (tuning and
 // tests); unset, the built-in choice or the autotuner decides
@@ -214,6 +218,12 @@ template <typename T> static void ensure_smem_attrs()
     set_reg_attrs<T, 256>();
     set_reg_attrs<T, 512>();
     set_reg_attrs<T, 1024>();
+    if constexpr (sizeof(T) == 4) {
+        // the persistent fused pass: 53 KB per CTA, 4 CTAs per SM
+        GF_CUDA(cudaFuncSetAttribute((const void *)k_col_r32_tma<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)r32_tma_smem<512>()));
+        GF_CUDA(cudaFuncSetAttribute((const void *)k_col_r32_tma<512>, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
 
     done.insert(dev);
 }
@@ -230,9 +240,59 @@ static int r32_width(int n)
     }
 }
 
-template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v)
+// The driver's tensor-map encoder (cuTensorMapEncodeTiled), through the
+// runtime's entry-point query so the library needs no link to libcuda.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+static int device_sm_count()
+{
+    static std::mutex mu;
+    static std::map<int, int> cache;
+    int dev = 0;
+    GF_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    GF_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    cache[dev] = n;
+    return n;
+}
+
+// The persistent, TMA-fed fused 512-point pass (k_col_r32_tma): complex64, the
+// centred half of a box in and out, unit column stride, tiles inside the rows
+// of the input, strides that a tensor map can describe.
+template <typename T> static bool tma_capable(const ColPassArgs<T> &a, int other)
+{
+    if constexpr (sizeof(T) != 4) {
+        return false;
+    } else {
+        constexpr int N = 512, W = R32<N>::W;
+        if (a.pl.n != N || !(a.mode & 1) || !(a.mode & 2) || a.col_stride != 1 || a.W != W) return false;
+        if (!(a.in_cnt == N / 2 && a.in_c == N / 4 && a.out_cnt == N / 2 && a.out_c == N / 4)) return false;
+        if (((uintptr_t)a.in & 15u) != 0 || a.in_other <= 0 || a.in_dim % a.in_other != 0) return false;
+        if ((a.in_other * 8) % 16 != 0 || (a.in_dim * 8) % 16 != 0) return false;
+        if ((long long)cdiv(a.ncols, W) * W > a.in_other || other > a.in_dim / a.in_other) return false;
+        return span_ok(a) && tensor_map_encoder() != nullptr;
+    }
+}
+
+template <typename T> static bool col_variant_ok(const ColPassArgs<T> &a, int v, int other = 1)
 {
     if (v == kColGeneric) return true;
+    if (v == kColR32Tma) return tma_capable(a, other);
     if (v == kColR32)
         return sizeof(T) == 4 && r32_width(a.pl.n) > 0 && span_ok(a) && (!(a.mode & 4) || a.W == r32_width(a.pl.n));
     if (v == kColMix) return span_ok(a) && mix_capable<T>(a.pl.n);
@@ -274,6 +334,27 @@ template <typename T, int N> static void col_r32(const ColPassArgs<T> &a, int ot
     else if (zout) k_col_r32<T, N, false, true><<<grid, G::THREADS, sm, st>>>(a);
     else k_col_r32<T, N, false, false><<<grid, G::THREADS, sm, st>>>(a);
 }
+// Launch of k_col_r32_tma: the input as a float tensor {2 in_other, in_dim /
+// in_other, in_cnt} (strides in_other and in_dim complex values), boxes of
+// {2 W, 1, N/2}; a persistent grid of 4 CTAs per SM.
+static void col_r32_tma(const ColPassArgs<float> &a, int other, cudaStream_t st)
+{
+    constexpr int N = 512;
+    using G = R32<N>;
+    CUtensorMap map;
+    const cuuint64_t dims[3] = {(cuuint64_t)(2 * a.in_other), (cuuint64_t)(a.in_dim / a.in_other), (cuuint64_t)a.in_cnt};
+    const cuuint64_t strides[2] = {(cuuint64_t)(a.in_other * 8), (cuuint64_t)(a.in_dim * 8)};
+    const cuuint32_t box[3] = {2 * G::W, 1, N / 2};
+    const cuuint32_t es[3] = {1, 1, 1};
+    const CUresult r = tensor_map_encoder()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<cplx<float> *>(a.in), dims,
+                                            strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) fail(GENFIRE_ERR_CUDA, "tensor map of the fused column pass could not be encoded.");
+    const int tiles_x = (int)cdiv(a.ncols, G::W), ntiles = tiles_x * other;
+    const int grid = std::min(ntiles, 4 * device_sm_count());
+    k_col_r32_tma<N><<<grid, G::THREADS, r32_tma_smem<N>(), st>>>(a, map, tiles_x, ntiles);
+}
+
 template <typename T, int N> static void rows_r32(const RowPassArgs<T> &a, bool forward, cudaStream_t st)
 {
     using G = R32<N>;
@@ -293,9 +374,11 @@ template <typename T> static void launch_colpass(ColPassArgs<T> a, int other, cu
 {
     a.P = a.W + 1;
     const int forced = forced_col_variant();
-    if (forced != kColAuto && col_variant_ok(a, forced)) variant = forced;
-    if (variant == kColAuto || !col_variant_ok(a, variant)) variant = default_col_variant(a);
-    if (variant == kColR32) {
+    if (forced != kColAuto && col_variant_ok(a, forced, other)) variant = forced;
+    if (variant == kColAuto || !col_variant_ok(a, variant, other)) variant = default_col_variant(a);
+    if (variant == kColR32Tma) {
+        if constexpr (sizeof(T) == 4) col_r32_tma(a, other, st);
+    } else if (variant == kColR32) {
         if constexpr (sizeof(T) == 4) {
             switch (a.pl.n) {
             case 128: col_r32<T, 128>(a, other, st); break;
@@ -329,7 +412,7 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     ensure_smem_attrs<T>();
     {
         const int f = forced_col_variant();
-        if (f != kColAuto && col_variant_ok(a, f)) return f;
+        if (f != kColAuto && col_variant_ok(a, f, other)) return f;
     }
     int dev = 0;
     GF_CUDA(cudaGetDevice(&dev));
@@ -347,8 +430,8 @@ template <typename T> static int autotune_colpass(ColPassArgs<T> a, int other, c
     // (keeps the choice stable against timing noise)
     int best = kColAuto;
     float best_ms = 0, default_ms = -1;
-    for (int v : {kColGeneric, kColReg1, kColReg2, kColMix, kColR32}) {
-        if (!col_variant_ok(a, v)) continue;
+    for (int v : {kColGeneric, kColReg1, kColReg2, kColMix, kColR32, kColR32Tma}) {
+        if (!col_variant_ok(a, v, other)) continue;
         launch_colpass<T>(a, other, st, v);
         GF_CUDA(cudaEventRecord(e0, st));
         for (int r = 0; r < 3; ++r) launch_colpass<T>(a, other, st, v);
@@ -871,6 +954,7 @@ struct ReconBase {
     // attributes that must be set before a capture, and the grid size (the
     // batch orders members by it)
     virtual void enqueue(cudaStream_t st) = 0;
+    virtual void check_device_error() = 0;
     virtual void prepare_capture() = 0;
     virtual long long grid_points() const = 0;
     // iterations still allowed, and the bookkeeping after one batched iteration
@@ -891,6 +975,7 @@ template <typename T> struct ReconT : ReconBase {
     const cplx<T> *tw1, *tw2;
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
     DevBuf rtab, rtaboff, rcap, rvals, rshoff, rhist;  // Rfree monitor
+    DevBuf errf;  // set by a pass whose bounded device-side wait expired
     int m = 0, nparts = 0, tiles1 = 0, ntab = 0, nshells = 0;
     long long nrfree = 0;
     double denom = 0;
@@ -1031,6 +1116,8 @@ template <typename T> struct ReconT : ReconBase {
         partial.alloc(sizeof(double) * nparts, st);
         hist.alloc(sizeof(double) * std::max(Nit, 1), st);
         GF_CUDA(cudaMemsetAsync(hist.p, 0, hist.bytes, st));
+        errf.alloc(sizeof(int), st);
+        GF_CUDA(cudaMemsetAsync(errf.p, 0, sizeof(int), st));
         Ctl c0;
         std::memset(&c0, 0, sizeof(c0));
         c0.m = m; c0.xbest = -1; c0.bestErr = 1e30;
@@ -1077,6 +1164,7 @@ template <typename T> struct ReconT : ReconBase {
         b.out = Y2.as<cplx<T>>(); b.out_dim = (long long)ld1 * n2; b.out_other = ld1; b.out_cnt = B3; b.out_c = B3 / 2;
         b.mode = 1 | 2 | 4;
         b.tab_off = taboff.as<int>(); b.tab = tab.as<TabEntry<T>>(); b.h1 = h1; b.partial = partial.as<double>();
+        b.err = errf.as<int>();
         b.cidx = &c->cidx;
         if (nshells > 0) {
             b.rtab_off = rtaboff.as<int>();
@@ -1364,6 +1452,15 @@ template <typename T> struct ReconT : ReconBase {
             if (p.monitor_R == 1 && it_done % p.monitorR_loopLength == 0) monitor();
         }
         GF_CUDA(cudaStreamSynchronize(st));
+        check_device_error();
+    }
+
+    void check_device_error() override
+    {
+        int e = 0;
+        GF_CUDA(cudaMemcpyAsync(&e, errf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        GF_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (e) fail(GENFIRE_ERR_TIMEOUT, "iteration: a bounded wait of the fused column pass expired.");
     }
 
     void result(void *rec, double *errK, double *eR, double *RA, double *RA2, bool on_device) override
@@ -1521,6 +1618,7 @@ void recon_batch_iterate(genfire_recon_batch *b, int count)
         for (genfire_recon *r : b->members) r->impl->advance();
     }
     GF_CUDA(cudaStreamSynchronize(st));
+    for (genfire_recon *r : b->members) r->impl->check_device_error();
 }
 
 void recon_batch_destroy(genfire_recon_batch *b)

@@ -445,6 +445,8 @@ template <typename T> struct ColPassArgs {
     const int *rtab_off;
     const uint2 *rtab;
     cplx<T> *rcap;
+    // set to 1 by a pass whose bounded device-side wait expired (NULL: none)
+    int *err;
 };
 
 // Copy of the withheld (Rfree) points of one tile of F3, read before the

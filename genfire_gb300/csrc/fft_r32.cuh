@@ -22,6 +22,8 @@
 
 #include "fft_reg.cuh"
 
+#include <cuda.h>  // CUtensorMap (the type only; the map is encoded by the host)
+
 namespace gf {
 
 template <int N> struct R32 {
@@ -210,6 +212,66 @@ constexpr int r32_col_min_blocks(int n) { return n == 512 ? 5 : n == 1024 ? 4 : 
 // with it, so they do without.
 constexpr int r32_prefetch_ahead(int n, bool fused) { return (n == 512 && !fused) ? 380 : 0; }
 
+// The transforms, the table phase and the stores of one tile (tile, other)
+// of a column pass whose input is already in x (slot m holds element t + P m);
+// tiles_x is the number of tiles along the columns (the index of the tile's
+// errK partial).  Shared by the one-tile-per-CTA pass and the persistent one.
+template <typename T, int N, bool ZIN, bool ZOUT>
+__device__ __forceinline__ void col_r32_tile(const ColPassArgs<T> &a, cplx<T> *s, cplx<T> (&x)[32], int tile, int other,
+                                             int tiles_x)
+{
+    using G = R32<N>;
+    constexpr int P = G::P, W = G::W;
+    using Lay = typename G::Lay;
+    const int c = threadIdx.x % W, t = threadIdx.x / W;
+    const int col = tile * W + c;
+    const bool cv = col < a.ncols;
+    const cplx<T> *twp = a.tw;
+    ErrAcc<T> err = 0;
+    bool fwd_layout = false;  // slots in the output order of a transform
+    if (a.mode & 1) {
+        r32_fft<T, N, false, ZIN>(x, s, c, t, twp, false);
+        fwd_layout = true;
+    }
+    if (a.mode & 2) {
+        if (a.mode & 1) {
+            // back to slot m = element t + P m, through the natural-order tile
+            // (where the Fourier constraint is applied)
+            __syncthreads();
+#pragma unroll
+            for (int sl = 0; sl < 32; ++sl) s[Lay::idx(t + P * G::out_m(sl), c)] = x[sl];
+            __syncthreads();
+            if (a.mode & 4) {
+                if (a.rtab) {
+                    capture_rfree<T>(s, a, tile, W, other, [](int q3, int cl) { return Lay::idx(q3, cl); });
+                    __syncthreads();
+                }
+                err = apply_table<T, Lay>(s, a, tile, W, other);
+                block_partial(err, a.partial + (long long)other * tiles_x + tile);
+                __syncthreads();
+            }
+#pragma unroll
+            for (int m = 0; m < 32; ++m) x[m] = s[Lay::idx(t + P * m, c)];
+        }
+        r32_fft<T, N, true>(x, s, c, t, twp, (a.mode & 1) != 0);
+        fwd_layout = true;
+    }
+    if (!fwd_layout || !cv) return;
+    cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
+    const unsigned odim = (unsigned)a.out_dim;
+#pragma unroll
+    for (int sl = 0; sl < 32; ++sl) {
+        if constexpr (ZOUT) {
+            if (G::keep(sl))
+                out[(unsigned)(t + G::half_off(G::out_m(sl))) * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
+            continue;
+        }
+        int e = t + P * G::out_m(sl) + a.out_c;
+        if (e >= N) e -= N;
+        if (e < a.out_cnt) out[(unsigned)e * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
+    }
+}
+
 // Column pass (the contract of k_colpass) for n = N.  ZIN: the input is the
 // centred half of a box (in_cnt N/2, in_c N/4) and the pass starts with a
 // forward transform; ZOUT: only the centred half is written (out_cnt N/2,
@@ -260,49 +322,105 @@ __global__ void __launch_bounds__(R32<N>::THREADS, r32_col_min_blocks(N)) k_col_
             x[m] = (cv && e < a.in_cnt) ? in[(unsigned)e * idim] : mk((T)0, (T)0);
         }
     }
-    ErrAcc<T> err = 0;
-    bool fwd_layout = false;  // slots in the output order of a transform
-    if (a.mode & 1) {
-        r32_fft<T, N, false, ZIN>(x, s, c, t, twp, false);
-        fwd_layout = true;
+    col_r32_tile<T, N, ZIN, ZOUT>(a, s, x, tile, other, gridDim.x);
+}
+
+// Persistent fused 512-point complex64 pass (F3 at 512 points): CTAs loop over
+// the tiles (tile, other) = (item % tiles_x, item / tiles_x), item += gridDim.x,
+// and each tile's input (the centred half of the box: N/2 rows x W columns,
+// 16 KB) comes into a shared-memory stage by a TMA tensor copy issued one tile
+// ahead, while the CTA transforms the current one.  tmap describes the input
+// as floats: {2 x in_other, in_dim / in_other, in_cnt} with the box
+// {2 W, 1, N/2} (x = 2 W tile, 64-byte aligned).  The wait for a copy is bounded
+// (clock64); on expiry the CTA stops at a reducing barrier, sets *a.err, waits
+// (full limit) for the copy in flight and returns.
+namespace r32tma {
+constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool wait(uint64_t *bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    while (!try_wait(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+__device__ __forceinline__ void load_tile(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            saddr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(0), "r"(saddr(bar))
+        : "memory");
+}
+}  // namespace r32tma
+
+template <int N> constexpr size_t r32_tma_stage_offset() { return (R32<N>::template smem<float>() + 127) / 128 * 128; }
+template <int N> constexpr uint32_t r32_tma_stage_bytes() { return (uint32_t)(N / 2 * R32<N>::W * sizeof(float2)); }
+template <int N> constexpr size_t r32_tma_smem() { return r32_tma_stage_offset<N>() + r32_tma_stage_bytes<N>() + 16; }
+
+template <int N>
+__global__ void __launch_bounds__(R32<N>::THREADS, 4)
+    k_col_r32_tma(ColPassArgs<float> a, const __grid_constant__ CUtensorMap tmap, int tiles_x, int ntiles)
+{
+    using G = R32<N>;
+    constexpr int W = G::W;
+    constexpr uint32_t kBytes = r32_tma_stage_bytes<N>();
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    cplx<float> *s = reinterpret_cast<cplx<float> *>(smem_raw);
+    cplx<float> *stage = reinterpret_cast<cplx<float> *>(smem_raw + r32_tma_stage_offset<N>());  // [N/2 rows][W]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw + r32_tma_stage_offset<N>() + kBytes);
+    const int c = threadIdx.x % W, t = threadIdx.x / W;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(r32tma::saddr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (a.mode & 2) {
-        if (a.mode & 1) {
-            // back to slot m = element t + P m, through the natural-order tile
-            // (where the Fourier constraint is applied)
-            __syncthreads();
-#pragma unroll
-            for (int sl = 0; sl < 32; ++sl) s[Lay::idx(t + P * G::out_m(sl), c)] = x[sl];
-            __syncthreads();
-            if (a.mode & 4) {
-                if (a.rtab) {
-                    capture_rfree<T>(s, a, tile, W, other, [](int q3, int cl) { return Lay::idx(q3, cl); });
-                    __syncthreads();
-                }
-                err = apply_table<T, Lay>(s, a, tile, W, other);
-                block_partial(err, a.partial + (long long)other * gridDim.x + tile);
-                __syncthreads();
-            }
-#pragma unroll
-            for (int m = 0; m < 32; ++m) x[m] = s[Lay::idx(t + P * m, c)];
+    __syncthreads();
+    int item = blockIdx.x;
+    if (threadIdx.x == 0 && item < ntiles)
+        r32tma::load_tile(stage, &tmap, 2 * W * (item % tiles_x), item / tiles_x, bar, kBytes);
+    bool pending = item < ntiles;  // a copy is in flight (uniform)
+    uint32_t phase = 0;
+    bool ok = true;
+    for (; item < ntiles; item += gridDim.x) {
+        const bool got = r32tma::wait(bar, phase);
+        if (__syncthreads_or(!got)) {
+            ok = false;
+            break;
         }
-        r32_fft<T, N, true>(x, s, c, t, twp, (a.mode & 1) != 0);
-        fwd_layout = true;
-    }
-    if (!fwd_layout || !cv) return;
-    cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
-    const unsigned odim = (unsigned)a.out_dim;
+        pending = false;
+        phase ^= 1;
+        cplx<float> x[32];
 #pragma unroll
-    for (int sl = 0; sl < 32; ++sl) {
-        if constexpr (ZOUT) {
-            if (G::keep(sl))
-                out[(unsigned)(t + G::half_off(G::out_m(sl))) * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
-            continue;
+        for (int m = 0; m < 32; ++m) {
+            if (m >= 8 && m < 24) x[m] = mk(0.f, 0.f);
+            else x[m] = stage[(t + G::half_off(m)) * W + c];
         }
-        int e = t + P * G::out_m(sl) + a.out_c;
-        if (e >= N) e -= N;
-        if (e < a.out_cnt) out[(unsigned)e * odim] = mk(x[sl].x * a.scale, x[sl].y * a.scale);
+        // generic-proxy reads of the stage before the next tensor copy (async proxy)
+        // overwrites it; after the barrier the stage and the exchange buffer are free
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        const int next = item + gridDim.x;
+        if (next < ntiles) {
+            if (threadIdx.x == 0) r32tma::load_tile(stage, &tmap, 2 * W * (next % tiles_x), next / tiles_x, bar, kBytes);
+            pending = true;
+        }
+        col_r32_tile<float, N, true, true>(a, s, x, item % tiles_x, item / tiles_x, tiles_x);
     }
+    if (!ok && threadIdx.x == 0 && a.err) atomicExch(a.err, 1);
+    if (pending && threadIdx.x == 0) r32tma::wait(bar, phase);  // the copy in flight lands before the CTA exits
 }
 
 // Row passes (the contracts of k_rows_r2c / k_rows_c2r) for n = N: W pairs of
