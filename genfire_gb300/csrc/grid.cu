@@ -666,9 +666,22 @@ static unsigned grid_for(genfire_ctx *ctx, long long n, int threads)
 // ===========================================================================
 struct Selection {
     DevBuf ind, dist, u, v;
+    DevBuf doff;  // off on the device (P + 1 entries)
     std::vector<long long> nk, off;
     long long total = 0;
 };
+
+// off[0] = 0, off[p + 1] = off[p] + nk[p] (one thread: P is small)
+__global__ void k_sel_offsets(const long long *__restrict__ nk, int P, long long *__restrict__ off)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long s = 0;
+    off[0] = 0;
+    for (int p = 0; p < P; ++p) {
+        s += nk[p];
+        off[p + 1] = s;
+    }
+}
 
 static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, int n1, int n2,
                           const std::vector<ProjGeom> &geo, Selection &sel)
@@ -692,6 +705,9 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     GF_CHECK_LAUNCH();
     k_sel_scan<<<P, 1024, 0, st>>>(counts.as<int>(), sp.nchunks, totals.as<long long>());
     GF_CHECK_LAUNCH();
+    sel.doff.alloc(sizeof(long long) * (P + 1), st);
+    k_sel_offsets<<<1, 32, 0, st>>>(totals.as<long long>(), P, sel.doff.as<long long>());
+    GF_CHECK_LAUNCH();
     sel.nk.assign(P, 0);
     GF_CUDA(cudaMemcpyAsync(sel.nk.data(), totals.p, sizeof(long long) * P, cudaMemcpyDeviceToHost, st));
     GF_CUDA(cudaStreamSynchronize(st));
@@ -703,13 +719,12 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     sel.dist.alloc(nt * sizeof(float), st);
     sel.u.alloc(nt * sizeof(float), st);
     sel.v.alloc(nt * sizeof(float), st);
-    DevBuf doff(sizeof(long long) * P, st);
-    GF_CUDA(cudaMemcpyAsync(doff.p, sel.off.data(), sizeof(long long) * P, cudaMemcpyHostToDevice, st));
-    k_sel_write<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), doff.as<long long>(),
+    // (the offsets come from the device copy: no host-to-device copy, whose
+    // pageable source would synchronise the stream)
+    k_sel_write<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), sel.doff.as<long long>(),
                                               rowcnt.as<uint16_t>(), sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
                                               sel.v.as<float>());
     GF_CHECK_LAUNCH();
-    GF_CUDA(cudaStreamSynchronize(st));  // keeps the host-side staging buffers alive until the copies ran
 }
 
 // CUDA events on the context stream between the stages of a gridding call
@@ -729,6 +744,7 @@ struct StageEvents {
     {
         if (!ev.empty()) GF_CUDA(cudaEventRecord(ev[i], st));
     }
+    cudaEvent_t event(int i) const { return ev.empty() ? nullptr : ev[i]; }
     double ms(int a, int b)
     {
         float t = 0;
@@ -758,10 +774,12 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
 
     DevBuf F(sizeof(cplx<T>) * (size_t)std::max<long long>(sel.total, 1), st);
     double dft_kernel_ms = 0;
+    DevBuf dft_err(sizeof(int), st);  // set by the tensor-core DFT when a bounded wait expired
+    GF_CUDA(cudaMemsetAsync(dft_err.p, 0, sizeof(int), st));
     if (sizeof(T) == sizeof(float)) {
         // MIXED / FP16_SCALED: split-BF16 / split-FP16 tensor-core DFT (grid_mma.cu)
-        dft_tcgen05(ctx, d_proj, D1, D2, n1, n2, P, sel.nk, sel.off, sel.u.as<float>(), sel.v.as<float>(),
-                    reinterpret_cast<float2 *>(F.p), stage_ms ? &dft_kernel_ms : nullptr,
+        dft_tcgen05(ctx, d_proj, D1, D2, n1, n2, P, sel.nk, sel.doff.as<long long>(), sel.u.as<float>(),
+                    sel.v.as<float>(), reinterpret_cast<float2 *>(F.p), dft_err.as<int>(), se.event(6), se.event(7),
                     p.precision == GENFIRE_PREC_FP16_SCALED);
     } else {
         // FP64: kDftJ consecutive points of one projection per CTA
@@ -779,8 +797,6 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
                                                                    reinterpret_cast<double2 *>(F.p));
             GF_CHECK_LAUNCH();
             se.mark(7, st);
-            GF_CUDA(cudaStreamSynchronize(st));
-            if (stage_ms) dft_kernel_ms = se.ms(6, 7);
         }
     }
     se.mark(2, st);
@@ -821,8 +837,12 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
     se.mark(4, st);
     if (d_rec) rec_ifft(ctx, p.precision, d_M, n1, n2, D1, D2, d_rec);
     se.mark(5, st);
+    int herr = 0;
+    GF_CUDA(cudaMemcpyAsync(&herr, dft_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     GF_CUDA(cudaStreamSynchronize(st));
+    if (herr) fail(GENFIRE_ERR_TIMEOUT, "tensor-core gridding: a bounded wait for the tensor core or a bulk copy expired.");
     if (stage_ms) {
+        dft_kernel_ms = sel.total > 0 ? se.ms(6, 7) : 0.0;
         stage_ms[0] = se.ms(0, 1);  // selection
         stage_ms[1] = se.ms(1, 2);  // DFT stage (operand preparation and the DFT kernel)
         stage_ms[2] = dft_kernel_ms;  // the DFT kernel alone

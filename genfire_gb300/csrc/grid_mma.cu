@@ -57,6 +57,9 @@
 #include <cuda_fp16.h>
 
 #include <cstdlib>
+#include <mutex>
+#include <set>
+#include <utility>
 
 namespace gf {
 
@@ -742,10 +745,68 @@ __global__ void k_sum_parts(const float2 *__restrict__ Fp, int nparts, long long
     }
 }
 
-// Host: F (float2, one per selected point) for all projections.
+// uoff[p] = units of the projections before p (uoff[P] = all units), from the
+// points' offsets: a projection with nk points has ceil(nk / 128) tiles per
+// block and nnc * nkr blocks.  One thread: P is small.
+__global__ void k_unit_offsets(const long long *__restrict__ off, int P, int per_tile, long long *__restrict__ uoff)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    long long s = 0;
+    uoff[0] = 0;
+    for (int p = 0; p < P; ++p) {
+        s += (off[p + 1] - off[p] + umma::kM - 1) / umma::kM * per_tile;
+        uoff[p + 1] = s;
+    }
+}
+
+// The unit list, ordered by projection, block (nc, kr) and tile: unit u belongs
+// to the last projection p with uoff[p] <= u (a projection without points has
+// uoff[p] = uoff[p + 1] and is skipped by that rule).
+__global__ void __launch_bounds__(256) k_make_units(const long long *__restrict__ off,
+                                                    const long long *__restrict__ uoff, int P, int nnc, int nkr,
+                                                    long long nunits, WsUnit *__restrict__ units)
+{
+    using namespace umma;
+    const long long u = blockIdx.x * 256LL + threadIdx.x;
+    if (u >= nunits) return;
+    int lo = 0, hi = P - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (uoff[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    const int p = lo;
+    const long long nk = off[p + 1] - off[p];
+    const long long tiles = (nk + kM - 1) / kM, local = u - uoff[p];
+    const long long t = local % tiles, rest = local / tiles;
+    const int kr = (int)(rest % nkr), nc = (int)(rest / nkr);
+    units[u] = WsUnit{off[p] + t * kM, p, (p * nnc + nc) * nkr + kr, (int)min((long long)kM, nk - t * kM), 0};
+}
+
+__global__ void k_fill_f32(float *__restrict__ x, int n, float v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v;
+}
+
+// The DFT kernels' dynamic shared memory is raised once per device and kernel.
+static void ws_smem_attr(int device, const void *kern)
+{
+    static std::mutex m;
+    static std::set<std::pair<int, const void *>> done;
+    std::lock_guard<std::mutex> g(m);
+    if (done.count({device, kern})) return;
+    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)umma::kWsSmem));
+    done.insert({device, kern});
+}
+
+// Host: F (float2, one per selected point) for all projections.  Everything is
+// enqueued on the context stream without a host synchronisation: the unit list
+// and the scales are made on the device, and the error flag is the caller's to
+// read once it synchronises.
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
-                 const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
-                 const float *d_v, float2 *d_F, double *kernel_ms, bool fp16)
+                 const std::vector<long long> &nk, const long long *d_off, const float *d_u, const float *d_v,
+                 float2 *d_F, int *d_err, cudaEvent_t ev_begin, cudaEvent_t ev_end, bool fp16)
 {
     using namespace umma;
     cudaStream_t st = ctx->stream;
@@ -753,42 +814,39 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     const int nnc = (D2p + kN - 1) / kN, nkr = (D1p + kKR - 1) / kKR;
     const int nparts = nnc * nkr;
     const int nblk = P * nnc * nkr;
-    long long ntot = 0;
-    for (int p = 0; p < P; ++p) ntot += nk[p];
+    long long ntot = 0, nunits = 0;
+    for (int p = 0; p < P; ++p) {
+        ntot += nk[p];
+        nunits += (nk[p] + kM - 1) / kM * nparts;
+    }
     if (ntot == 0) return;
+    if (nunits > INT32_MAX) fail(GENFIRE_ERR_ARG, "tensor-core gridding: too many selected points.");
 
     DevBuf B((size_t)nblk * kBBytes, st), scl(2 * sizeof(float) * P, st);
     float *d_scale = scl.as<float>(), *d_inv = d_scale + P;
     if (fp16) {
         k_proj_scale<<<P, 256, 0, st>>>(d_proj, (long long)D1 * D2, d_scale, d_inv);
-        GF_CHECK_LAUNCH();
     } else {
-        std::vector<float> ones(2 * (size_t)P, 1.f);
-        GF_CUDA(cudaMemcpyAsync(d_scale, ones.data(), sizeof(float) * ones.size(), cudaMemcpyHostToDevice, st));
-        GF_CUDA(cudaStreamSynchronize(st));  // the staging vector goes out of scope below
+        k_fill_f32<<<(2 * P + 255) / 256, 256, 0, st>>>(d_scale, 2 * P, 1.f);
     }
+    GF_CHECK_LAUNCH();
     if (fp16)
         k_split_projections<true><<<dim3((unsigned)nblk, kKCB), 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, B.as<uint16_t>());
     else
         k_split_projections<false><<<dim3((unsigned)nblk, kKCB), 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, B.as<uint16_t>());
     GF_CHECK_LAUNCH();
 
-    // units ordered by projection, block, tile
-    std::vector<WsUnit> units;
-    for (int p = 0; p < P; ++p)
-        for (int nc = 0; nc < nnc; ++nc)
-            for (int kr = 0; kr < nkr; ++kr)
-                for (long long j = 0; j < nk[p]; j += kM)
-                    units.push_back(WsUnit{off[p] + j, p, (p * nnc + nc) * nkr + kr,
-                                           (int)std::min<long long>(kM, nk[p] - j), 0});
-    DevBuf du(sizeof(WsUnit) * units.size(), st), derr(sizeof(int), st);
+    DevBuf du(sizeof(WsUnit) * (size_t)nunits, st), duoff(sizeof(long long) * (P + 1), st);
+    k_unit_offsets<<<1, 32, 0, st>>>(d_off, P, nparts, duoff.as<long long>());
+    GF_CHECK_LAUNCH();
+    k_make_units<<<(unsigned)((nunits + 255) / 256), 256, 0, st>>>(d_off, duoff.as<long long>(), P, nnc, nkr, nunits,
+                                                                   du.as<WsUnit>());
+    GF_CHECK_LAUNCH();
     DevBuf Fp(nparts > 1 ? sizeof(float2) * (size_t)nparts * ntot : 0, st);
-    GF_CUDA(cudaMemcpyAsync(du.p, units.data(), sizeof(WsUnit) * units.size(), cudaMemcpyHostToDevice, st));
-    GF_CUDA(cudaMemsetAsync(derr.p, 0, sizeof(int), st));
     WsArgs a;
     a.B = B.as<uint16_t>();
     a.units = du.as<WsUnit>();
-    a.nunits = (int)units.size();
+    a.nunits = (int)nunits;
     a.u = d_u;
     a.v = d_v;
     a.inv_scale = d_inv;
@@ -799,7 +857,7 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     auto lg = [](int n) { int t = 0; while ((1 << t) < n) ++t; return (1 << t) == n ? t : -1; };
     a.log2n1 = lg(n1); a.log2n2 = lg(n2);
     a.nnc = nnc; a.nkr = nkr;
-    a.err = derr.as<int>();
+    a.err = d_err;
     // GENFIRE_DEBUG_DFT_WAIT_CYCLES (a positive count of clock cycles) shortens
     // the pipeline's waits so that a test can make one expire and exercise the
     // kernel's error path on real work: the drain still waits with the full
@@ -813,14 +871,9 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     const bool pow2 = a.log2n1 >= 0 && a.log2n2 >= 0;
     const void *kern = fp16 ? (pow2 ? (const void *)k_dft_tcgen05<true, true> : (const void *)k_dft_tcgen05<true, false>)
                             : (pow2 ? (const void *)k_dft_tcgen05<false, true> : (const void *)k_dft_tcgen05<false, false>);
-    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWsSmem));
-    const int grid = (int)std::min<size_t>(units.size(), (size_t)ctx->sm_count);
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (kernel_ms) {
-        GF_CUDA(cudaEventCreate(&e0));
-        GF_CUDA(cudaEventCreate(&e1));
-        GF_CUDA(cudaEventRecord(e0, st));
-    }
+    ws_smem_attr(ctx->device, kern);
+    const int grid = (int)std::min<long long>(nunits, (long long)ctx->sm_count);
+    if (ev_begin) GF_CUDA(cudaEventRecord(ev_begin, st));
     if (fp16) {
         if (pow2) k_dft_tcgen05<true, true><<<grid, kWsThreads, kWsSmem, st>>>(a);
         else k_dft_tcgen05<true, false><<<grid, kWsThreads, kWsSmem, st>>>(a);
@@ -829,23 +882,13 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
         else k_dft_tcgen05<false, false><<<grid, kWsThreads, kWsSmem, st>>>(a);
     }
     GF_CHECK_LAUNCH();
-    if (kernel_ms) GF_CUDA(cudaEventRecord(e1, st));
+    if (ev_end) GF_CUDA(cudaEventRecord(ev_end, st));
     if (nparts > 1) {
         k_sum_parts<<<(unsigned)std::min<long long>((ntot + 255) / 256, 16LL * ctx->sm_count), 256, 0, st>>>(
             Fp.as<float2>(), nparts, ntot, d_F);
         GF_CHECK_LAUNCH();
     }
-    int herr = 0;
-    GF_CUDA(cudaMemcpyAsync(&herr, derr.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-    GF_CUDA(cudaStreamSynchronize(st));
-    if (kernel_ms) {
-        float t = 0;
-        cudaEventElapsedTime(&t, e0, e1);
-        *kernel_ms = t;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-    }
-    if (herr) fail(GENFIRE_ERR_TIMEOUT, "tensor-core gridding: a bounded wait for the tensor core or a bulk copy expired.");
+    // the buffers are released stream-ordered (cudaFreeAsync) after the kernels
 }
 
 }  // namespace gf

@@ -86,9 +86,13 @@ void grid_fft(genfire_ctx *ctx, const genfire_params &p, const double *d_proj, c
 // (grid_mma.cu): F[j] (complex64) for the points of every projection (counts
 // nk, offsets off); split-BF16 operands, or split-FP16 operands with
 // per-projection power-of-two scaling when fp16.
+// d_off: the points' offsets per projection on the device (P + 1 entries);
+// d_err (device, zeroed by the caller) is set when a bounded wait expired.  The
+// call does not synchronise; ev_begin / ev_end (may be null) are recorded
+// around the DFT kernel.
 void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1, int n2, int P,
-                 const std::vector<long long> &nk, const std::vector<long long> &off, const float *d_u,
-                 const float *d_v, float2 *d_F, double *kernel_ms, bool fp16);
+                 const std::vector<long long> &nk, const long long *d_off, const float *d_u, const float *d_v,
+                 float2 *d_F, int *d_err, cudaEvent_t ev_begin, cudaEvent_t ev_end, bool fp16);
 
 // Selection of one projection into host arrays (test entry point).
 long long select_one(genfire_ctx *ctx, const genfire_params &p, double phi, double theta, double psi,
