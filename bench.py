@@ -230,6 +230,17 @@ def run_ours(args, ws, rank, local, pg):
     _, t_grid_fp16 = time_call(lambda: ctx.grid_dft_device(ph, d_proj.data_ptr(), angles, d_M32.data_ptr()))
     grid_err_fp16 = float(torch.linalg.vector_norm(d_M32.to(torch.complex128) - d_M64) / torch.linalg.vector_norm(d_M64))
     stages_fp16 = ctx.grid_profile(ph, d_proj.data_ptr(), angles, d_M32.data_ptr())
+    # the second tensor-core form (GENFIRE_DFT_KERNEL=n256: Re and Im stacked in
+    # rows, N = 256 MMAs, 64-point tiles), opt-in, split BF16
+    os.environ["GENFIRE_DFT_KERNEL"] = "n256"
+    try:
+        ctx.grid_dft_device(pm, d_proj.data_ptr(), angles, d_M32.data_ptr())             # warm-up
+        _, t_grid_n256 = time_call(lambda: ctx.grid_dft_device(pm, d_proj.data_ptr(), angles, d_M32.data_ptr()))
+        grid_err_n256 = float(torch.linalg.vector_norm(d_M32.to(torch.complex128) - d_M64)
+                              / torch.linalg.vector_norm(d_M64))
+        stages_n256 = ctx.grid_profile(pm, d_proj.data_ptr(), angles, d_M32.data_ptr())
+    finally:
+        del os.environ["GENFIRE_DFT_KERNEL"]
     ctx.grid_dft_device(pm, d_proj.data_ptr(), angles, d_M32.data_ptr())   # the MIXED grid for the loop below
 
     # ---- DR loop, mixed (value): warm-up, then exactly K timed iterations
@@ -390,6 +401,10 @@ def run_ours(args, ws, rank, local, pg):
                                  "roofline": gridding_roofline(flops, nk, D, stages_fp16),
                                  "note": "split-FP16 operands (3 products), each projection scaled by a power of "
                                          "two; the same kernel as split BF16"},
+        "gridding_n256_form": {"gridding_ms": t_grid_n256 * 1e3, "rel_l2_vs_fp64": grid_err_n256,
+                               "stages_ms": stages_n256,
+                               "roofline": gridding_roofline(flops, nk, D, stages_n256, tile=64),
+                               "note": "opt-in second tensor-core form (GENFIRE_DFT_KERNEL=n256), split BF16"},
         "projector_roofline": projector,
         "fp64": {"dr_iters_per_s": K64 / t_dr64, "gridding_gflops": flops / t_grid_fp64 / 1e9,
                  "gridding_ms": t_grid_fp64 * 1e3, "timed_iterations": K64},
@@ -414,11 +429,12 @@ def run_ours(args, ws, rank, local, pg):
     return res
 
 
-def gridding_roofline(flops, nk, D, stages):
+def gridding_roofline(flops, nk, D, stages, tile=128):
     """The tcgen05 DFT kernel against the measured bf16 tensor peak: useful
     flops (sum_p 4 Nk D1 D2 + 8 Nk D2) and executed tensor flops (the 3 split
-    products over 128-point tiles and 256-column chunks) per its CUDA-event
-    duration."""
+    products, Re and Im, over tiles of `tile` points: 128 for the default
+    form, 64 for the N = 256 form whose 128 MMA rows are the Re and Im of 64
+    points) per its CUDA-event duration."""
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
             pk = json.load(f)
@@ -426,15 +442,15 @@ def gridding_roofline(flops, nk, D, stages):
     except Exception:
         peak, kind = 1900.0, "fallback"
     ms = stages["dft_kernel"]
-    tiles = float(np.sum(np.ceil(np.asarray(nk, dtype=np.float64) / 128.0)))
+    tiles = float(np.sum(np.ceil(np.asarray(nk, dtype=np.float64) / tile)))
     k_pad, n_pad = -(-D // 32) * 32, -(-D // 16) * 16
-    executed = tiles * 128.0 * k_pad * n_pad * 2.0 * 6
+    executed = tiles * tile * k_pad * n_pad * 2.0 * 6
     ach = flops / (ms * 1e-3) / 1e12
-    return {"kernel": "k_dft_tcgen05", "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+    return {"kernel": "k_dft_tcgen05" if tile == 128 else "k_dft_tcgen05_w", "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
             "frac": ach / peak, "peak_kind": "of " + kind, "ms_per_launch": ms,
             "executed_tflops": executed / (ms * 1e-3) / 1e12, "executed_frac": executed / (ms * 1e-3) / 1e12 / peak,
             "note": "achieved counts the useful DFT flops; executed counts the split products the tensor cores "
-                    "run (3 per complex-real product, Re and Im: 6 MMAs of 2 flops per MAC, on 128-point tiles "
+                    "run (3 per complex-real product, Re and Im: 6 products of 2 flops per MAC, on whole tiles "
                     "and the projection padded to 32 rows and 16 columns)"}
 
 

@@ -57,6 +57,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <set>
 #include <utility>
@@ -676,6 +677,304 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
     if (warp == kMmaWarp) tmem_dealloc(tmem, 512);
 }
 
+// ---------------------------------------------------------------------------
+// Second form (opt-in): Re and Im stacked in the MMA rows, N = 256.
+//
+// A tile holds 64 points; its 128 MMA rows are, in each 32-lane quadrant q,
+// lanes 0-15 the real parts and lanes 16-31 the imaginary parts of E_u for
+// points 16 q .. 16 q + 15.  The accumulator of a unit is then one 128-lane x
+// N matrix (row = Re or Im of a point), so N = 256 fits twice in the 512
+// tensor-memory columns and stays double buffered.  B blocks are 256 columns
+// x 128 rows (four K chunks of [hi | lo][256 x 32], 128 KB), and per K = 16
+// step three MMAs (M = 128, N = 256): A_hi B_hi, A_hi B_lo, A_lo B_hi.  An MMA
+// reads 4 KB of A and 8 KB of B for 2 x 128 x 128 x 16 MACs: 6 KB per
+// 128 x 128 x 16, against 8 KB in the first form, whose MMAs the shared-memory
+// pipe bounds.  A stages: 128 rows x 32 K, hi and lo (16 KB), six of them.
+//
+// Roles: two epilogue groups of four warps (group g drains accumulator buffer
+// g), one MMA warp, eight producers.  Producers: warp 9 + i writes quadrant
+// (9 + i) % 4 and half (i / 4) of each 32-wide K chunk; of the two lanes of a
+// point, the Re lane forms E_u for the first 8 K of its half and the Im lane
+// for the last 8, and they swap the other component's words with one shuffle
+// per packed pair, so each lane holds its row's 16 K (two 16-byte stores per
+// part).  Epilogue: each lane contracts its row (real Q) with E_v by the
+// packed Horner scheme; F = S_re + i S_im, the Im lane's sum taken by a
+// shuffle.  Waits are bounded as in the first form; their outcome is made
+// warp-uniform before the warp-collective tensor-memory loads.
+namespace umma {
+constexpr int kWPoints = 64;                          // points per tile
+constexpr int kWN = 256;                              // columns of one block (N of the MMAs)
+constexpr int kWKR = 128;                             // rows of one block (its K range)
+constexpr int kWKCB = kWKR / kKC;                     // K chunks per block (4)
+constexpr int kWAArr = 128 * kKC;                     // elements of one A array of a chunk (8 KB)
+constexpr int kWAStage = 2 * kWAArr * 2;              // hi + lo (16 KB)
+constexpr int kWStages = 6;
+constexpr int kWBArr = kWN * kKC;                     // elements of one B array of a chunk
+constexpr int kWBChunk = 2 * kWBArr * 2;              // hi + lo of one chunk (32 KB)
+constexpr int kWBBytes = kWKCB * kWBChunk;            // one block (128 KB)
+constexpr int kWNBars = 2 * kWStages + 4 + 3;         // afull, aempty, tfull x2, tempty x2, bfull, bdone, drain
+// roles: warps 0-7 epilogue (warp w drains accumulator buffer w / 4, quadrant
+// w % 4), warp 8 MMA issue and block copies, warps 9-16 A producers
+constexpr int kWMmaWarp = 8, kWProdWarp0 = 9;  // warps 0 .. kWMmaWarp - 1 are the epilogue
+constexpr int kWThreads = 32 * (kWProdWarp0 + kProdWarps);  // 544
+constexpr size_t kWSmem = (size_t)kWBBytes + (size_t)kWStages * kWAStage + 8 * kWNBars + 16;
+static_assert(kWSmem <= 227 * 1024, "shared memory of the N = 256 form");
+
+// a bounded wait whose outcome every lane of the warp shares
+__device__ __forceinline__ bool ws_wait_warp(uint64_t *bar, uint32_t parity, long long limit, volatile int *abort_flag)
+{
+    const bool got = ws_wait(bar, parity, limit, abort_flag);
+    return __all_sync(0xffffffffu, got);
+}
+}  // namespace umma
+
+template <bool F16, bool POW2>
+__global__ void __launch_bounds__(umma::kWThreads, 1) k_dft_tcgen05_w(WsArgs a)
+{
+    using namespace umma;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *sB = smem_raw;
+    unsigned char *sA = smem_raw + kWBBytes;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + kWBBytes + kWStages * kWAStage);
+    uint64_t *afull = bars, *aempty = bars + kWStages, *tfull = bars + 2 * kWStages, *tempty = tfull + 2;
+    uint64_t *bfull = tempty + 2, *bdone = bfull + 1, *drain = bdone + 1;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + kWNBars);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int s = 0; s < kWStages; ++s) {
+            mbar_init(&afull[s], kProdThreads);
+            mbar_init(&aempty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&tfull[b], 1);
+            mbar_init(&tempty[b], 32 * 4);  // the four warps of buffer b's epilogue group
+        }
+        mbar_init(bfull, 1);
+        mbar_init(bdone, 1);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == kWMmaWarp) {
+        tmem_alloc(tmem_slot, 512);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int u0 = (int)((long long)a.nunits * blockIdx.x / gridDim.x);
+    const int u1 = (int)((long long)a.nunits * (blockIdx.x + 1) / gridDim.x);
+    const long long lim = a.wait_cycles;
+    const int nparts = a.nnc * a.nkr;
+
+    if (warp == kWMmaWarp) {
+        if (lane == 0) {
+            // ---------------------------------------------------------------- MMA issue
+            int cur_blk = -1;
+            uint32_t g = 0, nbf = 0, nbd = 0;
+            bool b_pending = false;
+            for (int i = u0; i < u1; ++i) {
+                const WsUnit un = a.units[i];
+                const int part = un.blk % nparts, nc = part / a.nkr, kr = part % a.nkr;
+                const int Nc = min(kWN, a.D2p - kWN * nc);
+                const int nkc = min(kWKCB, (a.D1p - kWKR * kr) / kKC);
+                bool ok = true;
+                if (un.blk != cur_blk) {
+                    if (cur_blk >= 0) {
+                        mma_commit(bdone);
+                        if (!ws_wait(bdone, nbd & 1, lim, abort_flag)) break;
+                        ++nbd;
+                    }
+                    mbar_expect_tx(bfull, (uint32_t)(nkc * kWBChunk));
+                    const unsigned char *src = reinterpret_cast<const unsigned char *>(a.B) + (size_t)un.blk * kWBBytes;
+                    for (int c = 0; c < nkc; ++c) bulk_g2s(sB + c * kWBChunk, src + (size_t)c * kWBChunk, kWBChunk, bfull);
+                    b_pending = true;
+                    if (!ws_wait(bfull, nbf & 1, lim, abort_flag)) break;
+                    ++nbf;
+                    b_pending = false;
+                    cur_blk = un.blk;
+                }
+                const int li = i - u0, buf = li & 1;
+                if (li >= 2 && !ws_wait(&tempty[buf], ((li >> 1) - 1) & 1, lim, abort_flag)) break;
+                tc_fence_after();
+                const uint32_t idesc = F16 ? idesc_f16(128, Nc) : idesc_bf16(128, Nc);
+                const uint32_t dacc = tmem + (uint32_t)(buf * kWN);
+                for (int kc = 0; kc < nkc; ++kc, ++g) {
+                    const int s = (int)(g % kWStages);
+                    if (!ws_wait(&afull[s], (g / kWStages) & 1, lim, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t a_base = saddr(sA + s * kWAStage), b_base = saddr(sB + kc * kWBChunk);
+#pragma unroll
+                    for (int ks = 0; ks < 2; ++ks) {
+                        const uint32_t ko = ks * 16 * 16;  // 16 k = two core matrices = 256 bytes
+                        const uint64_t b_hi = sdesc(b_base + ko), b_lo = sdesc(b_base + kWBArr * 2 + ko);
+                        const uint64_t a_hi = sdesc(a_base + ko), a_lo = sdesc(a_base + kWAArr * 2 + ko);
+                        const uint32_t first = (kc == 0 && ks == 0) ? 0u : 1u;
+                        mma_bf16(dacc, a_hi, b_hi, idesc, first);
+                        mma_bf16(dacc, a_hi, b_lo, idesc, 1u);
+                        mma_bf16(dacc, a_lo, b_hi, idesc, 1u);
+                    }
+                    mma_commit(&aempty[s]);
+                }
+                if (!ok) break;
+                mma_commit(&tfull[buf]);
+            }
+            mma_commit(drain);
+            mbar_wait(drain, 0);
+            if (b_pending) mbar_wait(bfull, nbf & 1);
+        }
+    } else if (warp >= kWProdWarp0) {
+        // -------------------------------------------------------------------- A producers
+        const int qd = warp & 3, hh = (warp - kWProdWarp0) >> 2;
+        const int row = 32 * qd + lane;
+        const int pt = 16 * qd + (lane & 15), comp = lane >> 4;  // point of the tile; 0 = Re lane, 1 = Im lane
+        const double inv1 = 1.0 / (double)a.n1;
+        const int amin = -(a.D1 / 2);
+        uint32_t g = 0;
+        bool ok = true;
+        for (int i = u0; i < u1 && ok; ++i) {
+            const WsUnit un = a.units[i];
+            const int kr = (un.blk % nparts) % a.nkr;
+            const int nkc = min(kWKCB, (a.D1p - kWKR * kr) / kKC);
+            const bool row_ok = pt < un.nj;
+            const float uj = row_ok ? a.u[un.j0 + pt] : 0.f;
+            const float2 w1 = phase_any<POW2>(1, uj, a.log2n1, inv1);
+            const float2 w4 = phase_any<POW2>(4, uj, a.log2n1, inv1);
+            const float2 w2 = cmulf(w1, w1), w8 = cmulf(w4, w4);
+            const float2 w32 = cmulf(cmulf(w8, w8), cmulf(w8, w8));
+            const f2x_t w2x = pk(w2.x, w2.x), w2y = pk(w2.y, w2.y), w2n = pk(-w2.y, -w2.y);
+            const f2x_t w4x = pk(w4.x, w4.x), w4y = pk(w4.y, w4.y), w4n = pk(-w4.y, -w4.y);
+            float2 anchor = make_float2(0.f, 0.f);
+            for (int kc = 0; kc < nkc; ++kc, ++g) {
+                const int s = (int)(g % kWStages);
+                if (g >= (uint32_t)kWStages &&
+                    !ws_wait_warp(&aempty[s], ((g / kWStages) - 1) & 1, lim, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                // this lane's 8 consecutive k: a = amin + 128 kr + 32 kc + 16 hh + 8 comp + 0..7,
+                // as 4 packed pairs: pair 0 from the anchor (exact every 4 chunks, one
+                // rotation by 32 from the previous chunk's otherwise), pair 2 rotated
+                // from it by 4, pairs 1 and 3 from pairs 0 and 2 by 2
+                if ((kc & 3) == 0)
+                    anchor = row_ok ? phase_any<POW2>(amin + kWKR * kr + kKC * kc + 16 * hh + 8 * comp, uj, a.log2n1, inv1)
+                                    : make_float2(0.f, 0.f);
+                else
+                    anchor = cmulf(anchor, w32);
+                const float2 e1 = cmulf(anchor, w1);
+                f2x_t X[4], Y[4];
+                X[0] = pk(anchor.x, e1.x);
+                Y[0] = pk(anchor.y, e1.y);
+                X[2] = X[0]; Y[2] = Y[0]; rot_x2(X[2], Y[2], w4x, w4y, w4n);
+                X[1] = X[0]; Y[1] = Y[0]; rot_x2(X[1], Y[1], w2x, w2y, w2n);
+                X[3] = X[2]; Y[3] = Y[2]; rot_x2(X[3], Y[3], w2x, w2y, w2n);
+                uint32_t hi[8], lo[8];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) {
+                    uint32_t rh, rl, ih, il;
+                    split_x2<F16>(X[m], rh, rl);
+                    split_x2<F16>(Y[m], ih, il);
+                    // the Re lane keeps its real words and sends its imaginary ones to
+                    // the Im lane (lane ^ 16), which sends its real words back
+                    const uint32_t oh = comp ? ih : rh, ol = comp ? il : rl;
+                    const uint32_t xh = __shfl_xor_sync(0xffffffffu, comp ? rh : ih, 16);
+                    const uint32_t xl = __shfl_xor_sync(0xffffffffu, comp ? rl : il, 16);
+                    hi[m] = comp ? xh : oh;
+                    hi[4 + m] = comp ? oh : xh;
+                    lo[m] = comp ? xl : ol;
+                    lo[4 + m] = comp ? ol : xl;
+                }
+                uint16_t *As = reinterpret_cast<uint16_t *>(sA + s * kWAStage);
+#pragma unroll
+                for (int c8 = 0; c8 < 2; ++c8) {
+                    const int idx = kmaj_index(row, 16 * hh + 8 * c8);  // one 16-byte core-matrix row
+                    const int k0 = 4 * c8;
+                    *reinterpret_cast<uint4 *>(As + idx) = make_uint4(hi[k0], hi[k0 + 1], hi[k0 + 2], hi[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + kWAArr + idx) = make_uint4(lo[k0], lo[k0 + 1], lo[k0 + 2], lo[k0 + 3]);
+                }
+                fence_proxy_async();  // the stores are visible to the tensor core
+                mbar_arrive(&afull[s]);
+            }
+        }
+    } else {
+        // -------------------------------------------------------------------- epilogue
+        const int qd = warp & 3, grp = warp >> 2;  // group grp drains buffer grp: units u0 + grp, + 2, ...
+        const int pt = 16 * qd + (lane & 15), comp = lane >> 4;
+        const double inv2 = 1.0 / (double)a.n2;
+        const int bmin = -(a.D2 / 2);
+        const uint32_t lane_base = (uint32_t)(32 * qd) << 16;
+        for (int i = u0 + grp; i < u1; i += 2) {
+            const WsUnit un = a.units[i];
+            const int part = un.blk % nparts, nc = part / a.nkr;
+            const int Nc = min(kWN, a.D2p - kWN * nc);
+            const int li = i - u0, buf = li & 1;
+            if (!ws_wait_warp(&tfull[buf], (li >> 1) & 1, lim, abort_flag)) break;
+            tc_fence_after();
+            const bool row_ok = pt < un.nj;
+            const float vj = row_ok ? a.v[un.j0 + pt] : 0.f;
+            const float2 v1 = phase_any<POW2>(1, vj, a.log2n2, inv2);
+            const float2 v16 = phase_any<POW2>(16, vj, a.log2n2, inv2);
+            const float2 v2 = cmulf(v1, v1);
+            const f2x_t v2x = pk(v2.x, v2.x), v2y = pk(v2.y, v2.y), v2n = pk(-v2.y, -v2.y);
+            const uint32_t cacc = tmem + lane_base + (uint32_t)(buf * kWN);
+            float2 S = make_float2(0.f, 0.f), an = make_float2(0.f, 0.f);
+            // S = sum_b q_b E_v(j, b) for this lane's real row q, in 16-column
+            // groups: A(w^2) + w B(w^2) (even and odd columns, one packed chain)
+            // times the group's anchor
+            auto group = [&](const uint32_t(&q)[16], float2 anc) {
+                f2x_t H = pk(__uint_as_float(q[14]), __uint_as_float(q[15]));
+                f2x_t G = pk(0.f, 0.f);
+#pragma unroll
+                for (int t = 6; t >= 0; --t) {
+                    const f2x_t qr = pk(__uint_as_float(q[2 * t]), __uint_as_float(q[2 * t + 1]));
+                    const f2x_t h2 = fma_x2(H, v2x, fma_x2(G, v2n, qr));
+                    G = fma_x2(H, v2y, mul_x2(G, v2x));
+                    H = h2;
+                }
+                const float2 hr = upk(H), hi = upk(G);
+                const float2 sB = cmulf(make_float2(hr.y, hi.y), v1);
+                const float2 p = cmulf(make_float2(hr.x + sB.x, hi.x + sB.y), anc);
+                S.x += p.x;
+                S.y += p.y;
+            };
+            for (int c = 0; c < Nc; c += 32) {
+                const bool two = c + 16 < Nc;  // warp-uniform
+                uint32_t q0[16], q1[16];
+                tmem_ld16(cacc + (uint32_t)c, q0);
+                if (two) tmem_ld16(cacc + (uint32_t)(c + 16), q1);
+                const float2 an0 = (c & 63) == 0 ? (row_ok ? phase_any<POW2>(bmin + kWN * nc + c, vj, a.log2n2, inv2)
+                                                          : make_float2(0.f, 0.f))
+                                                 : cmulf(an, v16);
+                an = cmulf(an0, v16);
+                tmem_wait_ld();
+                group(q0, an0);
+                if (two) group(q1, an);
+            }
+            tc_fence_before();
+            mbar_arrive(&tempty[buf]);
+            // F = S_re + i S_im: the Re lane takes the Im lane's sum
+            const float ox = __shfl_xor_sync(0xffffffffu, S.x, 16), oy = __shfl_xor_sync(0xffffffffu, S.y, 16);
+            if (comp == 0 && row_ok) {
+                const float sc = a.inv_scale[un.proj];
+                a.F[(size_t)part * a.ntot + un.j0 + pt] = make_float2((S.x - oy) * sc, (S.y + ox) * sc);
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0 && *abort_flag) atomicExch(a.err, 1);
+    if (warp == kWMmaWarp) tmem_dealloc(tmem, 512);
+}
+
 // Per-projection power-of-two scales for FP16 operands: 2^(14 - e) with
 // max|P| < 2^e, so that the largest scaled value is below 2^14; inv = 2^(e - 14).
 __global__ void __launch_bounds__(256) k_proj_scale(const double *__restrict__ proj, long long per, float *scale,
@@ -700,33 +999,36 @@ __global__ void __launch_bounds__(256) k_proj_scale(const double *__restrict__ p
 }
 
 // Pre-split (scaled) projections into hi/lo blocks in the B layout: block
-// (p, nc, kr) holds columns b = 128 nc + (0..127) and rows a = 256 kr + (0..255)
-// as 8 K chunks of [hi | lo][128 x 32]; zero beyond D1 x D2.
-// Grid: x = block, y = K chunk; each thread converts 16 elements.
-template <bool F16>
+// (p, nc, kr) holds columns b = NB nc + (0..NB-1) and rows a = KR kr + (0..KR-1)
+// as KR / 32 K chunks of [hi | lo][NB x 32]; zero beyond D1 x D2.  NB x KR is
+// 128 x 256 (first form) or 256 x 128 (second form), 128 KB either way.
+// Grid: x = block, y = K chunk.
+template <bool F16, int NB, int KR>
 __global__ void __launch_bounds__(256) k_split_projections(const double *__restrict__ proj, int D1, int D2, int nnc,
                                                            int nkr, const float *__restrict__ scale,
                                                            uint16_t *__restrict__ B)
 {
     using namespace umma;
+    constexpr int kArr = NB * kKC;                 // elements of one array of a chunk
+    constexpr int kBlk = (KR / kKC) * 2 * kArr;    // elements of one block
     const int blk = blockIdx.x, kc = blockIdx.y;
     const int kr = blk % nkr, nc = (blk / nkr) % nnc, p = blk / (nkr * nnc);
     const double *src = proj + (long long)p * D1 * D2;
     const float sc = scale[p];
-    uint16_t *dst = B + (size_t)blk * (kBBytes / 2) + (size_t)kc * (2 * kBArr);
-    for (int e = threadIdx.x; e < kBArr; e += 256) {
+    uint16_t *dst = B + (size_t)blk * kBlk + (size_t)kc * (2 * kArr);
+    for (int e = threadIdx.x; e < kArr; e += 256) {
         // e is the linear position in the layout: invert kmaj_index
         const int rg = e >> 8, kg = (e >> 6) & 3, rr = (e >> 3) & 7, kk = e & 7;
-        const int b = nc * kN + rg * 8 + rr, aa = kr * kKR + kc * kKC + kg * 8 + kk;
+        const int b = nc * NB + rg * 8 + rr, aa = kr * KR + kc * kKC + kg * 8 + kk;
         const float xf = (b < D2 && aa < D1) ? (float)src[aa + (long long)D1 * b] * sc : 0.f;
         if constexpr (F16) {
             const __half hi = __float2half_rn(xf);
             dst[e] = __half_as_ushort(hi);
-            dst[kBArr + e] = __half_as_ushort(__float2half_rn(xf - __half2float(hi)));
+            dst[kArr + e] = __half_as_ushort(__float2half_rn(xf - __half2float(hi)));
         } else {
             const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
             dst[e] = __bfloat16_as_ushort(hi);
-            dst[kBArr + e] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
+            dst[kArr + e] = __bfloat16_as_ushort(__float2bfloat16_rn(xf - __bfloat162float(hi)));
         }
     }
 }
@@ -746,15 +1048,16 @@ __global__ void k_sum_parts(const float2 *__restrict__ Fp, int nparts, long long
 }
 
 // uoff[p] = units of the projections before p (uoff[P] = all units), from the
-// points' offsets: a projection with nk points has ceil(nk / 128) tiles per
+// points' offsets: a projection with nk points has ceil(nk / tp) tiles per
 // block and nnc * nkr blocks.  One thread: P is small.
-__global__ void k_unit_offsets(const long long *__restrict__ off, int P, int per_tile, long long *__restrict__ uoff)
+__global__ void k_unit_offsets(const long long *__restrict__ off, int P, int tp, int per_tile,
+                               long long *__restrict__ uoff)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     long long s = 0;
     uoff[0] = 0;
     for (int p = 0; p < P; ++p) {
-        s += (off[p + 1] - off[p] + umma::kM - 1) / umma::kM * per_tile;
+        s += (off[p + 1] - off[p] + tp - 1) / tp * per_tile;
         uoff[p + 1] = s;
     }
 }
@@ -763,10 +1066,9 @@ __global__ void k_unit_offsets(const long long *__restrict__ off, int P, int per
 // to the last projection p with uoff[p] <= u (a projection without points has
 // uoff[p] = uoff[p + 1] and is skipped by that rule).
 __global__ void __launch_bounds__(256) k_make_units(const long long *__restrict__ off,
-                                                    const long long *__restrict__ uoff, int P, int nnc, int nkr,
-                                                    long long nunits, WsUnit *__restrict__ units)
+                                                    const long long *__restrict__ uoff, int P, int tp, int nnc,
+                                                    int nkr, long long nunits, WsUnit *__restrict__ units)
 {
-    using namespace umma;
     const long long u = blockIdx.x * 256LL + threadIdx.x;
     if (u >= nunits) return;
     int lo = 0, hi = P - 1;
@@ -777,10 +1079,10 @@ __global__ void __launch_bounds__(256) k_make_units(const long long *__restrict_
     }
     const int p = lo;
     const long long nk = off[p + 1] - off[p];
-    const long long tiles = (nk + kM - 1) / kM, local = u - uoff[p];
+    const long long tiles = (nk + tp - 1) / tp, local = u - uoff[p];
     const long long t = local % tiles, rest = local / tiles;
     const int kr = (int)(rest % nkr), nc = (int)(rest / nkr);
-    units[u] = WsUnit{off[p] + t * kM, p, (p * nnc + nc) * nkr + kr, (int)min((long long)kM, nk - t * kM), 0};
+    units[u] = WsUnit{off[p] + t * tp, p, (p * nnc + nc) * nkr + kr, (int)min((long long)tp, nk - t * tp), 0};
 }
 
 __global__ void k_fill_f32(float *__restrict__ x, int n, float v)
@@ -790,14 +1092,29 @@ __global__ void k_fill_f32(float *__restrict__ x, int n, float v)
 }
 
 // The DFT kernels' dynamic shared memory is raised once per device and kernel.
-static void ws_smem_attr(int device, const void *kern)
+static void ws_smem_attr(int device, const void *kern, size_t bytes)
 {
     static std::mutex m;
     static std::set<std::pair<int, const void *>> done;
     std::lock_guard<std::mutex> g(m);
     if (done.count({device, kern})) return;
-    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)umma::kWsSmem));
+    GF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     done.insert({device, kern});
+}
+
+// Which tensor-core DFT: the first form (N = 128, 128-point tiles) by default;
+// GENFIRE_DFT_KERNEL=n256 selects the second (Re and Im stacked in rows,
+// N = 256, 64-point tiles).  On 256 x 256 projections (90 of them, 2.77 M
+// points) the first takes 1.63 ms and the second 1.80 ms: the second's MMAs
+// alone run in 1.15 ms against the first's 1.31 ms (fewer shared-memory bytes
+// per MAC), but its K split (blocks of 128 rows) and row-wise Re/Im double the
+// E_v contraction twice over.  The choice is a fixed rule, not a timing, so
+// that a gridding call gives the same bits in every process (the two forms
+// round differently).
+static bool dft_use_wide()
+{
+    const char *e = std::getenv("GENFIRE_DFT_KERNEL");
+    return e && std::strcmp(e, "n256") == 0;
 }
 
 // Host: F (float2, one per selected point) for all projections.  Everything is
@@ -810,18 +1127,22 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
 {
     using namespace umma;
     cudaStream_t st = ctx->stream;
+    const bool wide = dft_use_wide();
+    const int NB = wide ? kWN : kN, KR = wide ? kWKR : kKR;  // block shape
     const int D1p = (D1 + kKC - 1) / kKC * kKC, D2p = (D2 + 15) / 16 * 16;
-    const int nnc = (D2p + kN - 1) / kN, nkr = (D1p + kKR - 1) / kKR;
+    const int nnc = (D2p + NB - 1) / NB, nkr = (D1p + KR - 1) / KR;
     const int nparts = nnc * nkr;
     const int nblk = P * nnc * nkr;
+    const int tp = wide ? kWPoints : kM;  // points per tile
     long long ntot = 0, nunits = 0;
     for (int p = 0; p < P; ++p) {
         ntot += nk[p];
-        nunits += (nk[p] + kM - 1) / kM * nparts;
+        nunits += (nk[p] + tp - 1) / tp * nparts;
     }
     if (ntot == 0) return;
     if (nunits > INT32_MAX) fail(GENFIRE_ERR_ARG, "tensor-core gridding: too many selected points.");
 
+    static_assert(kBBytes == kWBBytes, "both block shapes hold 128 KB");
     DevBuf B((size_t)nblk * kBBytes, st), scl(2 * sizeof(float) * P, st);
     float *d_scale = scl.as<float>(), *d_inv = d_scale + P;
     if (fp16) {
@@ -830,17 +1151,22 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
         k_fill_f32<<<(2 * P + 255) / 256, 256, 0, st>>>(d_scale, 2 * P, 1.f);
     }
     GF_CHECK_LAUNCH();
-    if (fp16)
-        k_split_projections<true><<<dim3((unsigned)nblk, kKCB), 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, B.as<uint16_t>());
-    else
-        k_split_projections<false><<<dim3((unsigned)nblk, kKCB), 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, B.as<uint16_t>());
+    const dim3 sgrid((unsigned)nblk, KR / kKC);
+    uint16_t *dB = B.as<uint16_t>();
+    if (wide) {
+        if (fp16) k_split_projections<true, kWN, kWKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
+        else k_split_projections<false, kWN, kWKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
+    } else {
+        if (fp16) k_split_projections<true, kN, kKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
+        else k_split_projections<false, kN, kKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
+    }
     GF_CHECK_LAUNCH();
 
     DevBuf du(sizeof(WsUnit) * (size_t)nunits, st), duoff(sizeof(long long) * (P + 1), st);
-    k_unit_offsets<<<1, 32, 0, st>>>(d_off, P, nparts, duoff.as<long long>());
+    k_unit_offsets<<<1, 32, 0, st>>>(d_off, P, tp, nparts, duoff.as<long long>());
     GF_CHECK_LAUNCH();
-    k_make_units<<<(unsigned)((nunits + 255) / 256), 256, 0, st>>>(d_off, duoff.as<long long>(), P, nnc, nkr, nunits,
-                                                                   du.as<WsUnit>());
+    k_make_units<<<(unsigned)((nunits + 255) / 256), 256, 0, st>>>(d_off, duoff.as<long long>(), P, tp, nnc, nkr,
+                                                                   nunits, du.as<WsUnit>());
     GF_CHECK_LAUNCH();
     DevBuf Fp(nparts > 1 ? sizeof(float2) * (size_t)nparts * ntot : 0, st);
     WsArgs a;
@@ -869,18 +1195,19 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
         if (v > 0 && v < kWaitCycles) a.wait_cycles = v;
     }
     const bool pow2 = a.log2n1 >= 0 && a.log2n2 >= 0;
-    const void *kern = fp16 ? (pow2 ? (const void *)k_dft_tcgen05<true, true> : (const void *)k_dft_tcgen05<true, false>)
-                            : (pow2 ? (const void *)k_dft_tcgen05<false, true> : (const void *)k_dft_tcgen05<false, false>);
-    ws_smem_attr(ctx->device, kern);
+    const void *kern;
+    if (wide)
+        kern = fp16 ? (pow2 ? (const void *)k_dft_tcgen05_w<true, true> : (const void *)k_dft_tcgen05_w<true, false>)
+                    : (pow2 ? (const void *)k_dft_tcgen05_w<false, true> : (const void *)k_dft_tcgen05_w<false, false>);
+    else
+        kern = fp16 ? (pow2 ? (const void *)k_dft_tcgen05<true, true> : (const void *)k_dft_tcgen05<true, false>)
+                    : (pow2 ? (const void *)k_dft_tcgen05<false, true> : (const void *)k_dft_tcgen05<false, false>);
+    const size_t smem = wide ? kWSmem : kWsSmem;
+    ws_smem_attr(ctx->device, kern, smem);
     const int grid = (int)std::min<long long>(nunits, (long long)ctx->sm_count);
     if (ev_begin) GF_CUDA(cudaEventRecord(ev_begin, st));
-    if (fp16) {
-        if (pow2) k_dft_tcgen05<true, true><<<grid, kWsThreads, kWsSmem, st>>>(a);
-        else k_dft_tcgen05<true, false><<<grid, kWsThreads, kWsSmem, st>>>(a);
-    } else {
-        if (pow2) k_dft_tcgen05<false, true><<<grid, kWsThreads, kWsSmem, st>>>(a);
-        else k_dft_tcgen05<false, false><<<grid, kWsThreads, kWsSmem, st>>>(a);
-    }
+    void *args[] = {&a};
+    GF_CUDA(cudaLaunchKernel(kern, dim3((unsigned)grid), dim3(wide ? kWThreads : kWsThreads), args, smem, st));
     GF_CHECK_LAUNCH();
     if (ev_end) GF_CUDA(cudaEventRecord(ev_end, st));
     if (nparts > 1) {

@@ -152,15 +152,19 @@ def test_grid_dft_rejects_bad_parameters(lib, ctx, field, value, status):
     assert str(e.value).startswith("GENFIRE:")
 
 
+@pytest.mark.parametrize("form", ["n128", "n256"])
 @pytest.mark.parametrize("prec", ["mixed", "fp16"])
 @pytest.mark.parametrize("D1,D2,P,os_,cut", [(64, 64, 12, 2.0, 0.125), (40, 300, 3, 2.0, 0.3), (100, 72, 4, 2.0, 0.2),
                                              (128, 128, 3, 2.0, 0.125), (300, 40, 2, 2.0, 0.3),
                                              (280, 144, 2, 2.0, 0.2)])
-def test_grid_dft_mixed_tensor_core_shapes(lib, ctx, oracle, D1, D2, P, os_, cut, prec):
-    """Tensor-core DFT (split BF16 and split FP16): several 128-point tiles, K (D1)
-    not a multiple of 32 and above 256 (two resident blocks along K), N (D2) not a
-    multiple of 16 and above 128 (several 128-column blocks), a non-power-of-two
-    grid (FP64 phase reduction)."""
+def test_grid_dft_mixed_tensor_core_shapes(lib, ctx, oracle, monkeypatch, D1, D2, P, os_, cut, prec, form):
+    """Tensor-core DFT (split BF16 and split FP16), both forms (N = 128 with
+    128-point tiles, the default; N = 256 with Re and Im stacked in rows and
+    64-point tiles): several tiles, K (D1) not a multiple of 32 and above one
+    block's rows (256 or 128), N (D2) not a multiple of 16 and above one
+    block's columns (128 or 256), a non-power-of-two grid (FP64 phase
+    reduction)."""
+    monkeypatch.setenv("GENFIRE_DFT_KERNEL", form)
     projs, angles = _random_case(D1 + D2 + P, D1, D2, P)
     kw = dict(oversamplingRatio=os_, interpolationCutoffDistance=cut, vector3=(0, 0, 1))
     M, rec, nk = ctx.grid_dft(params(lib, D1, D2, P, precision=prec, **kw), projs, angles)

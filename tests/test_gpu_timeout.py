@@ -1,6 +1,7 @@
-"""The tensor-core gridding kernel's bounded waits, made to expire on real work.
+"""The tensor-core gridding kernels' bounded waits, made to expire on real work.
 
-Every mbarrier wait of k_dft_tcgen05 has a clock limit.  GENFIRE_DEBUG_DFT_WAIT_CYCLES
+Every mbarrier wait of k_dft_tcgen05 (and of its N = 256 form,
+k_dft_tcgen05_w, selected by GENFIRE_DFT_KERNEL=n256) has a clock limit.  GENFIRE_DEBUG_DFT_WAIT_CYCLES
 shortens the main loop's limit to one cycle (polled with the non-blocking
 mbarrier.test_wait), so a wait for a bulk copy or for the MMAs just issued
 expires while they are still in flight.  The kernel must
@@ -28,7 +29,9 @@ def _case(lib, oracle):
     return (params(lib, D, D, P, precision="mixed", **kw), oracle.make_params(D, D, P, **kw), projs, angles)
 
 
-def test_expired_wait_reports_timeout_and_context_recovers(lib, ctx, oracle, monkeypatch):
+@pytest.mark.parametrize("form", ["n128", "n256"])
+def test_expired_wait_reports_timeout_and_context_recovers(lib, ctx, oracle, monkeypatch, form):
+    monkeypatch.setenv("GENFIRE_DFT_KERNEL", form)
     p, op, projs, angles = _case(lib, oracle)
     Mo, _, nko = oracle.grid_dft(op, projs, angles)
     for _ in range(2):
