@@ -2,11 +2,13 @@
 //
 // Pipeline for P projections (all on the context stream):
 //   1. k_sel_count   per row (k2, k3) of the gridded space and projection: the
-//                    k1 interval near the plane, FP32 plane test of its points;
-//                    one count per 1024-row chunk
-//   2. k_sel_scan    per-projection exclusive scan of the chunk counts
-//   3. k_sel_write   ordered compaction: (index, D, u, v) in ascending index
-//                    order within each projection, i.e. the order of find()
+//                    k1 interval near the plane, FP32 plane test of its
+//                    points; the row's count
+//   2. CUB           exclusive scan of the row counts (the rows' output
+//                    offsets) and the list of rows that hold points
+//   3. k_sel_write   per listed row: (index, D, u, v) at its offset, so each
+//                    projection's points are in ascending index order, the
+//                    order of find()
 //   4. k_dft         F_j = sum_b E_v(j,b) sum_a E_u(j,a) P(a,b) per point
 //   5. k_accum_runs  the entries (projection-major) sorted stably by grid
 //                    index; each run of one grid point sums its contributions
@@ -19,6 +21,9 @@
 #include "internal.h"
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+#include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
 
 #include <algorithm>
 #include <cstring>
@@ -163,9 +168,8 @@ void check_params(const genfire_params &p, bool need_projs)
 // would bound the selection): for a float D, D < cutoff in double holds iff
 // D < cut_lt, the smallest float not below cutoff; n/2 is exact in FP32.
 struct SelParams {
-    int lo1, lo2, lo3, l1, l2;
+    int lo1, lo2, lo3, l1, l2, l3;
     int nrows;    // l2 * l3 rows of the gridded index space
-    int nchunks;  // CTAs per projection
     float cut_lt;      // D < cutoff  <=>  D < cut_lt
     float cut_margin;  // cutoff + 0.01 in FP32: the candidate-interval half width
     float half1, half2;
@@ -174,11 +178,12 @@ struct SelParams {
 // Rows (k2, k3) of the gridded index space are the work units: the points of
 // a row that can lie within the cutoff of the plane form one interval of k1,
 // found with conservative FP32 bounds; only those candidates get the exact
-// test, and rows are taken in (k3, k2) order so the output keeps the
-// ascending linear order of find().
+// test.  Row ri = i2 + l2 i3 holds the linear indices (k1 - lo1) + l1 ri, so
+// rows in ascending ri and k1 ascending within a row give the ascending order
+// of find().  The count pass runs one thread per row: a CTA is 8 warps, each
+// 32 consecutive rows (i2) of one i3.
 constexpr int kSelThreads = 256;
-constexpr int kSelItems = 4;
-constexpr int kSelChunk = kSelThreads * kSelItems;  // rows per CTA
+constexpr int kSelRowsX = 32, kSelRowsY = kSelThreads / kSelRowsX;
 
 // FP32 plane test of grid point (K1, K2, K3) (distancePointsPlane_YY,
 // closestpoint, R \ CP, box filter), with every rounding step explicit.
@@ -214,7 +219,9 @@ __device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp,
 // Candidate k1 range [k1a, k1b] of row (K2, K3): every k1 with
 // |k1 h1 + K2 h2 + K3 h3| below the cutoff, widened by a margin that covers the
 // FP32 rounding of D (|error| < 1e-3 for grids up to 2^16) and of the bounds.
-__device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp, float K2, float K3, int &k1a, int &k1b)
+// ih = 1 / h1 (IEEE division), formed once per projection.
+__device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp, float ih, float K2, float K3,
+                                          int &k1a, int &k1b)
 {
     const int lo = sp.lo1, hi = sp.lo1 + sp.l1 - 1;
     const float x = -(K2 * g.h[1] + K3 * g.h[2]);
@@ -225,7 +232,6 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
     if (fabsf(h1) >= 0.01f) {
         // bounds through the reciprocal: within a few ulps of the quotients,
         // which the one-point padding below covers
-        const float ih = 1.0f / h1;
         float b0 = (x - c) * ih, b1 = (x + c) * ih;
         if (b0 > b1) { const float t = b0; b0 = b1; b1 = t; }
         b0 = fmaxf(b0, (float)lo - 4.f);
@@ -238,103 +244,87 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
     }
 }
 
-// block-wide exclusive scan of one int per thread; *total receives the sum
-__device__ __forceinline__ int block_exclusive_scan(int x, int *total)
+// the projection's geometry in shared memory, and 1 / h1
+__device__ __forceinline__ void load_geometry(const ProjGeom *__restrict__ geo, int p, ProjGeom &sg, float &sih)
 {
-    __shared__ int wsum[kSelThreads / 32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int inc = x;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    if (lane == 31) wsum[w] = inc;
+    static_assert(sizeof(ProjGeom) % 4 == 0 && sizeof(ProjGeom) / 4 <= kSelThreads, "geometry words");
+    if (threadIdx.x < sizeof(ProjGeom) / 4)
+        reinterpret_cast<uint32_t *>(&sg)[threadIdx.x] = reinterpret_cast<const uint32_t *>(geo + p)[threadIdx.x];
     __syncthreads();
-    int woff = 0, tot = 0;
-#pragma unroll
-    for (int k = 0; k < kSelThreads / 32; ++k) {
-        const int c = wsum[k];
-        woff += (k < w) ? c : 0;
-        tot += c;
-    }
+    if (threadIdx.x == 0) sih = 1.0f / sg.h[0];
     __syncthreads();
-    *total = tot;
-    return woff + inc - x;
 }
 
-// Counts per CTA chunk, and per row (uint16: a row holds at most l1 <= 32769
-// points) so the write pass tests only the rows that hold points.
-__global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__restrict__ geo, SelParams sp,
-                                                          int *__restrict__ counts, uint16_t *__restrict__ rowcnt)
+// Points per row (uint16: a row holds at most l1 <= 32769 points).  Grid:
+// x = 32-row group along i2, y = group of 8 values of i3, z = projection of
+// the batch (p0 + z).
+__global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__restrict__ geo, int p0, SelParams sp,
+                                                          uint16_t *__restrict__ rowcnt)
 {
-    const int p = blockIdx.y, chunk = blockIdx.x;
-    const ProjGeom g = geo[p];
-    int total = 0;
-    for (int it = 0; it < kSelItems; ++it) {
-        const int ri = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
-        int cnt = 0;
-        if (ri < sp.nrows) {
-            const int i2 = ri % sp.l2, i3 = ri / sp.l2;
-            const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
-            int a0, a1;
-            row_range(g, sp, K2, K3, a0, a1);
-            for (int k1 = a0; k1 <= a1; ++k1) {
-                float D, u, v;
-                cnt += sel_test(g, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
-            }
-            rowcnt[(long long)p * sp.nrows + ri] = (uint16_t)cnt;
-        }
-        int tot;
-        block_exclusive_scan(cnt, &tot);
-        total += tot;
+    __shared__ ProjGeom sg;
+    __shared__ float sih;
+    const int p = p0 + blockIdx.z;
+    load_geometry(geo, p, sg, sih);
+    const int i2 = blockIdx.x * kSelRowsX + (threadIdx.x & (kSelRowsX - 1));
+    const int i3 = blockIdx.y * kSelRowsY + threadIdx.x / kSelRowsX;
+    if (i2 >= sp.l2 || i3 >= sp.l3) return;
+    const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
+    int a0, a1;
+    row_range(sg, sp, sih, K2, K3, a0, a1);
+    int cnt = 0;
+    for (int k1 = a0; k1 <= a1; ++k1) {
+        float D, u, v;
+        cnt += sel_test(sg, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
     }
-    if (threadIdx.x == 0) counts[(long long)p * sp.nchunks + chunk] = total;
+    rowcnt[(long long)blockIdx.z * sp.nrows + i2 + (long long)sp.l2 * i3] = (uint16_t)cnt;
 }
 
-// In-place exclusive scan of each projection's chunk counts; totals[p] = sum.
-__global__ void __launch_bounds__(1024) k_sel_scan(int *counts, int nchunks, long long *totals)
+// uint32 sum (wraps modulo 2^32) for the offset scan
+struct AddU32 {
+    __host__ __device__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
+};
+
+// nonzero row count (the rows the write pass visits)
+struct RowHolds {
+    const uint16_t *cnt;
+    __host__ __device__ bool operator()(uint32_t r) const { return cnt[r] != 0; }
+};
+
+// Per projection of the batch (one thread each): its point count, from the
+// rows' exclusive offsets (rowoff, modulo 2^32) and counts.
+__global__ void k_sel_totals(const uint32_t *__restrict__ rowoff, const uint16_t *__restrict__ rowcnt, int np,
+                             long long nrows, long long *__restrict__ nk)
 {
-    __shared__ long long part[1024];
-    int *c = counts + (long long)blockIdx.x * nchunks;
-    const int per = (nchunks + blockDim.x - 1) / blockDim.x;
-    const int b = threadIdx.x * per, e = min(b + per, nchunks);
-    long long s = 0;
-    for (int i = b; i < e; ++i) s += c[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        long long run = 0;
-        for (int i = 0; i < (int)blockDim.x; ++i) { long long t = part[i]; part[i] = run; run += t; }
-        totals[blockIdx.x] = run;
-    }
-    __syncthreads();
-    long long run = part[threadIdx.x];
-    for (int i = b; i < e; ++i) { int t = c[i]; c[i] = (int)run; run += t; }
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= np) return;
+    const long long last = np * nrows - 1;
+    const uint32_t b = rowoff[q * nrows];
+    const uint32_t e = q + 1 < np ? rowoff[(q + 1) * nrows] : rowoff[last] + (uint32_t)rowcnt[last];
+    nk[q] = (long long)(uint32_t)(e - b);
 }
 
-__global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__restrict__ geo, SelParams sp,
-                                                          const int *__restrict__ chunk_off,
-                                                          const long long *__restrict__ proj_off,
-                                                          const uint16_t *__restrict__ rowcnt,
+// The listed rows (each holds points), a grid-stride loop over the count the
+// list's selection left on the device: the row's points at the projection's
+// first output offset (doff) plus the row's offset within the projection.
+__global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__restrict__ geo, int p0, SelParams sp,
+                                                          const uint32_t *__restrict__ rows,
+                                                          const int *__restrict__ nrows_listed,
+                                                          const uint32_t *__restrict__ rowoff,
+                                                          const long long *__restrict__ doff,
                                                           uint32_t *__restrict__ ind, float *__restrict__ dist,
                                                           float *__restrict__ uu, float *__restrict__ vv)
 {
-    const int p = blockIdx.y, chunk = blockIdx.x;
-    const ProjGeom g = geo[p];
-    long long base = proj_off[p] + chunk_off[(long long)p * sp.nchunks + chunk];
-    for (int it = 0; it < kSelItems; ++it) {
-        const int ri = chunk * kSelChunk + it * kSelThreads + threadIdx.x;
-        const int cnt = ri < sp.nrows ? (int)rowcnt[(long long)p * sp.nrows + ri] : 0;
-        int a0 = 1, a1 = 0;
-        float K2 = 0.f, K3 = 0.f;
-        if (cnt > 0) {
-            K2 = (float)(sp.lo2 + ri % sp.l2);
-            K3 = (float)(sp.lo3 + ri / sp.l2);
-            row_range(g, sp, K2, K3, a0, a1);
-        }
-        int tot;
-        long long o = base + block_exclusive_scan(cnt, &tot);
+    const int n = *nrows_listed;
+    for (int i = blockIdx.x * kSelThreads + threadIdx.x; i < n; i += gridDim.x * kSelThreads) {
+        const uint32_t r = rows[i];  // batch row index: q * nrows + ri
+        const int q = (int)(r / (uint32_t)sp.nrows), ri = (int)(r - (uint32_t)q * (uint32_t)sp.nrows);
+        const ProjGeom &g = geo[p0 + q];
+        const float ih = 1.0f / g.h[0];
+        const int i3 = ri / sp.l2, i2 = ri - i3 * sp.l2;
+        const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
+        int a0, a1;
+        row_range(g, sp, ih, K2, K3, a0, a1);
+        long long o = doff[p0 + q] + (uint32_t)(rowoff[r] - rowoff[(uint32_t)q * (uint32_t)sp.nrows]);
         for (int k1 = a0; k1 <= a1; ++k1) {
             float D, u, v;
             if (sel_test(g, sp, (float)k1, K2, K3, D, u, v)) {
@@ -345,7 +335,6 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__res
                 ++o;
             }
         }
-        base += tot;
     }
 }
 
@@ -671,15 +660,33 @@ struct Selection {
     long long total = 0;
 };
 
-// off[0] = 0, off[p + 1] = off[p] + nk[p] (one thread: P is small)
-__global__ void k_sel_offsets(const long long *__restrict__ nk, int P, long long *__restrict__ off)
+// off[0] = 0, off[p + 1] = off[p] + nk[p]: one CTA of 1024 threads, a block
+// scan per 1024 projections with the running total carried
+__global__ void __launch_bounds__(1024) k_sel_offsets(const long long *__restrict__ nk, int P, long long *__restrict__ off)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    long long s = 0;
-    off[0] = 0;
-    for (int p = 0; p < P; ++p) {
-        s += nk[p];
-        off[p + 1] = s;
+    __shared__ long long wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long carry = 0;
+    if (threadIdx.x == 0) off[0] = 0;
+    for (int base = 0; base < P; base += 1024) {
+        const int i = base + threadIdx.x;
+        const long long x = i < P ? nk[i] : 0;
+        long long inc = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsum[w] = inc;
+        __syncthreads();
+        long long before = 0, tot = 0;
+        for (int k = 0; k < 32; ++k) {
+            before += k < w ? wsum[k] : 0;
+            tot += wsum[k];
+        }
+        if (i < P) off[i + 1] = carry + before + inc;
+        carry += tot;
+        __syncthreads();
     }
 }
 
@@ -689,42 +696,76 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     cudaStream_t st = ctx->stream;
     const int P = (int)geo.size();
     SelParams sp;
-    sp.lo1 = g.lo1; sp.lo2 = g.lo2; sp.lo3 = g.lo3; sp.l1 = g.l1; sp.l2 = g.l2;
+    sp.lo1 = g.lo1; sp.lo2 = g.lo2; sp.lo3 = g.lo3; sp.l1 = g.l1; sp.l2 = g.l2; sp.l3 = g.l3;
     sp.nrows = g.l2 * g.l3;
-    sp.nchunks = (int)cdiv(sp.nrows, kSelChunk);
     sp.cut_lt = (float)cutoff;
     if ((double)sp.cut_lt < cutoff) sp.cut_lt = std::nextafter(sp.cut_lt, INFINITY);
     sp.cut_margin = (float)cutoff + 0.01f;
     sp.half1 = (float)(n1 / 2.0); sp.half2 = (float)(n2 / 2.0);
     DevBuf dgeo(sizeof(ProjGeom) * P, st);
     GF_CUDA(cudaMemcpyAsync(dgeo.p, geo.data(), sizeof(ProjGeom) * P, cudaMemcpyHostToDevice, st));
-    DevBuf counts(sizeof(int) * (size_t)sp.nchunks * P, st), totals(sizeof(long long) * P, st);
-    DevBuf rowcnt(sizeof(uint16_t) * (size_t)sp.nrows * P, st);
-    dim3 grid(sp.nchunks, P);
-    k_sel_count<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), rowcnt.as<uint16_t>());
-    GF_CHECK_LAUNCH();
-    k_sel_scan<<<P, 1024, 0, st>>>(counts.as<int>(), sp.nchunks, totals.as<long long>());
-    GF_CHECK_LAUNCH();
+
+    // Batches of projections with at most 2^30 rows (CUB's item counts are
+    // int) and 65535 projections (the count pass's grid z).  Row offsets are uint32 and may wrap across a batch; a projection's
+    // own offsets are differences modulo 2^32, exact since it holds fewer than
+    // 2^31 points.
+    const long long nrows = sp.nrows;
+    const int pb = (int)std::max<long long>(1, std::min<long long>(std::min(P, 65535), (1LL << 30) / nrows));
+    struct Batch {
+        int p0, np;
+        DevBuf cnt, off, rows, nlisted;
+    };
+    std::vector<Batch> batches;
+    DevBuf dnk(sizeof(long long) * P, st), tmp;
+    for (int p0 = 0; p0 < P; p0 += pb) {
+        batches.emplace_back();
+        Batch &b = batches.back();
+        b.p0 = p0;
+        b.np = std::min(pb, P - p0);
+        const long long nr = (long long)b.np * nrows;
+        b.cnt.alloc(sizeof(uint16_t) * nr, st);
+        b.off.alloc(sizeof(uint32_t) * nr, st);
+        b.rows.alloc(sizeof(uint32_t) * nr, st);
+        b.nlisted.alloc(sizeof(int), st);
+        const dim3 grid((unsigned)cdiv(sp.l2, kSelRowsX), (unsigned)cdiv(sp.l3, kSelRowsY), (unsigned)b.np);
+        k_sel_count<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), p0, sp, b.cnt.as<uint16_t>());
+        GF_CHECK_LAUNCH();
+        const thrust::counting_iterator<uint32_t> ids(0);
+        const RowHolds holds{b.cnt.as<uint16_t>()};
+        size_t t1 = 0, t2 = 0;
+        GF_CUDA(cub::DeviceScan::ExclusiveScan(nullptr, t1, b.cnt.as<uint16_t>(), b.off.as<uint32_t>(), AddU32(),
+                                               (uint32_t)0, (int)nr, st));
+        GF_CUDA(cub::DeviceSelect::If(nullptr, t2, ids, b.rows.as<uint32_t>(), b.nlisted.as<int>(), (int)nr, holds, st));
+        if (std::max(t1, t2) > tmp.bytes) tmp.alloc(std::max(t1, t2), st);
+        GF_CUDA(cub::DeviceScan::ExclusiveScan(tmp.p, t1, b.cnt.as<uint16_t>(), b.off.as<uint32_t>(), AddU32(),
+                                               (uint32_t)0, (int)nr, st));
+        GF_CUDA(cub::DeviceSelect::If(tmp.p, t2, ids, b.rows.as<uint32_t>(), b.nlisted.as<int>(), (int)nr, holds, st));
+        k_sel_totals<<<(unsigned)cdiv(b.np, 128), 128, 0, st>>>(b.off.as<uint32_t>(), b.cnt.as<uint16_t>(), b.np,
+                                                                 nrows, dnk.as<long long>() + p0);
+        GF_CHECK_LAUNCH();
+    }
     sel.doff.alloc(sizeof(long long) * (P + 1), st);
-    k_sel_offsets<<<1, 32, 0, st>>>(totals.as<long long>(), P, sel.doff.as<long long>());
+    k_sel_offsets<<<1, 1024, 0, st>>>(dnk.as<long long>(), P, sel.doff.as<long long>());
     GF_CHECK_LAUNCH();
     sel.nk.assign(P, 0);
-    GF_CUDA(cudaMemcpyAsync(sel.nk.data(), totals.p, sizeof(long long) * P, cudaMemcpyDeviceToHost, st));
+    GF_CUDA(cudaMemcpyAsync(sel.nk.data(), dnk.p, sizeof(long long) * P, cudaMemcpyDeviceToHost, st));
     GF_CUDA(cudaStreamSynchronize(st));
     sel.off.assign(P + 1, 0);
     for (int p = 0; p < P; ++p) sel.off[p + 1] = sel.off[p] + sel.nk[p];
     sel.total = sel.off[P];
+    if (sel.total >= (1LL << 31)) fail(GENFIRE_ERR_ARG, "more than 2^31 selected points in one gridding call.");
     const size_t nt = (size_t)std::max<long long>(sel.total, 1);
     sel.ind.alloc(nt * sizeof(uint32_t), st);
     sel.dist.alloc(nt * sizeof(float), st);
     sel.u.alloc(nt * sizeof(float), st);
     sel.v.alloc(nt * sizeof(float), st);
-    // (the offsets come from the device copy: no host-to-device copy, whose
-    // pageable source would synchronise the stream)
-    k_sel_write<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), sp, counts.as<int>(), sel.doff.as<long long>(),
-                                              rowcnt.as<uint16_t>(), sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
-                                              sel.v.as<float>());
-    GF_CHECK_LAUNCH();
+    for (const Batch &b : batches) {
+        k_sel_write<<<(unsigned)(8 * ctx->sm_count), kSelThreads, 0, st>>>(
+            dgeo.as<ProjGeom>(), b.p0, sp, b.rows.as<uint32_t>(), b.nlisted.as<int>(), b.off.as<uint32_t>(),
+            sel.doff.as<long long>(), sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
+            sel.v.as<float>());
+        GF_CHECK_LAUNCH();
+    }
 }
 
 // CUDA events on the context stream between the stages of a gridding call
