@@ -448,11 +448,18 @@ __global__ void k_iota(uint32_t *__restrict__ v, long long n)
         v[i] = (uint32_t)i;
 }
 
+// Per touched point of the gridded space, one 32-byte record (one sector):
+// the FP64 weighted sums, or the last exact hit with the weight field -1.
+struct __align__(32) GridAcc {
+    double x, y;  // sum of w F, or the exact hit's value
+    double w;     // sum of w (> 0), or -1 for an exact hit
+    double pad;
+};
+
 template <typename T>
 __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order,
                              const float *__restrict__ dist, const cplx<T> *__restrict__ F, long long n,
-                             double2 *__restrict__ num, double *__restrict__ wsum, double2 *__restrict__ ex,
-                             uint8_t *__restrict__ hx, unsigned *__restrict__ touched)
+                             GridAcc *__restrict__ acc, unsigned *__restrict__ touched)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const uint32_t li = keys[i];
@@ -474,12 +481,10 @@ __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *
                 w += wgt;
             }
         }
-        if (w != 0.0) {
-            num[li] = a;
-            wsum[li] = w;
-        }
-        if (hit) ex[li] = e;
-        hx[li] = hit ? 1 : 0;
+        // one 32-byte record: the last exact hit (weight field -1) or the
+        // weighted sums (weight sum > 0)
+        double4 *r = reinterpret_cast<double4 *>(acc + li);
+        *r = hit ? make_double4(e.x, e.y, -1.0, 0.0) : make_double4(a.x, a.y, w, 0.0);
         atomicOr(&touched[li >> 5], 1u << (li & 31));
     }
 }
@@ -507,8 +512,7 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
 // setup) small against the bytes written.
 constexpr int kFinRows = 4;
 template <typename TO>
-__global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ num, const double *__restrict__ wsum,
-                                                  const double2 *__restrict__ ex, const uint8_t *__restrict__ hx,
+__global__ void __launch_bounds__(256) k_finalize(const GridAcc *__restrict__ acc,
                                                   const unsigned *__restrict__ touched, GridSpec g, int n1, int n2,
                                                   int centro, cplx<TO> *__restrict__ M)
 {
@@ -548,20 +552,16 @@ __global__ void __launch_bounds__(256) k_finalize(const double2 *__restrict__ nu
         const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
         bool cj;
         const long long li = src_index(g, n1, n2, centro, c, c2, c3, cj);
-        if (hx[li]) {
-            const double2 v = ex[li];
-            M[row + c] = mk((TO)v.x, (TO)(cj ? -v.y : v.y));
+        const double4 a = *reinterpret_cast<const double4 *>(acc + li);
+        if (a.z < 0.0) {  // exact hit
+            M[row + c] = mk((TO)a.x, (TO)(cj ? -a.y : a.y));
         } else if constexpr (sizeof(TO) == 8) {
-            const double ws = wsum[li];
-            double2 v = num[li];
-            v.x /= ws;
-            v.y /= ws;
-            M[row + c] = mk(v.x, cj ? -v.y : v.y);
+            const double vx = a.x / a.z, vy = a.y / a.z;
+            M[row + c] = mk(vx, cj ? -vy : vy);
         } else {
             // single-precision output: the average is formed in FP32 from the FP64 sums
-            const float ws = (float)wsum[li];
-            const double2 v = num[li];
-            const float x = __fdiv_rn((float)v.x, ws), y = __fdiv_rn((float)v.y, ws);
+            const float ws = (float)a.z;
+            const float x = __fdiv_rn((float)a.x, ws), y = __fdiv_rn((float)a.y, ws);
             M[row + c] = mk((TO)x, (TO)(cj ? -y : y));
         }
     }
@@ -844,7 +844,7 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
 
     // weighted average in FP64, projection by projection
     const size_t G = (size_t)g.total;
-    DevBuf num(sizeof(double2) * G, st), wsum(sizeof(double) * G, st), ex(sizeof(double2) * G, st), hx(G, st);
+    DevBuf acc(sizeof(GridAcc) * G, st);  // written only at touched points
     DevBuf touched(sizeof(unsigned) * ((G + 31) / 32), st);  // the only array that is cleared
     GF_CUDA(cudaMemsetAsync(touched.p, 0, touched.bytes, st));
     if (sel.total > 0) {
@@ -863,14 +863,12 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
                                                 vin.as<uint32_t>(), vout.as<uint32_t>(), n, 0, bits, st));
         k_accum_runs<T><<<grid_for(ctx, n, 256), 256, 0, st>>>(keys.as<uint32_t>(), vout.as<uint32_t>(),
                                                                 sel.dist.as<float>(), F.as<cplx<T>>(), n,
-                                                                num.as<double2>(), wsum.as<double>(),
-                                                                ex.as<double2>(), hx.as<uint8_t>(),
+                                                                acc.as<GridAcc>(),
                                                                 touched.as<unsigned>());
         GF_CHECK_LAUNCH();
     }
     se.mark(3, st);
-    k_finalize<T><<<dim3(cdiv(n1, 512), cdiv(n2, kFinRows), n1), 256, 0, st>>>(num.as<double2>(), wsum.as<double>(),
-                                                               ex.as<double2>(), hx.as<uint8_t>(),
+    k_finalize<T><<<dim3(cdiv(n1, 512), cdiv(n2, kFinRows), n1), 256, 0, st>>>(acc.as<GridAcc>(),
                                                                touched.as<unsigned>(), g, n1, n2,
                                                                p.DFT_CentroSymmetricity,
                                                                reinterpret_cast<cplx<T> *>(d_M));
