@@ -10,13 +10,16 @@
 //                    projection's points are in ascending index order, the
 //                    order of find()
 //   4. k_dft         F_j = sum_b E_v(j,b) sum_a E_u(j,a) P(a,b) per point
-//   5. k_accum_runs  the entries (projection-major) sorted stably by grid
+//                    (k_dft_tcgen05 in grid_mma.cu for MIXED / FP16_SCALED)
+//   5. k_fill_grid   the output grid's zero pattern (CentroSymmetricity's
+//                    -0 imaginary parts on the mirrored half)
+//   6. k_accum_runs  the entries (projection-major) sorted stably by grid
 //                    index; each run of one grid point sums its contributions
 //                    in FP64 in projection order and keeps the last exact hit,
 //                    the reference's accumulation order
-//                    (fillInFourierGrid_DFT.m:268-291), in one launch
-//   6. k_finalize    FS = sum(w F) / sum(w), exact override, CentroSymmetricity
-//                    mirror, cast to the output precision
+//                    (fillInFourierGrid_DFT.m:268-291), then writes
+//                    FS = sum(w F) / sum(w) (or the exact hit), cast to the
+//                    output precision, at the point and at its centro mirror
 #include "fft.cuh"
 #include "internal.h"
 
@@ -439,27 +442,49 @@ __global__ void __launch_bounds__(256) k_dft(const T *__restrict__ proj, int D1,
 // ===========================================================================
 // One pass over the entries sorted (stably) by grid index: the first entry of
 // each run sums the run's contributions in their order -- projection order --
-// and keeps the last exact hit, and sets the point's bit in the touched
-// bitmap.  Only touched points get their sums, flag and exact value written;
-// nothing else of the gridded space is cleared or read.
+// keeps the last exact hit and writes the point's final value into the output
+// grid, which k_fill_grid has set to its zero pattern; nothing of the gridded
+// space is stored in between.
 __global__ void k_iota(uint32_t *__restrict__ v, long long n)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         v[i] = (uint32_t)i;
 }
 
-// Per touched point of the gridded space, one 32-byte record (one sector):
-// the FP64 weighted sums, or the last exact hit with the weight field -1.
-struct __align__(32) GridAcc {
-    double x, y;  // sum of w F, or the exact hit's value
-    double w;     // sum of w (> 0), or -1 for an exact hit
-    double pad;
-};
+// The output grid (n1 x n2 x n1, dim 1 fastest) before the touched points are
+// written: zero, with the imaginary part -0 where CentroSymmetricity mirrors
+// (k1 > 0: M(k) = conj(FS(-k)) of an untouched FS(-k) = 0 is (0, -0)), the
+// reference's conj of its zero fill.  Grid: x over pairs of c1 (one 16-byte
+// store for two complex64 when vec: n1 even and M 16-byte aligned, checked by
+// the host), y = c2, z = c3.
+template <typename TO>
+__global__ void __launch_bounds__(256) k_fill_grid(int n1, int n2, int centro, bool vec, cplx<TO> *__restrict__ M)
+{
+    const int c1 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+    if (c1 >= n1) return;
+    cplx<TO> *row = M + (long long)n1 * (blockIdx.y + (long long)n2 * blockIdx.z);
+    const int h = n1 / 2;  // k1 = c1 - h
+    const TO z0 = (centro && c1 > h) ? -(TO)0 : (TO)0, z1 = (centro && c1 + 1 > h) ? -(TO)0 : (TO)0;
+    if (sizeof(TO) == 4 && vec) {
+        *reinterpret_cast<float4 *>(row + c1) = make_float4(0.f, (float)z0, 0.f, (float)z1);
+    } else {
+        row[c1] = mk((TO)0, z0);
+        if (c1 + 1 < n1) row[c1 + 1] = mk((TO)0, z1);
+    }
+}
 
-template <typename T>
+// Each run of one grid point (the entries sorted stably by gridded-space
+// index, projection-major within a run) sums its contributions in FP64 in
+// projection order (fillInFourierGrid_DFT.m:268-291): weight 1/D, except an
+// exact hit (D < 1e-7), the last of which replaces the average.  The point's
+// value is written straight into the output grid: at its own position, and
+// conjugated at -k when CentroSymmetricity mirrors it there (k1 < 0, -k inside
+// the grid).  FP32 output averages in FP32 from the FP64 sums; FP64 output
+// divides in FP64.
+template <typename T, typename TO>
 __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order,
                              const float *__restrict__ dist, const cplx<T> *__restrict__ F, long long n,
-                             GridAcc *__restrict__ acc, unsigned *__restrict__ touched)
+                             GridSpec g, int n1, int n2, int centro, cplx<TO> *__restrict__ M)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const uint32_t li = keys[i];
@@ -481,11 +506,31 @@ __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *
                 w += wgt;
             }
         }
-        // one 32-byte record: the last exact hit (weight field -1) or the
-        // weighted sums (weight sum > 0)
-        double4 *r = reinterpret_cast<double4 *>(acc + li);
-        *r = hit ? make_double4(e.x, e.y, -1.0, 0.0) : make_double4(a.x, a.y, w, 0.0);
-        atomicOr(&touched[li >> 5], 1u << (li & 31));
+        TO x, y;
+        if (hit) {
+            x = (TO)e.x;
+            y = (TO)e.y;
+        } else if constexpr (sizeof(TO) == 8) {
+            x = a.x / w;
+            y = a.y / w;
+        } else {
+            const float ws = (float)w;
+            x = __fdiv_rn((float)a.x, ws);
+            y = __fdiv_rn((float)a.y, ws);
+        }
+        // gridded-space coordinates of li
+        const int k1 = g.lo1 + (int)(li % (uint32_t)g.l1);
+        const uint32_t r = li / (uint32_t)g.l1;
+        const int k2 = g.lo2 + (int)(r % (uint32_t)g.l2), k3 = g.lo3 + (int)(r / (uint32_t)g.l2);
+        const int h1 = n1 / 2, h2 = n2 / 2;
+        auto inside = [&](int a1, int a2, int a3) {
+            return a1 + h1 >= 0 && a1 + h1 < n1 && a2 + h2 >= 0 && a2 + h2 < n2 && a3 + h1 >= 0 && a3 + h1 < n1;
+        };
+        auto at = [&](int a1, int a2, int a3) {
+            return (long long)(a1 + h1) + (long long)n1 * ((a2 + h2) + (long long)n2 * (a3 + h1));
+        };
+        if (inside(k1, k2, k3) && !(centro && k1 > 0)) M[at(k1, k2, k3)] = mk(x, y);
+        if (centro && k1 < 0 && inside(-k1, -k2, -k3)) M[at(-k1, -k2, -k3)] = mk(x, -y);
     }
 }
 
@@ -499,72 +544,6 @@ __device__ __forceinline__ long long src_index(const GridSpec &g, int n1, int n2
     conj = false;
     if (centro && k1 > 0) { k1 = -k1; k2 = -k2; k3 = -k3; conj = true; }
     return (long long)(k1 - g.lo1) + (long long)g.l1 * ((k2 - g.lo2) + (long long)g.l2 * (k3 - g.lo3));
-}
-
-// Grid: x over dim 1 (c1, two points per thread, independent loads), y over
-// groups of kFinRows values of c2, z = c3, so no index has to be decoded.
-// Most of the grid is untouched: each thread reads its points' bits of the
-// touched bitmap (and nothing else) and writes zero where the bit is clear;
-// the touched points of the CTA's rows are gathered into one shared list and
-// then averaged by consecutive threads, so the FP64 divisions of the FP64
-// output (a slow pipe on this part) run in full warps instead of one lane of
-// many warps.  Several rows per CTA keep the CTA count (and the per-CTA
-// setup) small against the bytes written.
-constexpr int kFinRows = 4;
-template <typename TO>
-__global__ void __launch_bounds__(256) k_finalize(const GridAcc *__restrict__ acc,
-                                                  const unsigned *__restrict__ touched, GridSpec g, int n1, int n2,
-                                                  int centro, cplx<TO> *__restrict__ M)
-{
-    constexpr int KPT = 2;  // points per thread and row (independent loads in flight)
-    __shared__ int list[256 * KPT * kFinRows];  // (row in group) << 16 | c1
-    __shared__ int cnt;
-    if (threadIdx.x == 0) cnt = 0;
-    __syncthreads();
-    const int c3 = blockIdx.z;
-    // every bitmap word of the CTA's points is requested before any is used
-    constexpr int NP = KPT * kFinRows;
-    int li[NP];  // gridded-space index (< 2^31)
-    bool cj[NP], in[NP];
-    unsigned tb[NP];
-#pragma unroll
-    for (int k = 0; k < NP; ++k) {
-        const int r = k / KPT, q = k % KPT;
-        const int c2 = blockIdx.y * kFinRows + r;
-        const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
-        in[k] = c1 < n1 && c2 < n2;
-        li[k] = in[k] ? (int)src_index(g, n1, n2, centro, c1, c2, c3, cj[k]) : 0;
-        tb[k] = in[k] ? touched[li[k] >> 5] : 0u;
-    }
-#pragma unroll
-    for (int k = 0; k < NP; ++k) {
-        if (!in[k]) continue;
-        const int r = k / KPT, q = k % KPT;
-        const int c2 = blockIdx.y * kFinRows + r;
-        const int c1 = blockIdx.x * blockDim.x * KPT + q * blockDim.x + threadIdx.x;
-        if ((tb[k] >> (li[k] & 31)) & 1u) list[atomicAdd(&cnt, 1)] = (r << 16) | c1;
-        else M[(long long)n1 * (c2 + (long long)n2 * c3) + c1] = mk((TO)0, cj[k] ? -(TO)0 : (TO)0);
-    }
-    __syncthreads();
-    const int m = cnt;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const int c = list[i] & 0xFFFF, c2 = blockIdx.y * kFinRows + (list[i] >> 16);
-        const long long row = (long long)n1 * (c2 + (long long)n2 * c3);
-        bool cj;
-        const long long li = src_index(g, n1, n2, centro, c, c2, c3, cj);
-        const double4 a = *reinterpret_cast<const double4 *>(acc + li);
-        if (a.z < 0.0) {  // exact hit
-            M[row + c] = mk((TO)a.x, (TO)(cj ? -a.y : a.y));
-        } else if constexpr (sizeof(TO) == 8) {
-            const double vx = a.x / a.z, vy = a.y / a.z;
-            M[row + c] = mk(vx, cj ? -vy : vy);
-        } else {
-            // single-precision output: the average is formed in FP32 from the FP64 sums
-            const float ws = (float)a.z;
-            const float x = __fdiv_rn((float)a.x, ws), y = __fdiv_rn((float)a.y, ws);
-            M[row + c] = mk((TO)x, (TO)(cj ? -y : y));
-        }
-    }
 }
 
 __global__ void k_centro(const double2 *__restrict__ FS, GridSpec g, int n1, int n2, double2 *__restrict__ M)
@@ -799,7 +778,7 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
                        void *d_M, void *d_rec, int64_t *nk_out, double *stage_ms)
 {
     cudaStream_t st = ctx->stream;
-    StageEvents se(8, stage_ms != nullptr);
+    StageEvents se(9, stage_ms != nullptr);
     se.mark(0, st);
     const int D1 = p.Dim1, D2 = p.Dim2, P = p.NumProjs;
     const int n1 = oversampled(D1, p.oversamplingRatio), n2 = oversampled(D2, p.oversamplingRatio);
@@ -844,9 +823,12 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
 
     // weighted average in FP64, projection by projection
     const size_t G = (size_t)g.total;
-    DevBuf acc(sizeof(GridAcc) * G, st);  // written only at touched points
-    DevBuf touched(sizeof(unsigned) * ((G + 31) / 32), st);  // the only array that is cleared
-    GF_CUDA(cudaMemsetAsync(touched.p, 0, touched.bytes, st));
+    // the output grid's zero pattern, then the touched points written over it
+    const bool vec = (n1 % 2 == 0) && (reinterpret_cast<uintptr_t>(d_M) % 16 == 0);
+    k_fill_grid<T><<<dim3(cdiv(n1, 512), n2, n1), 256, 0, st>>>(n1, n2, p.DFT_CentroSymmetricity, vec,
+                                                                reinterpret_cast<cplx<T> *>(d_M));
+    GF_CHECK_LAUNCH();
+    se.mark(8, st);
     if (sel.total > 0) {
         // stable radix sort of (grid index, entry) keeps projection order within a grid point
         const long long n = sel.total;
@@ -861,18 +843,13 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
         DevBuf tmp(std::max<size_t>(tb, 1), st);
         GF_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, sel.ind.as<uint32_t>(), keys.as<uint32_t>(),
                                                 vin.as<uint32_t>(), vout.as<uint32_t>(), n, 0, bits, st));
-        k_accum_runs<T><<<grid_for(ctx, n, 256), 256, 0, st>>>(keys.as<uint32_t>(), vout.as<uint32_t>(),
-                                                                sel.dist.as<float>(), F.as<cplx<T>>(), n,
-                                                                acc.as<GridAcc>(),
-                                                                touched.as<unsigned>());
+        k_accum_runs<T, T><<<grid_for(ctx, n, 256), 256, 0, st>>>(keys.as<uint32_t>(), vout.as<uint32_t>(),
+                                                                   sel.dist.as<float>(), F.as<cplx<T>>(), n, g, n1,
+                                                                   n2, p.DFT_CentroSymmetricity,
+                                                                   reinterpret_cast<cplx<T> *>(d_M));
         GF_CHECK_LAUNCH();
     }
     se.mark(3, st);
-    k_finalize<T><<<dim3(cdiv(n1, 512), cdiv(n2, kFinRows), n1), 256, 0, st>>>(acc.as<GridAcc>(),
-                                                               touched.as<unsigned>(), g, n1, n2,
-                                                               p.DFT_CentroSymmetricity,
-                                                               reinterpret_cast<cplx<T> *>(d_M));
-    GF_CHECK_LAUNCH();
     se.mark(4, st);
     if (d_rec) rec_ifft(ctx, p.precision, d_M, n1, n2, D1, D2, d_rec);
     se.mark(5, st);
@@ -885,8 +862,8 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
         stage_ms[0] = se.ms(0, 1);  // selection
         stage_ms[1] = se.ms(1, 2);  // DFT stage (operand preparation and the DFT kernel)
         stage_ms[2] = dft_kernel_ms;  // the DFT kernel alone
-        stage_ms[3] = se.ms(2, 3);  // weighted sums
-        stage_ms[4] = se.ms(3, 4);  // average, centro mirror, cast
+        stage_ms[3] = se.ms(8, 3);  // sort, weighted sums, average, centro mirror, cast (written into the grid)
+        stage_ms[4] = se.ms(2, 8);  // the output grid's zero pattern
         stage_ms[5] = se.ms(4, 5);  // recIFFT
     }
 }
