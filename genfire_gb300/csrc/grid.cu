@@ -108,6 +108,7 @@ void proj_geometry(const genfire_params &p, double phi, double theta, double psi
     float nn = std::sqrt(g.nrm[0] * g.nrm[0] + g.nrm[1] * g.nrm[1] + g.nrm[2] * g.nrm[2]);
     g.h[0] = g.nrm[0] / nn; g.h[1] = g.nrm[1] / nn; g.h[2] = g.nrm[2] / nn;
     g.nsq = g.nrm[0] * g.nrm[0] + g.nrm[1] * g.nrm[1] + g.nrm[2] * g.nrm[2];
+    g.ih = 1.0f / g.h[0];
     // LU with partial pivoting (first largest pivot), reciprocal column scaling
     float *A = g.lu;
     std::memcpy(A, g.R, sizeof(float) * 9);
@@ -222,9 +223,9 @@ __device__ __forceinline__ bool sel_test(const ProjGeom &g, const SelParams &sp,
 // Candidate k1 range [k1a, k1b] of row (K2, K3): every k1 with
 // |k1 h1 + K2 h2 + K3 h3| below the cutoff, widened by a margin that covers the
 // FP32 rounding of D (|error| < 1e-3 for grids up to 2^16) and of the bounds.
-// ih = 1 / h1 (IEEE division), formed once per projection.
-__device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp, float ih, float K2, float K3,
-                                          int &k1a, int &k1b)
+// g.ih = 1 / h1 (IEEE division), formed once per projection on the host.
+__device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp, float K2, float K3, int &k1a,
+                                          int &k1b)
 {
     const int lo = sp.lo1, hi = sp.lo1 + sp.l1 - 1;
     const float x = -(K2 * g.h[1] + K3 * g.h[2]);
@@ -235,6 +236,7 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
     if (fabsf(h1) >= 0.01f) {
         // bounds through the reciprocal: within a few ulps of the quotients,
         // which the one-point padding below covers
+        const float ih = g.ih;
         float b0 = (x - c) * ih, b1 = (x + c) * ih;
         if (b0 > b1) { const float t = b0; b0 = b1; b1 = t; }
         b0 = fmaxf(b0, (float)lo - 4.f);
@@ -247,39 +249,37 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
     }
 }
 
-// the projection's geometry in shared memory, and 1 / h1
-__device__ __forceinline__ void load_geometry(const ProjGeom *__restrict__ geo, int p, ProjGeom &sg, float &sih)
-{
-    static_assert(sizeof(ProjGeom) % 4 == 0 && sizeof(ProjGeom) / 4 <= kSelThreads, "geometry words");
-    if (threadIdx.x < sizeof(ProjGeom) / 4)
-        reinterpret_cast<uint32_t *>(&sg)[threadIdx.x] = reinterpret_cast<const uint32_t *>(geo + p)[threadIdx.x];
-    __syncthreads();
-    if (threadIdx.x == 0) sih = 1.0f / sg.h[0];
-    __syncthreads();
-}
-
 // Points per row (uint16: a row holds at most l1 <= 32769 points).  Grid:
-// x = 32-row group along i2, y = group of 8 values of i3, z = projection of
-// the batch (p0 + z).
+// x = 32-row group along i2, y = group of 32 values of i3 (each thread takes
+// i3, i3 + 8, i3 + 16, i3 + 24), z = projection of the batch (p0 + z).
+constexpr int kSelI3PerThread = 4;
 __global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__restrict__ geo, int p0, SelParams sp,
                                                           uint16_t *__restrict__ rowcnt)
 {
+    static_assert(sizeof(ProjGeom) % 4 == 0 && sizeof(ProjGeom) / 4 <= kSelThreads, "geometry words");
     __shared__ ProjGeom sg;
-    __shared__ float sih;
-    const int p = p0 + blockIdx.z;
-    load_geometry(geo, p, sg, sih);
+    if (threadIdx.x < sizeof(ProjGeom) / 4)
+        reinterpret_cast<uint32_t *>(&sg)[threadIdx.x] =
+            reinterpret_cast<const uint32_t *>(geo + p0 + blockIdx.z)[threadIdx.x];
+    __syncthreads();
     const int i2 = blockIdx.x * kSelRowsX + (threadIdx.x & (kSelRowsX - 1));
-    const int i3 = blockIdx.y * kSelRowsY + threadIdx.x / kSelRowsX;
-    if (i2 >= sp.l2 || i3 >= sp.l3) return;
-    const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
-    int a0, a1;
-    row_range(sg, sp, sih, K2, K3, a0, a1);
-    int cnt = 0;
-    for (int k1 = a0; k1 <= a1; ++k1) {
-        float D, u, v;
-        cnt += sel_test(sg, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
+    if (i2 >= sp.l2) return;
+    const float K2 = (float)(sp.lo2 + i2);
+    uint16_t *out = rowcnt + (long long)blockIdx.z * sp.nrows + i2;
+#pragma unroll 1
+    for (int it = 0; it < kSelI3PerThread; ++it) {
+        const int i3 = (blockIdx.y * kSelI3PerThread + it) * kSelRowsY + threadIdx.x / kSelRowsX;
+        if (i3 >= sp.l3) break;
+        const float K3 = (float)(sp.lo3 + i3);
+        int a0, a1;
+        row_range(sg, sp, K2, K3, a0, a1);
+        int cnt = 0;
+        for (int k1 = a0; k1 <= a1; ++k1) {
+            float D, u, v;
+            cnt += sel_test(sg, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
+        }
+        out[(long long)sp.l2 * i3] = (uint16_t)cnt;
     }
-    rowcnt[(long long)blockIdx.z * sp.nrows + i2 + (long long)sp.l2 * i3] = (uint16_t)cnt;
 }
 
 // uint32 sum (wraps modulo 2^32) for the offset scan
@@ -322,11 +322,10 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__res
         const uint32_t r = rows[i];  // batch row index: q * nrows + ri
         const int q = (int)(r / (uint32_t)sp.nrows), ri = (int)(r - (uint32_t)q * (uint32_t)sp.nrows);
         const ProjGeom &g = geo[p0 + q];
-        const float ih = 1.0f / g.h[0];
         const int i3 = ri / sp.l2, i2 = ri - i3 * sp.l2;
         const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
         int a0, a1;
-        row_range(g, sp, ih, K2, K3, a0, a1);
+        row_range(g, sp, K2, K3, a0, a1);
         long long o = doff[p0 + q] + (uint32_t)(rowoff[r] - rowoff[(uint32_t)q * (uint32_t)sp.nrows]);
         for (int k1 = a0; k1 <= a1; ++k1) {
             float D, u, v;
@@ -706,7 +705,8 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
         b.off.alloc(sizeof(uint32_t) * nr, st);
         b.rows.alloc(sizeof(uint32_t) * nr, st);
         b.nlisted.alloc(sizeof(int), st);
-        const dim3 grid((unsigned)cdiv(sp.l2, kSelRowsX), (unsigned)cdiv(sp.l3, kSelRowsY), (unsigned)b.np);
+        const dim3 grid((unsigned)cdiv(sp.l2, kSelRowsX), (unsigned)cdiv(sp.l3, kSelRowsY * kSelI3PerThread),
+                        (unsigned)b.np);
         k_sel_count<<<grid, kSelThreads, 0, st>>>(dgeo.as<ProjGeom>(), p0, sp, b.cnt.as<uint16_t>());
         GF_CHECK_LAUNCH();
         const thrust::counting_iterator<uint32_t> ids(0);

@@ -37,6 +37,7 @@ struct ProjGeom {
     float nrm[3];
     float h[3];
     float nsq;
+    float ih;  // 1 / h[0] (IEEE division; used only when |h[0]| >= 0.01)
     float lu[9];
     int piv[3];
 };
