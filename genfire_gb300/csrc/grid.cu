@@ -249,6 +249,12 @@ __device__ __forceinline__ void row_range(const ProjGeom &g, const SelParams &sp
     }
 }
 
+// Rows whose candidate interval is longer than this are shared by the whole
+// warp (lanes take consecutive k1), instead of one lane looping over them:
+// planes nearly parallel to k1 give rows of a few hundred candidates, most of
+// which pass, and one lane per such row left the passes waiting on a tail.
+constexpr int kSelLongRow = 64;
+
 // Points per row (uint16: a row holds at most l1 <= 32769 points).  Grid:
 // x = 32-row group along i2, y = group of 32 values of i3 (each thread takes
 // i3, i3 + 8, i3 + 16, i3 + 24), z = projection of the batch (p0 + z).
@@ -262,23 +268,38 @@ __global__ void __launch_bounds__(kSelThreads) k_sel_count(const ProjGeom *__res
         reinterpret_cast<uint32_t *>(&sg)[threadIdx.x] =
             reinterpret_cast<const uint32_t *>(geo + p0 + blockIdx.z)[threadIdx.x];
     __syncthreads();
-    const int i2 = blockIdx.x * kSelRowsX + (threadIdx.x & (kSelRowsX - 1));
-    if (i2 >= sp.l2) return;
+    const int lane = threadIdx.x & 31;
+    const int i2 = blockIdx.x * kSelRowsX + lane;
+    const bool valid = i2 < sp.l2;  // the warp stays whole for its ballots
     const float K2 = (float)(sp.lo2 + i2);
     uint16_t *out = rowcnt + (long long)blockIdx.z * sp.nrows + i2;
 #pragma unroll 1
     for (int it = 0; it < kSelI3PerThread; ++it) {
-        const int i3 = (blockIdx.y * kSelI3PerThread + it) * kSelRowsY + threadIdx.x / kSelRowsX;
+        const int i3 = (blockIdx.y * kSelI3PerThread + it) * kSelRowsY + threadIdx.x / kSelRowsX;  // warp-uniform
         if (i3 >= sp.l3) break;
         const float K3 = (float)(sp.lo3 + i3);
-        int a0, a1;
-        row_range(sg, sp, K2, K3, a0, a1);
+        int a0 = 1, a1 = 0;
+        if (valid) row_range(sg, sp, K2, K3, a0, a1);
+        const bool longrow = a1 - a0 + 1 > kSelLongRow;
         int cnt = 0;
-        for (int k1 = a0; k1 <= a1; ++k1) {
-            float D, u, v;
-            cnt += sel_test(sg, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
+        if (!longrow)
+            for (int k1 = a0; k1 <= a1; ++k1) {
+                float D, u, v;
+                cnt += sel_test(sg, sp, (float)k1, K2, K3, D, u, v) ? 1 : 0;
+            }
+        for (unsigned lm = __ballot_sync(0xffffffffu, longrow); lm; lm &= lm - 1) {
+            const int src = __ffs(lm) - 1;
+            const int sa0 = __shfl_sync(0xffffffffu, a0, src), sa1 = __shfl_sync(0xffffffffu, a1, src);
+            const float sK2 = __shfl_sync(0xffffffffu, K2, src);
+            int c = 0;
+            for (int k0 = sa0; k0 <= sa1; k0 += 32) {
+                const int k1 = k0 + lane;
+                float D, u, v;
+                c += __popc(__ballot_sync(0xffffffffu, k1 <= sa1 && sel_test(sg, sp, (float)k1, sK2, K3, D, u, v)));
+            }
+            if (lane == src) cnt = c;
         }
-        out[(long long)sp.l2 * i3] = (uint16_t)cnt;
+        if (valid) out[(long long)sp.l2 * i3] = (uint16_t)cnt;
     }
 }
 
@@ -306,36 +327,106 @@ __global__ void k_sel_totals(const uint32_t *__restrict__ rowoff, const uint16_t
     nk[q] = (long long)(uint32_t)(e - b);
 }
 
-// The listed rows (each holds points), a grid-stride loop over the count the
-// list's selection left on the device: the row's points at the projection's
-// first output offset (doff) plus the row's offset within the projection.
+// The row's placement: projection q of the batch, row ri, the candidate
+// interval [a0, a1] and the output offset of its first point.
+struct SelRow {
+    int q, ri, a0, a1;
+    float K2, K3;
+    long long o;
+};
+__device__ __forceinline__ SelRow sel_row(const ProjGeom *__restrict__ geo, int p0, const SelParams &sp, uint32_t r,
+                                          const uint32_t *__restrict__ rowoff, const long long *__restrict__ doff)
+{
+    SelRow w;
+    w.q = (int)(r / (uint32_t)sp.nrows);
+    w.ri = (int)(r - (uint32_t)w.q * (uint32_t)sp.nrows);
+    const int i3 = w.ri / sp.l2, i2 = w.ri - i3 * sp.l2;
+    w.K2 = (float)(sp.lo2 + i2);
+    w.K3 = (float)(sp.lo3 + i3);
+    row_range(geo[p0 + w.q], sp, w.K2, w.K3, w.a0, w.a1);
+    w.o = doff[p0 + w.q] + (uint32_t)(rowoff[r] - rowoff[(uint32_t)w.q * (uint32_t)sp.nrows]);
+    return w;
+}
+
+// The listed rows (each holds points), 32 per warp and step of a grid-stride
+// loop over the count the list's selection left on the device: the row's
+// points at the projection's first output offset (doff) plus the row's offset
+// within the projection, in ascending k1.  Rows with more than kSelLongRow
+// candidates are queued for k_sel_write_long instead: they are consecutive in
+// the list (the rows of planes nearly parallel to k1), and one warp taking 32
+// of them in turn was the pass's tail.
 __global__ void __launch_bounds__(kSelThreads) k_sel_write(const ProjGeom *__restrict__ geo, int p0, SelParams sp,
                                                           const uint32_t *__restrict__ rows,
                                                           const int *__restrict__ nrows_listed,
                                                           const uint32_t *__restrict__ rowoff,
                                                           const long long *__restrict__ doff,
                                                           uint32_t *__restrict__ ind, float *__restrict__ dist,
-                                                          float *__restrict__ uu, float *__restrict__ vv)
+                                                          float *__restrict__ uu, float *__restrict__ vv,
+                                                          uint32_t *__restrict__ longq, int *__restrict__ nlong)
 {
     const int n = *nrows_listed;
-    for (int i = blockIdx.x * kSelThreads + threadIdx.x; i < n; i += gridDim.x * kSelThreads) {
-        const uint32_t r = rows[i];  // batch row index: q * nrows + ri
-        const int q = (int)(r / (uint32_t)sp.nrows), ri = (int)(r - (uint32_t)q * (uint32_t)sp.nrows);
-        const ProjGeom &g = geo[p0 + q];
-        const int i3 = ri / sp.l2, i2 = ri - i3 * sp.l2;
-        const float K2 = (float)(sp.lo2 + i2), K3 = (float)(sp.lo3 + i3);
-        int a0, a1;
-        row_range(g, sp, K2, K3, a0, a1);
-        long long o = doff[p0 + q] + (uint32_t)(rowoff[r] - rowoff[(uint32_t)q * (uint32_t)sp.nrows]);
-        for (int k1 = a0; k1 <= a1; ++k1) {
+    const int lane = threadIdx.x & 31;
+    const long long nwarps = (long long)gridDim.x * (kSelThreads / 32);
+    for (long long base = ((long long)blockIdx.x * (kSelThreads / 32) + (threadIdx.x >> 5)) * 32; base < n;
+         base += nwarps * 32) {
+        const long long i = base + lane;
+        SelRow w{0, 0, 1, 0, 0.f, 0.f, 0};
+        if (i < n) w = sel_row(geo, p0, sp, rows[i], rowoff, doff);
+        const bool longrow = w.a1 - w.a0 + 1 > kSelLongRow;
+        const unsigned lm = __ballot_sync(0xffffffffu, longrow);
+        if (lm) {  // one queue slot per long row, taken by the warp at once
+            int at = 0;
+            if (lane == 0) at = atomicAdd(nlong, __popc(lm));
+            at = __shfl_sync(0xffffffffu, at, 0);
+            if (longrow) longq[at + __popc(lm & ((1u << lane) - 1u))] = rows[i];
+        }
+        if (longrow) continue;
+        const ProjGeom &g = geo[p0 + w.q];
+        long long o = w.o;
+        for (int k1 = w.a0; k1 <= w.a1; ++k1) {
             float D, u, v;
-            if (sel_test(g, sp, (float)k1, K2, K3, D, u, v)) {
-                ind[o] = (uint32_t)((k1 - sp.lo1) + sp.l1 * ri);
+            if (sel_test(g, sp, (float)k1, w.K2, w.K3, D, u, v)) {
+                ind[o] = (uint32_t)((k1 - sp.lo1) + sp.l1 * w.ri);
                 dist[o] = D;
                 uu[o] = u;
                 vv[o] = v;
                 ++o;
             }
+        }
+    }
+}
+
+// The queued long rows, one per warp (grid-stride): lanes test consecutive k1
+// and place their points by the ballot's prefix count, so the row's points
+// stay in ascending k1.
+__global__ void __launch_bounds__(kSelThreads) k_sel_write_long(const ProjGeom *__restrict__ geo, int p0,
+                                                               SelParams sp, const uint32_t *__restrict__ longq,
+                                                               const int *__restrict__ nlong,
+                                                               const uint32_t *__restrict__ rowoff,
+                                                               const long long *__restrict__ doff,
+                                                               uint32_t *__restrict__ ind, float *__restrict__ dist,
+                                                               float *__restrict__ uu, float *__restrict__ vv)
+{
+    const int n = *nlong;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (kSelThreads / 32);
+    for (int j = blockIdx.x * (kSelThreads / 32) + (threadIdx.x >> 5); j < n; j += nwarps) {
+        const SelRow w = sel_row(geo, p0, sp, longq[j], rowoff, doff);
+        const ProjGeom &g = geo[p0 + w.q];
+        long long o = w.o;
+        for (int k0 = w.a0; k0 <= w.a1; k0 += 32) {
+            const int k1 = k0 + lane;
+            float D = 0.f, u = 0.f, v = 0.f;
+            const bool pass = k1 <= w.a1 && sel_test(g, sp, (float)k1, w.K2, w.K3, D, u, v);
+            const unsigned bm = __ballot_sync(0xffffffffu, pass);
+            if (pass) {
+                const long long oo = o + __popc(bm & ((1u << lane) - 1u));
+                ind[oo] = (uint32_t)((k1 - sp.lo1) + sp.l1 * w.ri);
+                dist[oo] = D;
+                uu[oo] = u;
+                vv[oo] = v;
+            }
+            o += __popc(bm);
         }
     }
 }
@@ -738,9 +829,23 @@ static void select_points(genfire_ctx *ctx, const GridSpec &g, double cutoff, in
     sel.dist.alloc(nt * sizeof(float), st);
     sel.u.alloc(nt * sizeof(float), st);
     sel.v.alloc(nt * sizeof(float), st);
-    for (const Batch &b : batches) {
-        k_sel_write<<<(unsigned)(8 * ctx->sm_count), kSelThreads, 0, st>>>(
+    // one full wave of resident CTAs for each grid-stride write pass
+    int per_sm = 0, per_sm_long = 0;
+    GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sel_write, kSelThreads, 0));
+    GF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_long, k_sel_write_long, kSelThreads, 0));
+    const unsigned wgrid = (unsigned)std::max(1, per_sm) * (unsigned)ctx->sm_count;
+    const unsigned lgrid = (unsigned)std::max(1, per_sm_long) * (unsigned)ctx->sm_count;
+    for (Batch &b : batches) {
+        // the long-row queue: at most one entry per row of the batch
+        DevBuf lq(sizeof(uint32_t) * (size_t)b.np * (size_t)nrows, st), nlong(sizeof(int), st);
+        GF_CUDA(cudaMemsetAsync(nlong.p, 0, sizeof(int), st));
+        k_sel_write<<<wgrid, kSelThreads, 0, st>>>(
             dgeo.as<ProjGeom>(), b.p0, sp, b.rows.as<uint32_t>(), b.nlisted.as<int>(), b.off.as<uint32_t>(),
+            sel.doff.as<long long>(), sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
+            sel.v.as<float>(), lq.as<uint32_t>(), nlong.as<int>());
+        GF_CHECK_LAUNCH();
+        k_sel_write_long<<<lgrid, kSelThreads, 0, st>>>(
+            dgeo.as<ProjGeom>(), b.p0, sp, lq.as<uint32_t>(), nlong.as<int>(), b.off.as<uint32_t>(),
             sel.doff.as<long long>(), sel.ind.as<uint32_t>(), sel.dist.as<float>(), sel.u.as<float>(),
             sel.v.as<float>());
         GF_CHECK_LAUNCH();
