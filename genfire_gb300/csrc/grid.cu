@@ -566,7 +566,13 @@ __global__ void __launch_bounds__(256) k_fill_grid(int n1, int n2, int centro, b
 // Each run of one grid point (the entries sorted stably by gridded-space
 // index, projection-major within a run) sums its contributions in FP64 in
 // projection order (fillInFourierGrid_DFT.m:268-291): weight 1/D, except an
-// exact hit (D < 1e-7), the last of which replaces the average.  The point's
+// exact hit (D < 1e-7), the last of which replaces the average.  The FP64 path
+// forms 1/D in FP64; the reduced-precision paths form it in FP32, as the
+// reference forms 1./master_dist in single (:275), and sum in FP64 (the
+// products of FP32 values are exact in FP64), which takes the FP64 division
+// off a pipe that issues 2 operations per clock per SM.  exact_lt is the
+// smallest float not below 1e-7, so dist < exact_lt decides as the double
+// comparison does.  The point's
 // value is written straight into the output grid: at its own position, and
 // conjugated at -k when CentroSymmetricity mirrors it there (k1 < 0, -k inside
 // the grid).  FP32 output averages in FP32 from the FP64 sums; FP64 output
@@ -574,7 +580,7 @@ __global__ void __launch_bounds__(256) k_fill_grid(int n1, int n2, int centro, b
 template <typename T, typename TO>
 __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ order,
                              const float *__restrict__ dist, const cplx<T> *__restrict__ F, long long n,
-                             GridSpec g, int n1, int n2, int centro, cplx<TO> *__restrict__ M)
+                             float exact_lt, GridSpec g, int n1, int n2, int centro, cplx<TO> *__restrict__ M)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const uint32_t li = keys[i];
@@ -584,15 +590,20 @@ __global__ void k_accum_runs(const uint32_t *__restrict__ keys, const uint32_t *
         bool hit = false;
         for (long long t = i; t < n && keys[t] == li; ++t) {
             const uint32_t o = order[t];
-            const double d = (double)dist[o];
+            const float df = dist[o];
             const cplx<T> f = F[o];
-            if (d < 1e-7) {
+            if (df < exact_lt) {
                 e = make_double2((double)f.x, (double)f.y);
                 hit = true;
-            } else {
-                const double wgt = 1.0 / d;
+            } else if constexpr (sizeof(T) == 8) {
+                const double wgt = 1.0 / (double)df;
                 a.x += (double)f.x * wgt;
                 a.y += (double)f.y * wgt;
+                w += wgt;
+            } else {
+                const double wgt = (double)(1.0f / df);
+                a.x = fma((double)f.x, wgt, a.x);
+                a.y = fma((double)f.y, wgt, a.y);
                 w += wgt;
             }
         }
@@ -948,8 +959,11 @@ static void grid_dft_t(genfire_ctx *ctx, const genfire_params &p, const double *
         DevBuf tmp(std::max<size_t>(tb, 1), st);
         GF_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, tb, sel.ind.as<uint32_t>(), keys.as<uint32_t>(),
                                                 vin.as<uint32_t>(), vout.as<uint32_t>(), n, 0, bits, st));
+        float exact_lt = 1e-7f;  // the smallest float not below 1e-7
+        if ((double)exact_lt < 1e-7) exact_lt = std::nextafter(exact_lt, INFINITY);
         k_accum_runs<T, T><<<grid_for(ctx, n, 256), 256, 0, st>>>(keys.as<uint32_t>(), vout.as<uint32_t>(),
-                                                                   sel.dist.as<float>(), F.as<cplx<T>>(), n, g, n1,
+                                                                   sel.dist.as<float>(), F.as<cplx<T>>(), n,
+                                                                   exact_lt, g, n1,
                                                                    n2, p.DFT_CentroSymmetricity,
                                                                    reinterpret_cast<cplx<T> *>(d_M));
         GF_CHECK_LAUNCH();

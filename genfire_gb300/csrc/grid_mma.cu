@@ -1049,16 +1049,34 @@ __global__ void k_sum_parts(const float2 *__restrict__ Fp, int nparts, long long
 
 // uoff[p] = units of the projections before p (uoff[P] = all units), from the
 // points' offsets: a projection with nk points has ceil(nk / tp) tiles per
-// block and nnc * nkr blocks.  One thread: P is small.
-__global__ void k_unit_offsets(const long long *__restrict__ off, int P, int tp, int per_tile,
-                               long long *__restrict__ uoff)
+// block and nnc * nkr blocks.  One CTA of 1024 threads: a block scan per 1024
+// projections with the running total carried.
+__global__ void __launch_bounds__(1024) k_unit_offsets(const long long *__restrict__ off, int P, int tp, int per_tile,
+                                                       long long *__restrict__ uoff)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    long long s = 0;
-    uoff[0] = 0;
-    for (int p = 0; p < P; ++p) {
-        s += (off[p + 1] - off[p] + tp - 1) / tp * per_tile;
-        uoff[p + 1] = s;
+    __shared__ long long wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    long long carry = 0;
+    if (threadIdx.x == 0) uoff[0] = 0;
+    for (int base = 0; base < P; base += 1024) {
+        const int p = base + threadIdx.x;
+        const long long x = p < P ? (off[p + 1] - off[p] + tp - 1) / tp * per_tile : 0;
+        long long inc = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        if (lane == 31) wsum[w] = inc;
+        __syncthreads();
+        long long before = 0, tot = 0;
+        for (int k = 0; k < 32; ++k) {
+            before += k < w ? wsum[k] : 0;
+            tot += wsum[k];
+        }
+        if (p < P) uoff[p + 1] = carry + before + inc;
+        carry += tot;
+        __syncthreads();
     }
 }
 
@@ -1163,7 +1181,7 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     GF_CHECK_LAUNCH();
 
     DevBuf du(sizeof(WsUnit) * (size_t)nunits, st), duoff(sizeof(long long) * (P + 1), st);
-    k_unit_offsets<<<1, 32, 0, st>>>(d_off, P, tp, nparts, duoff.as<long long>());
+    k_unit_offsets<<<1, 1024, 0, st>>>(d_off, P, tp, nparts, duoff.as<long long>());
     GF_CHECK_LAUNCH();
     k_make_units<<<(unsigned)((nunits + 255) / 256), 256, 0, st>>>(d_off, duoff.as<long long>(), P, tp, nnc, nkr,
                                                                    nunits, du.as<WsUnit>());
