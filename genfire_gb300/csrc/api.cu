@@ -189,8 +189,8 @@ genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p, const
         if (recIFFT) dR.alloc(nR, st);
         GF_CUDA(cudaMemcpyAsync(dp.p, projections, sizeof(double) * npj, cudaMemcpyHostToDevice, st));
         gf::grid_dft(ctx, *p, dp.as<double>(), angles, dM.p, recIFFT ? dR.p : nullptr, nk);
-        GF_CUDA(cudaMemcpyAsync(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st));
-        if (recIFFT) GF_CUDA(cudaMemcpyAsync(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st));
+        gf::copy_host(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st);
+        if (recIFFT) gf::copy_host(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st);
         GF_CUDA(cudaStreamSynchronize(st));
     });
 }
@@ -246,8 +246,8 @@ genfire_status genfire_grid_fft(genfire_ctx *ctx, const genfire_params *p, const
         if (recIFFT) dR.alloc(nR, st);
         GF_CUDA(cudaMemcpyAsync(dp.p, projections, sizeof(double) * npj, cudaMemcpyHostToDevice, st));
         gf::grid_fft(ctx, *p, dp.as<double>(), angles, dM.p, recIFFT ? dR.p : nullptr, npairs);
-        GF_CUDA(cudaMemcpyAsync(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st));
-        if (recIFFT) GF_CUDA(cudaMemcpyAsync(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st));
+        gf::copy_host(measuredK, dM.p, nM, cudaMemcpyDeviceToHost, st);
+        if (recIFFT) gf::copy_host(recIFFT, dR.p, nR, cudaMemcpyDeviceToHost, st);
         GF_CUDA(cudaStreamSynchronize(st));
     });
 }

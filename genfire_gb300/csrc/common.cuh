@@ -94,6 +94,29 @@ struct DevBuf {
 };
 
 inline unsigned cdiv(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// A copy between a caller's host buffer and the device.  Buffers of 64 MB and
+// more are page-locked for the copy (cudaHostRegister, undone once the copy
+// has completed), so the copy engines read or write them directly: copies of
+// the 1 GB measured grid from pageable memory ran at 190 GB/s on some GB300
+// boxes and at 8-10 GB/s on others, registration costs 2-5 ms per GB.  When
+// registration fails (memory already registered, read-only or foreign
+// mappings) the plain pageable copy runs.  The call returns with the copy
+// complete.
+constexpr size_t kPinBytes = size_t(64) << 20;
+inline void copy_host(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st)
+{
+    void *host = kind == cudaMemcpyHostToDevice ? const_cast<void *>(src) : dst;
+    bool reg = false;
+    if (bytes >= kPinBytes) {
+        if (cudaHostRegister(host, bytes, cudaHostRegisterDefault) == cudaSuccess) reg = true;
+        else (void)cudaGetLastError();  // clear the registration error: the plain copy follows
+    }
+    const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, st);
+    const cudaError_t es = e == cudaSuccess ? cudaStreamSynchronize(st) : e;
+    if (reg) cudaHostUnregister(host);
+    GF_CUDA(es);
+}
 inline int floordiv2(int n) { return n / 2; }
 inline int imod(long long a, long long n) { long long r = a % n; return (int)(r < 0 ? r + n : r); }
 

@@ -1039,10 +1039,12 @@ template <typename T> struct ReconT : ReconBase {
 
         // measured data on the device
         M.alloc(sizeof(cplx<T>) * N, st);
-        GF_CUDA(cudaMemcpyAsync(M.p, Min, sizeof(cplx<T>) * N, kind, st));
+        if (on_device) GF_CUDA(cudaMemcpyAsync(M.p, Min, sizeof(cplx<T>) * N, kind, st));
+        else copy_host(M.p, Min, sizeof(cplx<T>) * N, kind, st);
         if (maskin) {
             mask.alloc(N, st);
-            GF_CUDA(cudaMemcpyAsync(mask.p, maskin, N, kind, st));
+            if (on_device) GF_CUDA(cudaMemcpyAsync(mask.p, maskin, N, kind, st));
+            else copy_host(mask.p, maskin, N, kind, st);
         }
         // constraint table
         TabGeom g;
