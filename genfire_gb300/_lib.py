@@ -234,12 +234,14 @@ class Context:
         return nk
 
     def grid_profile(self, p, d_proj_ptr, angles, d_M_ptr):
-        """Device ms of the gridding stages: selection, DFT stage, DFT kernel, sums, finalize, recIFFT."""
+        """Device ms of the gridding stages: selection, DFT stage, DFT kernel, sums (sort, weighted sums,
+        average, centro mirror, cast, written into measuredK), zero_fill (measuredK's zero pattern),
+        recIFFT."""
         A = fortran(angles, np.float64)
         ms = np.zeros(6)
         self.check(load().genfire_grid_profile(self._h, C.byref(p), C.c_void_p(d_proj_ptr), ptr(A, C.c_double),
                                                C.c_void_p(d_M_ptr), ptr(ms, C.c_double)))
-        return dict(zip(("selection", "dft_stage", "dft_kernel", "sums", "finalize", "rec_ifft"), ms.tolist()))
+        return dict(zip(("selection", "dft_stage", "dft_kernel", "sums", "zero_fill", "rec_ifft"), ms.tolist()))
 
     def grid_fft(self, p, projections, angles, want_rec=True):
         """fillInFourierGrid (griddingMethod 1): (measuredK m^3, recIFFT or None, gridded pairs)."""

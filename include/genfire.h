@@ -131,7 +131,11 @@ void *genfire_stream(genfire_ctx *ctx);
  *                MIXED; NULL to skip
  *   nk           NumProjs counts of gridded K-points per projection; NULL ok
  * Index sets are bit-exact with the FP32 selection of the reference
- * (:175-192) evaluated with a fixed operation order. */
+ * (:175-192) evaluated with a fixed operation order.  Host buffers of 64 MB
+ * and more (measuredK, recIFFT here; measuredK and measuredK_mask in
+ * genfire_reconstruct and a host genfire_recon_create) are page-locked with
+ * cudaHostRegister for the duration of their copy and released before the
+ * call returns; when registration fails the copy runs from pageable memory. */
 genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p,
                                 const double *projections, const double *angles,
                                 void *measuredK, void *recIFFT, int64_t *nk);
@@ -143,8 +147,9 @@ genfire_status genfire_grid_dft_device(genfire_ctx *ctx, const genfire_params *p
  * stages from CUDA events on the context stream (tracing; the reference
  * prints only the total, fillInFourierGrid_DFT.m:306-308): stage_ms[0]
  * K-point selection, [1] DFT stage (operand preparation and the DFT kernel),
- * [2] the DFT kernel alone, [3] weighted sums, [4] average, centro mirror and
- * cast, [5] recIFFT (0 here). */
+ * [2] the DFT kernel alone, [3] sort, weighted sums, average, centro mirror
+ * and cast (written into measuredK), [4] measuredK's zero pattern, [5]
+ * recIFFT (0 here). */
 genfire_status genfire_grid_profile(genfire_ctx *ctx, const genfire_params *p, const double *d_projections,
                                     const double *angles, void *d_measuredK, double *stage_ms);
 
