@@ -133,3 +133,39 @@ def test_reconstruct_rejects_bad_mode(lib, ctx):
     with pytest.raises(lib.GenfireError) as e:
         ctx.reconstruct(params(lib, 8, 8, 1, oversamplingRatio=2, constraintEnforcementMode=4), M)
     assert e.value.status == 1 and "not understood" in str(e.value)
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_large_host_buffers_page_locked_or_not(lib, ctx, pinned):
+    """Host buffers of 64 MB and more are page-locked for their copy (cudaHostRegister,
+    released before the call returns); a buffer the caller has already page-locked
+    makes the registration fail and the copy runs as given.  Both give the results
+    of the same data copied from device memory: a 128^3 object on a 256^3 grid
+    (the complex64 measured grid is 134 MB)."""
+    torch = pytest.importorskip("torch")
+    D, os_ = 128, 2.0
+    rng = np.random.default_rng(11)
+    n = 256
+    M = np.zeros((n, n, n), np.complex64, order="F")
+    idx = rng.integers(0, n, size=(3, 20000))
+    M[idx[0], idx[1], idx[2]] = (rng.standard_normal(20000) + 1j * rng.standard_normal(20000)).astype(np.complex64)
+    M = np.asfortranarray(M)
+    p = params(lib, D, D, 1, oversamplingRatio=os_, numIterations=3, constraintEnforcementMode=1,
+               precision="mixed")
+    d_M = torch.from_numpy(M.reshape(-1, order="F").view(np.float32)).cuda()
+    r = ctx.recon(p, d_M.data_ptr(), on_device=True)
+    r.iterate(3)
+    ref, errK_ref, _, _, _ = r.result()
+    r.close()
+    if pinned:
+        t = torch.empty(M.size * 2, dtype=torch.float32, pin_memory=True)
+        host = t.numpy().view(np.complex64).reshape(M.shape, order="F")
+        host[...] = M
+    else:
+        host = M
+    assert host.nbytes >= 64 << 20
+    rec, errK, _, _, _ = ctx.reconstruct(p, host)
+    assert np.array_equal(rec, ref) and np.array_equal(errK, errK_ref)
+    # the caller's buffer is left as it was: registrable again (not left page-locked by the call)
+    rec2, _, _, _, _ = ctx.reconstruct(p, host)
+    assert np.array_equal(rec2, ref)
