@@ -908,6 +908,20 @@ void rfree_candidates(genfire_ctx *ctx, const genfire_params &p, const void *M, 
 
 // Object in box coordinates from an initial object (D1 x D2 x D1) or zeros.
 // grid: x over e1, y = e2, z = e3
+// Row mask of the radix-32 row passes: mask[b] = 1 when one of rows
+// [rows_per_cta b, rows_per_cta (b + 1)) of the box-shaped support holds a
+// voxel.  One CTA per entry.
+__global__ void __launch_bounds__(256) k_row_support_mask(const uint8_t *__restrict__ S, int B1, int nrows,
+                                                          int rows_per_cta, uint8_t *__restrict__ mask)
+{
+    const long long r0 = (long long)blockIdx.x * rows_per_cta;
+    const long long r1 = min((long long)nrows, r0 + rows_per_cta);
+    int any = 0;
+    for (long long e = r0 * B1 + threadIdx.x; e < r1 * B1; e += 256) any |= S[e];
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) mask[blockIdx.x] = any ? 1 : 0;
+}
+
 template <typename T>
 __global__ void k_place(const T *__restrict__ init, int D1, int D2, int B1, int B2, int B3, T *__restrict__ x)
 {
@@ -974,6 +988,7 @@ template <typename T> struct ReconT : ReconBase {
     FftPlan pl1, pl2;
     const cplx<T> *tw1, *tw2;
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
+    DevBuf rowmask;  // per CTA of the radix-32 row passes: any support voxel in its rows
     DevBuf rtab, rtaboff, rcap, rvals, rshoff, rhist;  // Rfree monitor
     DevBuf errf;  // set by a pass whose bounded device-side wait expired
     int m = 0, nparts = 0, tiles1 = 0, ntab = 0, nshells = 0;
@@ -1110,6 +1125,17 @@ template <typename T> struct ReconT : ReconBase {
             S.alloc(ns, st);
             if (support) GF_CUDA(cudaMemcpyAsync(S.p, support, ns, kind, st));
             else GF_CUDA(cudaMemsetAsync(S.p, 1, ns, st));
+            // the radix-32 row passes' CTAs (W row pairs each) that hold no
+            // support voxel; the object buffers are finite everywhere (the
+            // placement and the clear above), so rows the passes skip stay finite
+            if (sizeof(T) == 4 && (n1 == 512 || n1 == 1024) && rows_r32_enabled() && support) {
+                const int rows_per_cta = 2 * (n1 == 512 ? R32<512>::W : R32<1024>::W);
+                const int nrow = B2 * B3, ncta = (int)cdiv((nrow + 1) / 2, rows_per_cta / 2);
+                rowmask.alloc(ncta, st);
+                k_row_support_mask<<<ncta, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, rows_per_cta,
+                                                         rowmask.as<uint8_t>());
+                GF_CHECK_LAUNCH();
+            }
         }
         Y1.alloc(sizeof(cplx<T>) * (size_t)ld1 * B2 * B3, st);
         Y2.alloc(sizeof(cplx<T>) * (size_t)ld1 * n2 * B3, st);
@@ -1223,6 +1249,7 @@ template <typename T> struct ReconT : ReconBase {
         r.ctl = c;
         r.changes = changes.as<int>();
         r.support = p.constraintSupport ? S.as<uint8_t>() : nullptr;
+        r.rowmask = rowmask.as<uint8_t>();  // nullptr when not built
         r.positivity = p.constraintPositivity;
         r.Y = Y1.as<cplx<T>>();
         r.scale = (T)1;
@@ -1245,6 +1272,9 @@ template <typename T> struct ReconT : ReconBase {
         q.ctl = nullptr;
         q.changes = nullptr;
         q.support = nullptr;
+        // the R-factor monitor projects this pass's raw output, so with it on
+        // every row is written
+        q.rowmask = p.monitor_R == 1 ? nullptr : rowmask.as<uint8_t>();
         q.positivity = 0;
         q.scale = (T)(1.0 / ((double)n1 * n2 * n1));
         launch_rows<T>(q, false, st);

@@ -582,6 +582,10 @@ template <typename T> struct RowPassArgs {
     T *xs[2];
     const int *xsel;
     const uint8_t *support;  // box-shaped support mask, nullptr for none
+    // radix-32 row passes: per CTA, nonzero when one of its rows holds a
+    // support voxel; F1 writes zero half spectra for the other CTAs and I1
+    // skips them (nullptr: every CTA works)
+    const uint8_t *rowmask;
     int positivity;
     cplx<T> *Y;        // ld1 x nrows half spectrum
     T scale;           // inverse only
