@@ -989,6 +989,7 @@ template <typename T> struct ReconT : ReconBase {
     const cplx<T> *tw1, *tw2;
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
     DevBuf rowmask;  // per CTA of the radix-32 row passes: any support voxel in its rows
+    DevBuf zmask;    // per slab of the box along dim 3: any support voxel in it
     DevBuf rtab, rtaboff, rcap, rvals, rshoff, rhist;  // Rfree monitor
     DevBuf errf;  // set by a pass whose bounded device-side wait expired
     int m = 0, nparts = 0, tiles1 = 0, ntab = 0, nshells = 0;
@@ -1135,6 +1136,10 @@ template <typename T> struct ReconT : ReconBase {
                 k_row_support_mask<<<ncta, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, rows_per_cta,
                                                          rowmask.as<uint8_t>());
                 GF_CHECK_LAUNCH();
+                // slabs along dim 3 (the dim-2 passes' `other`): B2 rows each
+                zmask.alloc(B3, st);
+                k_row_support_mask<<<B3, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, B2, zmask.as<uint8_t>());
+                GF_CHECK_LAUNCH();
             }
         }
         Y1.alloc(sizeof(cplx<T>) * (size_t)ld1 * B2 * B3, st);
@@ -1181,6 +1186,8 @@ template <typename T> struct ReconT : ReconBase {
         a.in = Y1.as<cplx<T>>(); a.in_dim = ld1; a.in_other = (long long)ld1 * B2; a.in_cnt = B2; a.in_c = B2 / 2;
         a.out = Y2.as<cplx<T>>(); a.out_dim = ld1; a.out_other = (long long)ld1 * n2; a.out_cnt = n2; a.out_c = 0;
         a.mode = 1;
+        a.zmask = zmask.as<uint8_t>();  // zero slabs stay zero (nullptr when not built)
+        a.zmask_zero = 1;
         return a;
     }
     // F3: dim 3 forward, constraint, dim 3 inverse (in place)
@@ -1209,6 +1216,11 @@ template <typename T> struct ReconT : ReconBase {
         d.in = Y2.as<cplx<T>>(); d.in_dim = ld1; d.in_other = (long long)ld1 * n2; d.in_cnt = n2; d.in_c = 0;
         d.out = Y1.as<cplx<T>>(); d.out_dim = ld1; d.out_other = (long long)ld1 * B2; d.out_cnt = B2; d.out_c = B2 / 2;
         d.mode = 2;
+        // slabs without support voxels: their rows are skipped by I1 and masked
+        // by the next F1, so they are not transformed back; with the R-factor
+        // monitor on, I1 writes every row and reads them all
+        d.zmask = p.monitor_R == 1 ? nullptr : zmask.as<uint8_t>();
+        d.zmask_zero = 0;
         if (with_ctl) {
             d.ctl = ctl.as<Ctl>();
             d.partial = partial.as<double>();

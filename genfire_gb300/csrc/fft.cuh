@@ -447,6 +447,13 @@ template <typename T> struct ColPassArgs {
     cplx<T> *rcap;
     // set to 1 by a pass whose bounded device-side wait expired (NULL: none)
     int *err;
+    // radix-32 column passes: per value of `other`, nonzero when that slab of
+    // the box holds a support voxel.  For the other slabs a forward pass whose
+    // input there is zero (zmask_zero = 1) writes zeros without transforming,
+    // and an inverse pass whose output there is never read (zmask_zero = 0)
+    // does nothing (nullptr: every CTA works)
+    const uint8_t *zmask;
+    int zmask_zero;
 };
 
 // Copy of the withheld (Rfree) points of one tile of F3, read before the

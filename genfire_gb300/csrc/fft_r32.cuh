@@ -289,6 +289,19 @@ __global__ void __launch_bounds__(R32<N>::THREADS, r32_col_min_blocks(N)) k_col_
     const int tile = blockIdx.x, other = blockIdx.y;
     const int col = tile * W + c;
     const bool cv = col < a.ncols;
+    if (a.zmask && !a.zmask[other]) {
+        // a slab without support voxels (see ColPassArgs::zmask)
+        if (a.zmask_zero && cv) {
+            cplx<T> *out = a.out + (long long)other * a.out_other + (long long)col * a.col_stride;
+#pragma unroll 4
+            for (int m = 0; m < 32; ++m) {
+                int e = t + P * m + a.out_c;
+                if (e >= N) e -= N;
+                if (e < a.out_cnt) out[(unsigned)e * (unsigned)a.out_dim] = mk((T)0, (T)0);
+            }
+        }
+        return;
+    }
     const cplx<T> *twp = a.tw;  // twiddles<T>(N): see R32<N>::TWT
     cplx<T> x[32];
     if constexpr (r32_prefetch_ahead(N, ZIN && ZOUT) > 0) {
