@@ -990,6 +990,7 @@ template <typename T> struct ReconT : ReconBase {
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
     DevBuf rowmask;  // per CTA of the radix-32 row passes: any support voxel in its rows
     DevBuf zmask;    // per slab of the box along dim 3: any support voxel in it
+    double frac_rows = 1.0, frac_slabs = 1.0;  // the shares of those masks that are set
     DevBuf rtab, rtaboff, rcap, rvals, rshoff, rhist;  // Rfree monitor
     DevBuf errf;  // set by a pass whose bounded device-side wait expired
     int m = 0, nparts = 0, tiles1 = 0, ntab = 0, nshells = 0;
@@ -1140,6 +1141,13 @@ template <typename T> struct ReconT : ReconBase {
                 zmask.alloc(B3, st);
                 k_row_support_mask<<<B3, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, B2, zmask.as<uint8_t>());
                 GF_CHECK_LAUNCH();
+                // the shares of set entries, for the passes' byte counts (profile)
+                std::vector<uint8_t> hr(ncta), hz(B3);
+                GF_CUDA(cudaMemcpyAsync(hr.data(), rowmask.p, ncta, cudaMemcpyDeviceToHost, st));
+                GF_CUDA(cudaMemcpyAsync(hz.data(), zmask.p, B3, cudaMemcpyDeviceToHost, st));
+                GF_CUDA(cudaStreamSynchronize(st));
+                frac_rows = (double)std::count(hr.begin(), hr.end(), (uint8_t)1) / ncta;
+                frac_slabs = (double)std::count(hz.begin(), hz.end(), (uint8_t)1) / B3;
             }
         }
         Y1.alloc(sizeof(cplx<T>) * (size_t)ld1 * B2 * B3, st);
@@ -1299,12 +1307,16 @@ template <typename T> struct ReconT : ReconBase {
         const double S = sizeof(cplx<T>), Rs = sizeof(T);
         const double box = (double)B1 * B2 * B3;
         const double half_box = (double)h1 * B2 * B3, half_mid = (double)h1 * n2 * B3;
-        b[0] = box * Rs + (p.constraintSupport ? box : 0.0) + half_box * S;
-        b[1] = half_box * S + half_mid * S;
+        // with the support masks the row and dim-2 passes move only the rows
+        // and slabs that hold support voxels (F1 and F2 still write every zero)
+        const bool skip = p.monitor_R != 1;
+        const double fr = frac_rows, fz = frac_slabs;
+        b[0] = (box * Rs + (p.constraintSupport ? box : 0.0)) * fr + half_box * S;
+        b[1] = half_box * S * fz + half_mid * S;
         b[2] = 2 * half_mid * S + ntab * (double)sizeof(TabEntry<T>) + (h1 * (double)n2 + 1) * 4 + nparts * 8.0;
         if (nshells > 0) b[2] += nrfree * (8.0 + 3 * S) + (h1 * (double)n2 + 1) * 4;
-        b[3] = half_mid * S + half_box * S + nparts * 8.0;
-        b[4] = half_box * S + box * Rs;
+        b[3] = (half_mid * S + half_box * S) * (skip ? fz : 1.0) + nparts * 8.0;
+        b[4] = (half_box * S + box * Rs) * (skip ? fr : 1.0);
     }
 
     void profile(int count, double *ms, double *bytes) override
