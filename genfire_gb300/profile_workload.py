@@ -4,7 +4,7 @@ object of 2000 Gaussian atoms, 90 random-Euler projections of 256 x 256
 positivity and the ellipsoid support.
 
     python -m genfire_gb300.profile_workload grid [calls] [mixed|fp16]
-        fillInFourierGrid_DFT calls (selection, tensor-core DFT, sums, finalize)
+        fillInFourierGrid_DFT calls (selection, tensor-core DFT, zero fill, sums)
     python -m genfire_gb300.profile_workload iterate [iterations]
         the constraint table of the MIXED grid, then iterations (F1 F2 F3 I2 I1)
     python -m genfire_gb300.profile_workload project [calls]
