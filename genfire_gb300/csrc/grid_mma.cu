@@ -411,6 +411,10 @@ struct WsArgs {
     int D1, D2, D1p, D2p;     // D1p: D1 rounded up to 32; D2p: D2 rounded up to 16
     int n1, n2, log2n1, log2n2;
     int nnc, nkr;
+    // first form, one K block of D1 = 64 H rows: K runs a = 0 .. 32H-1 (chunks
+    // 0 .. H-1) then a = -1 .. -32H (chunks H .. 2H-1), consumed as the pairs
+    // (p, H + p); 0 for the natural order
+    int mirror;
     int *err;                 // set to 1 when a bounded wait expired
     long long wait_cycles;    // limit of the pipeline's waits (the drain always allows kWaitCycles)
 };
@@ -498,7 +502,9 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t a_base = saddr(sA + s * kAStage), b_base = saddr(sB + kc * kBChunk);
+                    // the B chunk of this A chunk (pairs (p, H + p) in the mirrored order)
+                    const int bc = a.mirror ? ((kc & 1) ? a.mirror + (kc >> 1) : (kc >> 1)) : kc;
+                    const uint32_t a_base = saddr(sA + s * kAStage), b_base = saddr(sB + bc * kBChunk);
 #pragma unroll
                     for (int ks = 0; ks < 2; ++ks) {
                         const uint32_t ko = ks * 16 * 16;  // 16 k = two core matrices = 256 bytes
@@ -548,28 +554,17 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
             const f2x_t w8x = pk(w8.x, w8.x), w8y = pk(w8.y, w8.y), w8n = pk(-w8.y, -w8.y);
             const f2x_t wcx = pk(w12.x, w12.x), wcy = pk(w12.y, w12.y), wcn = pk(-w12.y, -w12.y);
             float2 anchor = make_float2(0.f, 0.f);
-            for (int kc = 0; kc < nkc; ++kc, ++g) {
-                const int s = (int)(g % kStages);
-                if (g >= (uint32_t)kStages && !ws_wait(&aempty[s], ((g / kStages) - 1) & 1, lim, abort_flag)) {
-                    ok = false;
-                    break;
-                }
-                // 16 consecutive k of row r: a = amin + kr*256 + kc*32 + 16h + 0..15.  The
-                // anchor E_u(a) is exact every 4 chunks and one rotation by 32 from the
-                // previous chunk's otherwise.  The values are held as 8 pairs (2p, 2p+1),
-                // each pair's real parts and imaginary parts packed: pair 0 from the
-                // anchor, pairs 2, 4, 6 rotated from it by 4, 8, 12 and every odd pair
-                // from the one before it by 2 (four independent chains of packed
-                // rotations, at most three rotations from the anchor)
-                if ((kc & 3) == 0)
-                    anchor = row_ok ? phase_any<POW2>(amin + kKR * kr + kKC * kc + 16 * h, uj, a.log2n1, inv1)
-                                    : make_float2(0.f, 0.f);
-                else
-                    anchor = cmulf(anchor, w32);
-                const float2 e1 = cmulf(anchor, w1);
+            // 16 consecutive k of row r from an anchor E_u(a): 8 pairs (2p, 2p+1), each
+            // pair's real parts and imaginary parts packed: pair 0 from the anchor,
+            // pairs 2, 4, 6 rotated from it by 4, 8, 12 and every odd pair from the one
+            // before it by 2 (four independent chains of packed rotations, at most
+            // three rotations from the anchor), split into hi/lo words
+            uint32_t rh[9], rl[9], ih[9], il[9];
+            auto gen = [&](float2 anc) {
+                const float2 e1 = cmulf(anc, w1);
                 f2x_t X[8], Y[8];
-                X[0] = pk(anchor.x, e1.x);
-                Y[0] = pk(anchor.y, e1.y);
+                X[0] = pk(anc.x, e1.x);
+                Y[0] = pk(anc.y, e1.y);
                 X[2] = X[0]; Y[2] = Y[0]; rot_x2(X[2], Y[2], w4x, w4y, w4n);
                 X[4] = X[0]; Y[4] = Y[0]; rot_x2(X[4], Y[4], w8x, w8y, w8n);
                 X[6] = X[0]; Y[6] = Y[0]; rot_x2(X[6], Y[6], wcx, wcy, wcn);
@@ -579,24 +574,79 @@ __global__ void __launch_bounds__(umma::kWsThreads, 1) k_dft_tcgen05(WsArgs a)
                     Y[m + 1] = Y[m];
                     rot_x2(X[m + 1], Y[m + 1], w2x, w2y, w2n);
                 }
-                uint32_t rh[8], rl[8], ih[8], il[8];
 #pragma unroll
                 for (int m = 0; m < 8; ++m) {
                     split_x2<F16>(X[m], rh[m], rl[m]);
                     split_x2<F16>(Y[m], ih[m], il[m]);
                 }
-                uint16_t *As = reinterpret_cast<uint16_t *>(sA + s * kAStage);
+                // the 17th value, E_u(a + 16) = E_u(a + 15) E_u(1), in the low halves
+                const float2 v15 = make_float2(upk(X[7]).y, upk(Y[7]).y);
+                const float2 v16 = cmulf(v15, w1);
+                split_x2<F16>(pk(v16.x, 0.f), rh[8], rl[8]);
+                split_x2<F16>(pk(v16.y, 0.f), ih[8], il[8]);
+            };
+            // the next A stage, once the MMAs that read it last have completed
+            auto acquire = [&](int &st) -> bool {
+                st = (int)(g % kStages);
+                return g < (uint32_t)kStages || ws_wait(&aempty[st], ((g / kStages) - 1) & 1, lim, abort_flag);
+            };
+            auto store = [&](int st, const uint32_t *wrh, const uint32_t *wrl, const uint32_t *wih, const uint32_t *wil) {
+                uint16_t *As = reinterpret_cast<uint16_t *>(sA + st * kAStage);
 #pragma unroll
                 for (int c8 = 0; c8 < 2; ++c8) {
                     const int idx = kmaj_index(r, 16 * h + 8 * c8);  // one 16-byte core-matrix row
                     const int k0 = 4 * c8;
-                    *reinterpret_cast<uint4 *>(As + 0 * (kABytes / 2) + idx) = make_uint4(rh[k0], rh[k0 + 1], rh[k0 + 2], rh[k0 + 3]);
-                    *reinterpret_cast<uint4 *>(As + 1 * (kABytes / 2) + idx) = make_uint4(rl[k0], rl[k0 + 1], rl[k0 + 2], rl[k0 + 3]);
-                    *reinterpret_cast<uint4 *>(As + 2 * (kABytes / 2) + idx) = make_uint4(ih[k0], ih[k0 + 1], ih[k0 + 2], ih[k0 + 3]);
-                    *reinterpret_cast<uint4 *>(As + 3 * (kABytes / 2) + idx) = make_uint4(il[k0], il[k0 + 1], il[k0 + 2], il[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 0 * (kABytes / 2) + idx) = make_uint4(wrh[k0], wrh[k0 + 1], wrh[k0 + 2], wrh[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 1 * (kABytes / 2) + idx) = make_uint4(wrl[k0], wrl[k0 + 1], wrl[k0 + 2], wrl[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 2 * (kABytes / 2) + idx) = make_uint4(wih[k0], wih[k0 + 1], wih[k0 + 2], wih[k0 + 3]);
+                    *reinterpret_cast<uint4 *>(As + 3 * (kABytes / 2) + idx) = make_uint4(wil[k0], wil[k0 + 1], wil[k0 + 2], wil[k0 + 3]);
                 }
                 fence_proxy_async();  // the stores are visible to the tensor core
-                mbar_arrive(&afull[s]);
+                mbar_arrive(&afull[st]);
+                ++g;
+            };
+            if (a.mirror) {
+                // K as a = 0 .. 32H-1, then a = -1 .. -32H: the chunk pair (p, H + p).
+                // The negative chunk's element k holds E_u(-(32p + k) - 1) =
+                // conj E_u(32p + k + 1): this thread's values shifted by one (its 17th
+                // value closes the row), the words re-paired by a byte permute and the
+                // imaginary parts negated by their sign bits (the hi/lo split of -x is
+                // -hi, -lo).  The anchor E_u(32p + 16h) is exact every 4 pairs.
+                for (int pp = 0; pp < nkc / 2; ++pp) {
+                    if ((pp & 3) == 0)
+                        anchor = row_ok ? phase_any<POW2>(kKC * pp + 16 * h, uj, a.log2n1, inv1) : make_float2(0.f, 0.f);
+                    else
+                        anchor = cmulf(anchor, w32);
+                    gen(anchor);
+                    int st;
+                    if (!acquire(st)) { ok = false; break; }
+                    store(st, rh, rl, ih, il);
+                    uint32_t nrh[8], nrl[8], nih[8], nil[8];
+#pragma unroll
+                    for (int m = 0; m < 8; ++m) {
+                        nrh[m] = __byte_perm(rh[m], rh[m + 1], 0x5432);
+                        nrl[m] = __byte_perm(rl[m], rl[m + 1], 0x5432);
+                        nih[m] = __byte_perm(ih[m], ih[m + 1], 0x5432) ^ 0x80008000u;
+                        nil[m] = __byte_perm(il[m], il[m + 1], 0x5432) ^ 0x80008000u;
+                    }
+                    if (!acquire(st)) { ok = false; break; }
+                    store(st, nrh, nrl, nih, nil);
+                }
+            } else {
+                for (int kc = 0; kc < nkc; ++kc) {
+                    // 16 consecutive k of row r: a = amin + kr*256 + kc*32 + 16h + 0..15; the
+                    // anchor E_u(a) is exact every 4 chunks and one rotation by 32 from the
+                    // previous chunk's otherwise
+                    if ((kc & 3) == 0)
+                        anchor = row_ok ? phase_any<POW2>(amin + kKR * kr + kKC * kc + 16 * h, uj, a.log2n1, inv1)
+                                        : make_float2(0.f, 0.f);
+                    else
+                        anchor = cmulf(anchor, w32);
+                    gen(anchor);
+                    int st;
+                    if (!acquire(st)) { ok = false; break; }
+                    store(st, rh, rl, ih, il);
+                }
             }
         }
     } else {
@@ -1005,7 +1055,7 @@ __global__ void __launch_bounds__(256) k_proj_scale(const double *__restrict__ p
 // Grid: x = block, y = K chunk.
 template <bool F16, int NB, int KR>
 __global__ void __launch_bounds__(256) k_split_projections(const double *__restrict__ proj, int D1, int D2, int nnc,
-                                                           int nkr, const float *__restrict__ scale,
+                                                           int nkr, int mirror_m, const float *__restrict__ scale,
                                                            uint16_t *__restrict__ B)
 {
     using namespace umma;
@@ -1019,8 +1069,13 @@ __global__ void __launch_bounds__(256) k_split_projections(const double *__restr
     for (int e = threadIdx.x; e < kArr; e += 256) {
         // e is the linear position in the layout: invert kmaj_index
         const int rg = e >> 8, kg = (e >> 6) & 3, rr = (e >> 3) & 7, kk = e & 7;
-        const int b = nc * NB + rg * 8 + rr, aa = kr * KR + kc * kKC + kg * 8 + kk;
-        const float xf = (b < D2 && aa < D1) ? (float)src[aa + (long long)D1 * b] * sc : 0.f;
+        // K row: natural (aa = a + D1/2), or with mirror_m = D1/2 the order
+        // a = 0 .. m-1 then a = -1 .. -m (see WsArgs::mirror)
+        const int kabs = kc * kKC + kg * 8 + kk;
+        const int b = nc * NB + rg * 8 + rr;
+        const int aa = mirror_m ? (kabs < mirror_m ? kabs + mirror_m : 2 * mirror_m - 1 - kabs) : kr * KR + kabs;
+        // rows outside 0 .. D1-1 (the block's padding, in either order) are zero
+        const float xf = (b < D2 && aa >= 0 && aa < D1) ? (float)src[aa + (long long)D1 * b] * sc : 0.f;
         if constexpr (F16) {
             const __half hi = __float2half_rn(xf);
             dst[e] = __half_as_ushort(hi);
@@ -1135,6 +1190,14 @@ static bool dft_use_wide()
     return e && std::strcmp(e, "n256") == 0;
 }
 
+// The first form's mirrored K order (WsArgs::mirror) where the shape allows it;
+// GENFIRE_DFT_MIRROR=0 keeps the natural order.
+static bool dft_mirror_enabled()
+{
+    const char *e = std::getenv("GENFIRE_DFT_MIRROR");
+    return !(e && e[0] == '0');
+}
+
 // Host: F (float2, one per selected point) for all projections.  Everything is
 // enqueued on the context stream without a host synchronisation: the unit list
 // and the scales are made on the device, and the error flag is the caller's to
@@ -1169,14 +1232,17 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
         k_fill_f32<<<(2 * P + 255) / 256, 256, 0, st>>>(d_scale, 2 * P, 1.f);
     }
     GF_CHECK_LAUNCH();
+    // the mirrored K order of the first form: one K block of D1 = 64 H rows
+    const int mirror = (!wide && D1 % 64 == 0 && D1 <= kKR && dft_mirror_enabled()) ? D1 / 64 : 0;
     const dim3 sgrid((unsigned)nblk, KR / kKC);
     uint16_t *dB = B.as<uint16_t>();
     if (wide) {
-        if (fp16) k_split_projections<true, kWN, kWKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
-        else k_split_projections<false, kWN, kWKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
+        if (fp16) k_split_projections<true, kWN, kWKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, 0, d_scale, dB);
+        else k_split_projections<false, kWN, kWKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, 0, d_scale, dB);
     } else {
-        if (fp16) k_split_projections<true, kN, kKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
-        else k_split_projections<false, kN, kKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, d_scale, dB);
+        const int mm = mirror ? D1 / 2 : 0;
+        if (fp16) k_split_projections<true, kN, kKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, mm, d_scale, dB);
+        else k_split_projections<false, kN, kKR><<<sgrid, 256, 0, st>>>(d_proj, D1, D2, nnc, nkr, mm, d_scale, dB);
     }
     GF_CHECK_LAUNCH();
 
@@ -1201,6 +1267,7 @@ void dft_tcgen05(genfire_ctx *ctx, const double *d_proj, int D1, int D2, int n1,
     auto lg = [](int n) { int t = 0; while ((1 << t) < n) ++t; return (1 << t) == n ? t : -1; };
     a.log2n1 = lg(n1); a.log2n2 = lg(n2);
     a.nnc = nnc; a.nkr = nkr;
+    a.mirror = mirror;
     a.err = d_err;
     // GENFIRE_DEBUG_DFT_WAIT_CYCLES (a positive count of clock cycles) shortens
     // the pipeline's waits so that a test can make one expire and exercise the
