@@ -988,7 +988,7 @@ template <typename T> struct ReconT : ReconBase {
     FftPlan pl1, pl2;
     const cplx<T> *tw1, *tw2;
     DevBuf xbuf[2], xptrs, S, Y1, Y2, M, mask, tab, taboff, partial, ctl, changes, hist, dmeas, dR, dsums;
-    DevBuf rowmask;  // per CTA of the radix-32 row passes: any support voxel in its rows
+    DevBuf pairmask;  // per row pair of the row passes: any support voxel in its two rows
     DevBuf zmask;    // per slab of the box along dim 3: any support voxel in it
     double frac_rows = 1.0, frac_slabs = 1.0;  // the shares of those masks that are set
     DevBuf rtab, rtaboff, rcap, rvals, rshoff, rhist;  // Rfree monitor
@@ -1127,27 +1127,30 @@ template <typename T> struct ReconT : ReconBase {
             S.alloc(ns, st);
             if (support) GF_CUDA(cudaMemcpyAsync(S.p, support, ns, kind, st));
             else GF_CUDA(cudaMemsetAsync(S.p, 1, ns, st));
-            // the radix-32 row passes' CTAs (W row pairs each) that hold no
-            // support voxel; the object buffers are finite everywhere (the
-            // placement and the clear above), so rows the passes skip stay finite
-            if (sizeof(T) == 4 && (n1 == 512 || n1 == 1024) && rows_r32_enabled() && support) {
-                const int rows_per_cta = 2 * (n1 == 512 ? R32<512>::W : R32<1024>::W);
-                const int nrow = B2 * B3, ncta = (int)cdiv((nrow + 1) / 2, rows_per_cta / 2);
-                rowmask.alloc(ncta, st);
-                k_row_support_mask<<<ncta, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, rows_per_cta,
-                                                         rowmask.as<uint8_t>());
+            // the row pairs that hold no support voxel, for every row-pass
+            // engine (a CTA skips its rows when all of its pairs are empty);
+            // the object buffers are finite everywhere (the placement and the
+            // clear above), so rows the passes skip stay finite
+            if (support) {
+                const int nrow = B2 * B3, npairs = (nrow + 1) / 2;
+                pairmask.alloc(npairs, st);
+                k_row_support_mask<<<npairs, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, 2, pairmask.as<uint8_t>());
                 GF_CHECK_LAUNCH();
-                // slabs along dim 3 (the dim-2 passes' `other`): B2 rows each
-                zmask.alloc(B3, st);
-                k_row_support_mask<<<B3, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, B2, zmask.as<uint8_t>());
-                GF_CHECK_LAUNCH();
-                // the shares of set entries, for the passes' byte counts (profile)
-                std::vector<uint8_t> hr(ncta), hz(B3);
-                GF_CUDA(cudaMemcpyAsync(hr.data(), rowmask.p, ncta, cudaMemcpyDeviceToHost, st));
-                GF_CUDA(cudaMemcpyAsync(hz.data(), zmask.p, B3, cudaMemcpyDeviceToHost, st));
+                std::vector<uint8_t> hr(npairs);
+                GF_CUDA(cudaMemcpyAsync(hr.data(), pairmask.p, npairs, cudaMemcpyDeviceToHost, st));
+                // slabs along dim 3 (the radix-32 dim-2 passes' `other`): B2 rows each
+                std::vector<uint8_t> hz;
+                if (sizeof(T) == 4 && (n1 == 512 || n1 == 1024) && rows_r32_enabled()) {
+                    zmask.alloc(B3, st);
+                    k_row_support_mask<<<B3, 256, 0, st>>>(S.as<uint8_t>(), B1, nrow, B2, zmask.as<uint8_t>());
+                    GF_CHECK_LAUNCH();
+                    hz.resize(B3);
+                    GF_CUDA(cudaMemcpyAsync(hz.data(), zmask.p, B3, cudaMemcpyDeviceToHost, st));
+                }
                 GF_CUDA(cudaStreamSynchronize(st));
-                frac_rows = (double)std::count(hr.begin(), hr.end(), (uint8_t)1) / ncta;
-                frac_slabs = (double)std::count(hz.begin(), hz.end(), (uint8_t)1) / B3;
+                // the shares of set entries, for the passes' byte counts (profile)
+                frac_rows = (double)std::count(hr.begin(), hr.end(), (uint8_t)1) / npairs;
+                if (!hz.empty()) frac_slabs = (double)std::count(hz.begin(), hz.end(), (uint8_t)1) / B3;
             }
         }
         Y1.alloc(sizeof(cplx<T>) * (size_t)ld1 * B2 * B3, st);
@@ -1269,7 +1272,7 @@ template <typename T> struct ReconT : ReconBase {
         r.ctl = c;
         r.changes = changes.as<int>();
         r.support = p.constraintSupport ? S.as<uint8_t>() : nullptr;
-        r.rowmask = rowmask.as<uint8_t>();  // nullptr when not built
+        r.pairmask = pairmask.as<uint8_t>();  // nullptr when not built
         r.positivity = p.constraintPositivity;
         r.Y = Y1.as<cplx<T>>();
         r.scale = (T)1;
@@ -1294,7 +1297,7 @@ template <typename T> struct ReconT : ReconBase {
         q.support = nullptr;
         // the R-factor monitor projects this pass's raw output, so with it on
         // every row is written
-        q.rowmask = p.monitor_R == 1 ? nullptr : rowmask.as<uint8_t>();
+        q.pairmask = p.monitor_R == 1 ? nullptr : pairmask.as<uint8_t>();
         q.positivity = 0;
         q.scale = (T)(1.0 / ((double)n1 * n2 * n1));
         launch_rows<T>(q, false, st);

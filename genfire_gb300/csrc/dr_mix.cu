@@ -154,6 +154,10 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_row_r2c_mix(RowPas
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
     const int vc = c * N1;
     if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
+    if (row_pairs_empty(a, W)) {
+        zero_half_rows(a, W);
+        return;
+    }
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     cplx<T> v[N1][8];
@@ -196,6 +200,7 @@ __global__ void __launch_bounds__(mix_threads<T, N2, N1>()) k_row_c2r_mix(RowPas
     cplx<T> *sB = sA + Lay::SIZE;
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
     const int vc = c * N1;
+    if (row_pairs_empty(a, W)) return;
     T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     // pack the two half spectra of the pair: each thread takes q = j, j + N2/8, ...

@@ -589,10 +589,10 @@ template <typename T> struct RowPassArgs {
     T *xs[2];
     const int *xsel;
     const uint8_t *support;  // box-shaped support mask, nullptr for none
-    // radix-32 row passes: per CTA, nonzero when one of its rows holds a
-    // support voxel; F1 writes zero half spectra for the other CTAs and I1
-    // skips them (nullptr: every CTA works)
-    const uint8_t *rowmask;
+    // per row pair, nonzero when one of its two rows holds a support voxel;
+    // a CTA whose row pairs are all zero writes zero half spectra (forward) or
+    // nothing (inverse: set only when nothing else reads that output)
+    const uint8_t *pairmask;
     int positivity;
     cplx<T> *Y;        // ld1 x nrows half spectrum
     T scale;           // inverse only
@@ -602,6 +602,29 @@ template <typename T> struct RowPassArgs {
     const int *changes;
 };
 
+// The CTA's row pairs [blockIdx.x W, (blockIdx.x + 1) W) hold no support voxel
+// (RowPassArgs::pairmask); every thread reaches the same answer.
+template <typename T> __device__ __forceinline__ bool row_pairs_empty(const RowPassArgs<T> &a, int W)
+{
+    if (!a.pairmask) return false;
+    const int npairs = (a.nrows + 1) / 2;
+    for (int c = 0; c < W; ++c) {
+        const int p = blockIdx.x * W + c;
+        if (p < npairs && a.pairmask[p]) return false;
+    }
+    return true;
+}
+// A forward row pass's output for such a CTA: its rows are zero after the
+// support constraint, and so are their half spectra.
+template <typename T> __device__ __forceinline__ void zero_half_rows(const RowPassArgs<T> &a, int W)
+{
+    const int r0 = blockIdx.x * W * 2;
+    for (int i = threadIdx.x; i < 2 * W * a.h1; i += blockDim.x) {
+        const int rr = i / a.h1, q = i - rr * a.h1;
+        if (r0 + rr < a.nrows) a.Y[(long long)(r0 + rr) * a.ld1 + q] = mk((T)0, (T)0);
+    }
+}
+
 // forward: real rows (after positivity and support, reconstruct.m:126-131) -> half spectrum
 template <typename T>
 __global__ void __launch_bounds__(kTileMaxThreads<T>) k_rows_r2c(RowPassArgs<T> a)
@@ -610,6 +633,10 @@ __global__ void __launch_bounds__(kTileMaxThreads<T>) k_rows_r2c(RowPassArgs<T> 
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     const int n = a.pl.n, W = a.W, P = a.P, tid = threadIdx.x, nt = blockDim.x;
     if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
+    if (row_pairs_empty(a, W)) {
+        zero_half_rows(a, W);
+        return;
+    }
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0base = blockIdx.x * W * 2;
     for (int i = tid; i < n * P; i += nt) s[i] = mk((T)0, (T)0);
@@ -655,6 +682,7 @@ __global__ void __launch_bounds__(kTileMaxThreads<T>) k_rows_c2r(RowPassArgs<T> 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);
     const int n = a.pl.n, W = a.W, P = a.P, tid = threadIdx.x, nt = blockDim.x;
+    if (row_pairs_empty(a, W)) return;
     T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0base = blockIdx.x * W * 2;
     for (int idx = tid; idx < W * a.h1; idx += nt) {

@@ -460,14 +460,8 @@ __global__ void __launch_bounds__(R32<N>::THREADS) k_row_r2c_r32(RowPassArgs<T> 
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     const bool ok0 = r0 < a.nrows, ok1 = r1 < a.nrows;
     const long long o0 = (long long)r0 * a.B1, o1 = o0 + a.B1;
-    if (a.rowmask && !a.rowmask[blockIdx.x]) {
-        // none of the CTA's rows holds a support voxel: after the support
-        // constraint they are zero, and so are their half spectra
-        cplx<T> *ya = a.Y + (long long)r0 * a.ld1, *yb = ya + a.ld1;
-        for (int q = t; q < a.h1; q += P) {
-            if (ok0) ya[q] = mk((T)0, (T)0);
-            if (ok1) yb[q] = mk((T)0, (T)0);
-        }
+    if (row_pairs_empty(a, W)) {
+        zero_half_rows(a, W);
         return;
     }
     cplx<T> x[32];
@@ -530,12 +524,12 @@ __global__ void __launch_bounds__(R32<N>::THREADS) k_row_r2c_r32(RowPassArgs<T> 
 template <typename T, int N, bool ZOUT>
 __global__ void __launch_bounds__(R32<N>::THREADS) k_row_c2r_r32(RowPassArgs<T> a)
 {
-    // the CTA's rows hold no support voxel: the next forward pass treats them
-    // as zero without reading them (the row mask is only set when nothing
-    // else reads this pass's output outside the support)
-    if (a.rowmask && !a.rowmask[blockIdx.x]) return;
     using G = R32<N>;
     constexpr int P = G::P, W = G::W;
+    // the CTA's rows hold no support voxel: the next forward pass treats them
+    // as zero without reading them (the mask is only set when nothing else
+    // reads this pass's output outside the support)
+    if (row_pairs_empty(a, W)) return;
     using RowLay = typename G::RowLay;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *s = reinterpret_cast<cplx<T> *>(smem_raw);

@@ -423,6 +423,10 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     cplx<T> *sB = sA + Lay::SIZE;
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
     if (a.ctl && blockIdx.x == 0 && threadIdx.x == 0) ctl_begin_update(a.ctl, a.changes);
+    if (row_pairs_empty(a, W)) {
+        zero_half_rows(a, W);
+        return;
+    }
     const T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     cplx<T> v[1][8];
@@ -457,6 +461,7 @@ __global__ void __launch_bounds__(N / 8 * reg_width<T>(N), kRegMinBlocks<T>) k_r
     cplx<T> *sA = reinterpret_cast<cplx<T> *>(smem_raw);
     cplx<T> *sB = sA + Lay::SIZE;
     const int c = threadIdx.x / TPC, j = threadIdx.x % TPC;
+    if (row_pairs_empty(a, W)) return;
     T *x = (a.xsel && *a.xsel) ? a.xs[1] : a.xs[0];
     const int r0 = (blockIdx.x * W + c) * 2, r1 = r0 + 1;
     // pack the two half spectra of the pair: each thread takes q = j, j + N/8, ...

@@ -171,26 +171,30 @@ def test_large_host_buffers_page_locked_or_not(lib, ctx, pinned):
     assert np.array_equal(rec2, ref)
 
 
-def test_support_masks_leave_the_reconstruction_unchanged(lib, ctx):
-    """At a 512^3 grid (the radix-32 passes) a sparse support lets F1 and F2 write
-    zeros for the box's rows and slabs without support voxels and I2 and I1 skip
-    them; only the R-factor monitor, which projects the raw iterate, turns the
-    skipping off.  The reconstruction and errK with the monitor on (every row and
-    slab produced) and off (masked) are identical, and the monitor's R-factors
-    are finite."""
-    D, P, n = 256, 2, 512
+@pytest.mark.parametrize("n,prec", [(512, "mixed"), (128, "mixed"), (128, "fp64"), (192, "mixed"), (100, "mixed")])
+def test_support_masks_leave_the_reconstruction_unchanged(lib, ctx, n, prec):
+    """A sparse support lets F1 write zero half spectra for the box's row pairs
+    without support voxels and I1 skip them, in every row-pass engine (radix-32
+    at 512^3, the register passes at 128^3 in FP32 and FP64, the mixed-radix
+    passes at 192^3, the generic passes at 100^3); at 512^3 the dim-2 passes
+    do the same for empty slabs.
+    Only the R-factor monitor, which projects the raw iterate, turns the
+    inverse skipping off.  The reconstruction and errK with the monitor on and
+    off are identical, and the monitor's R-factors are finite."""
+    D, P = n // 2, 2
     rng = np.random.default_rng(21)
-    M = np.zeros((n, n, n), np.complex64, order="F")
-    k = rng.integers(n // 2 - 60, n // 2 + 60, size=(3, 40000))
-    M[k[0], k[1], k[2]] = (rng.standard_normal(40000) + 1j * rng.standard_normal(40000)).astype(np.complex64)
+    M = np.zeros((n, n, n), np.complex64 if prec == "mixed" else np.complex128, order="F")
+    nk, w = 40000 * n // 512, 60 * n // 512
+    k = rng.integers(n // 2 - w, n // 2 + w, size=(3, nk))
+    M[k[0], k[1], k[2]] = rng.standard_normal(nk) + 1j * rng.standard_normal(nk)
     g = np.indices((D, D, D)) - D // 2
-    support = np.asfortranarray((g[0] ** 2 + g[1] ** 2 + (1.6 * g[2]) ** 2) <= 100 ** 2)
+    support = np.asfortranarray((g[0] ** 2 + g[1] ** 2 + (1.6 * g[2]) ** 2) <= (100 * D // 256) ** 2)
     projs = np.asfortranarray(rng.random((D, D, P)))
     angles = np.asfortranarray([[10.0, 20.0, 30.0], [50.0, -40.0, 70.0]])
     out = {}
     for mon in (0, 1):
         p = params(lib, D, D, P, oversamplingRatio=2.0, numIterations=6, constraintEnforcementMode=3,
-                   monitor_R=mon, monitorR_loopLength=3, vector3=(0, 0, 1), precision="mixed")
+                   monitor_R=mon, monitorR_loopLength=3, vector3=(0, 0, 1), precision=prec)
         out[mon] = ctx.reconstruct(p, M, support=support, projections=projs, angles=angles)
     rec0, errK0 = out[0][0], out[0][1]
     rec1, errK1, errR1 = out[1][0], out[1][1], out[1][2]
