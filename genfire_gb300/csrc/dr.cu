@@ -908,9 +908,10 @@ void rfree_candidates(genfire_ctx *ctx, const genfire_params &p, const void *M, 
 
 // Object in box coordinates from an initial object (D1 x D2 x D1) or zeros.
 // grid: x over e1, y = e2, z = e3
-// Row mask of the radix-32 row passes: mask[b] = 1 when one of rows
+// Support masks of the passes: mask[b] = 1 when one of rows
 // [rows_per_cta b, rows_per_cta (b + 1)) of the box-shaped support holds a
-// voxel.  One CTA per entry.
+// voxel (2 rows per entry: the row passes' pairs; B2 rows: the slabs along
+// dim 3 of the radix-32 dim-2 passes).  One CTA per entry.
 __global__ void __launch_bounds__(256) k_row_support_mask(const uint8_t *__restrict__ S, int B1, int nrows,
                                                           int rows_per_cta, uint8_t *__restrict__ mask)
 {

@@ -603,16 +603,18 @@ template <typename T> struct RowPassArgs {
 };
 
 // The CTA's row pairs [blockIdx.x W, (blockIdx.x + 1) W) hold no support voxel
-// (RowPassArgs::pairmask); every thread reaches the same answer.
+// (RowPassArgs::pairmask); every thread reaches the same answer.  The W loads
+// are independent (no early exit), so they cost one memory latency.
 template <typename T> __device__ __forceinline__ bool row_pairs_empty(const RowPassArgs<T> &a, int W)
 {
     if (!a.pairmask) return false;
     const int npairs = (a.nrows + 1) / 2;
+    int any = 0;
     for (int c = 0; c < W; ++c) {
         const int p = blockIdx.x * W + c;
-        if (p < npairs && a.pairmask[p]) return false;
+        if (p < npairs) any |= a.pairmask[p];
     }
-    return true;
+    return any == 0;
 }
 // A forward row pass's output for such a CTA: its rows are zero after the
 // support constraint, and so are their half spectra.

@@ -29,11 +29,12 @@ def pair_mask(S, B1, nrows):
 def cta_empty(mask, nrows, W, b):
     """row_pairs_empty for CTA b."""
     npairs = (nrows + 1) // 2
+    any_ = 0
     for c in range(W):
         p = b * W + c
-        if p < npairs and mask[p]:
-            return False
-    return True
+        if p < npairs:
+            any_ |= int(mask[p])
+    return any_ == 0
 
 
 def zero_writes(nrows, h1, ld1, W, b):
