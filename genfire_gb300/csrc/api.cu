@@ -136,12 +136,10 @@ genfire_status genfire_destroy(genfire_ctx *ctx)
     cudaSetDevice(ctx->device);
     // batches and reconstructions still alive use this context's stream: free them first
     while (!ctx->batches.empty()) gf::recon_batch_destroy(*ctx->batches.begin());
-    while (!ctx->recons.empty()) {
-        genfire_recon *r = *ctx->recons.begin();
-        ctx->recons.erase(r);
-        delete r->impl;
-        delete r;
-    }
+    // (recon_destroy lives where the reconstruction type is complete, so its
+    // destructor runs: a delete here, of an incomplete type, would free the
+    // object without releasing its device buffers and graph)
+    while (!ctx->recons.empty()) gf::recon_destroy(*ctx->recons.begin());
     if (ctx->stream) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
