@@ -44,6 +44,26 @@ static double now(void)
     return t.tv_sec + 1e-9 * t.tv_nsec;
 }
 
+/* host allocations: a failure ends the program with a message */
+static void *xmalloc(size_t n)
+{
+    void *p = malloc(n ? n : 1);
+    if (!p) {
+        fprintf(stderr, "genfire_run: out of host memory (%zu bytes)\n", n);
+        exit(1);
+    }
+    return p;
+}
+static void *xcalloc(size_t n, size_t size)
+{
+    void *p = calloc(n ? n : 1, size ? size : 1);
+    if (!p) {
+        fprintf(stderr, "genfire_run: out of host memory (%zu x %zu bytes)\n", n, size);
+        exit(1);
+    }
+    return p;
+}
+
 static uint64_t rng_state = 88172645463325252ull;
 static double urand(void)
 {
@@ -89,7 +109,7 @@ static int synthetic(int argc, char **argv)
 
     /* a few Gaussian blobs, projected with the library's projector */
     size_t nv = (size_t)D * D * D;
-    double *vol = calloc(nv, sizeof(double));
+    double *vol = xcalloc(nv, sizeof(double));
     for (int b = 0; b < 6; ++b) {
         double cx = (urand() - 0.5) * D * 0.5, cy = (urand() - 0.5) * D * 0.5, cz = (urand() - 0.5) * D * 0.5;
         for (int k = 0; k < D; ++k)
@@ -99,26 +119,26 @@ static int synthetic(int argc, char **argv)
                     vol[i + (size_t)D * (j + (size_t)D * k)] += exp(-(x * x + y * y + z * z) / 8.0);
                 }
     }
-    double *angles = malloc(sizeof(double) * 3 * P);
+    double *angles = xmalloc(sizeof(double) * 3 * P);
     for (int i = 0; i < P; ++i) {
         angles[i] = 360 * urand();
         angles[i + P] = -70 + 140 * urand();
         angles[i + 2 * P] = 360 * urand();
     }
-    double *projs = malloc(sizeof(double) * (size_t)D * D * P);
+    double *projs = xmalloc(sizeof(double) * (size_t)D * D * P);
     CHECK(genfire_project(ctx, GENFIRE_PREC_FP64, vol, D, D, D, P, angles, NULL, projs));
 
     size_t es = mixed ? sizeof(float) : sizeof(double);
-    void *M = malloc(2 * es * (size_t)n1 * n2 * n1);
-    int64_t *nk = malloc(sizeof(int64_t) * P);
+    void *M = xmalloc(2 * es * (size_t)n1 * n2 * n1);
+    int64_t *nk = xmalloc(sizeof(int64_t) * P);
     double t0 = now();
     CHECK(genfire_grid_dft(ctx, &p, projs, angles, M, NULL, nk));
     double t1 = now();
     int64_t tot = 0;
     for (int i = 0; i < P; ++i) tot += nk[i];
 
-    void *rec = malloc(es * nv);
-    double *errK = malloc(sizeof(double) * N);
+    void *rec = xmalloc(es * nv);
+    double *errK = xmalloc(sizeof(double) * N);
     double t2 = now();
     CHECK(genfire_reconstruct(ctx, &p, M, NULL, NULL, NULL, NULL, NULL, rec, errK, NULL, NULL, NULL));
     double t3 = now();
@@ -161,7 +181,7 @@ static int mat_copy(const char *in, const char *out)
     uint8_t *l = NULL;
     mat_var v = {a.name, a.ndims, a.dims, MAT_DOUBLE, a.re};
     if (a.is_logical) {
-        l = malloc(a.numel > 0 ? (size_t)a.numel : 1);
+        l = xmalloc(a.numel > 0 ? (size_t)a.numel : 1);
         for (int64_t i = 0; i < a.numel; ++i) l[i] = a.re[i] != 0;
         v.mx_class = MAT_LOGICAL;
         v.data = l;
@@ -207,18 +227,18 @@ static int staged(genfire_ctx *ctx, const genfire_params *p, const void *M, cons
     uint8_t *mask = NULL;
     int64_t *counts = NULL, *ind = NULL, *wcounts = NULL, *wind = NULL;
     if (nbins > 0) {
-        mask = malloc(N);
+        mask = xmalloc(N);
         for (size_t i = 0; i < N; ++i) {
             if (es == sizeof(float)) mask[i] = ((const float *)M)[2 * i] != 0 || ((const float *)M)[2 * i + 1] != 0;
             else mask[i] = ((const double *)M)[2 * i] != 0 || ((const double *)M)[2 * i + 1] != 0;
         }
-        counts = calloc(nbins, sizeof(int64_t));
+        counts = xcalloc(nbins, sizeof(int64_t));
         CHECK(genfire_rfree_candidates(ctx, p, M, 0, nbins, counts, NULL));
         int64_t tot = 0;
         for (int s = 0; s < nbins; ++s) tot += counts[s];
-        ind = malloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
-        wind = malloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
-        wcounts = calloc(nbins, sizeof(int64_t));
+        ind = xmalloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
+        wind = xmalloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
+        wcounts = xcalloc(nbins, sizeof(int64_t));
         CHECK(genfire_rfree_candidates(ctx, p, M, 0, nbins, counts, ind));
         int64_t o = 0, w = 0;
         for (int s = 0; s < nbins; o += counts[s], ++s) {
@@ -269,7 +289,7 @@ static int staged(genfire_ctx *ctx, const genfire_params *p, const void *M, cons
     }
     if (st == GENFIRE_OK) st = genfire_recon_result(r, rec, errK, NULL, NULL, NULL, 0);
     if (st == GENFIRE_OK && nbins > 0) {
-        *rfree_out = malloc(sizeof(double) * (size_t)nbins * (Nit > 0 ? Nit : 1));
+        *rfree_out = xmalloc(sizeof(double) * (size_t)nbins * (Nit > 0 ? Nit : 1));
         st = genfire_recon_rfree(r, NULL, *rfree_out);
     }
     genfire_recon_destroy(r);
@@ -342,7 +362,7 @@ int main(int argc, char **argv)
     const int P = p.NumProjs, D1 = p.Dim1, D2 = p.Dim2;
     if (an.dims[0] != P) { fprintf(stderr, "GENFIRE: Number of projections and Angles does not match!\n"); return 1; }
     if (an.dims[1] > 3) { fprintf(stderr, "GENFIRE: Input Angle 2nd dimenstions larger than three!\n"); return 1; }
-    double *angles = calloc(3 * (size_t)P, sizeof(double));
+    double *angles = xcalloc(3 * (size_t)P, sizeof(double));
     if (an.dims[1] == 1) memcpy(angles + P, an.re, sizeof(double) * P);  /* [0, theta, 0] */
     else memcpy(angles, an.re, sizeof(double) * 3 * P);
     const size_t nv = (size_t)D1 * D2 * D1;
@@ -357,11 +377,11 @@ int main(int argc, char **argv)
     if (p.griddingMethod > 2) { fprintf(stderr, "GENFIRE: Unrecognized gridding method.\n"); return 1; }
     const int mixed = p.precision != GENFIRE_PREC_FP64;
     const size_t es = mixed ? sizeof(float) : sizeof(double);
-    uint8_t *support = malloc(nv);
+    uint8_t *support = xmalloc(nv);
     for (size_t i = 0; i < nv; ++i) support[i] = sp.re ? sp.re[i] != 0 : 1;
     void *init = NULL;
     if (x0.re) {
-        init = malloc(es * nv);
+        init = xmalloc(es * nv);
         for (size_t i = 0; i < nv; ++i) {
             if (mixed) ((float *)init)[i] = (float)x0.re[i];
             else ((double *)init)[i] = x0.re[i];
@@ -379,7 +399,7 @@ int main(int argc, char **argv)
     /* runGridding (:172-186): measuredK (complex64 for MIXED, as the single
      * cast; complex128 in the FP64 drop-in) */
     printf("GENFIRE: Assembling Fourier grid...\n\n");
-    void *M = malloc(2 * es * (size_t)n1 * n2 * n1);
+    void *M = xmalloc(2 * es * (size_t)n1 * n2 * n1);
     double t0 = now();
     if (p.griddingMethod == 1) CHECK(genfire_grid_fft(ctx, &p, pj.re, angles, M, NULL, NULL));
     else CHECK(genfire_grid_dft(ctx, &p, pj.re, angles, M, NULL, NULL));
@@ -388,8 +408,8 @@ int main(int argc, char **argv)
     /* reconstruct (reconstruct.m:28-194) */
     printf("GENFIRE: Reconstructing... \n\n");
     const int N = p.numIterations;
-    void *rec = malloc(es * nv);
-    double *errK = malloc(sizeof(double) * (N > 0 ? N : 1));
+    void *rec = xmalloc(es * nv);
+    double *errK = xmalloc(sizeof(double) * (N > 0 ? N : 1));
     double *rfree = NULL;
     if (save_every <= 0 && nbins <= 0) {
         CHECK(genfire_reconstruct(ctx, &p, M, NULL, support, init, pj.re, angles, rec, errK, NULL, NULL, NULL));
@@ -401,12 +421,12 @@ int main(int argc, char **argv)
     printf("GENFIRE: Reconstruction completed in %.12g seconds.\n\n", round(10 * (t2 - t1)) / 10);
 
     /* Tian_calc_Rfactor_realspace (Genfire_test.m:47-48) and the saved results */
-    double *recd = malloc(sizeof(double) * nv);
+    double *recd = xmalloc(sizeof(double) * nv);
     for (size_t i = 0; i < nv; ++i) recd[i] = mixed ? ((float *)rec)[i] : ((double *)rec)[i];
     double Rtot = 0, Kmin = N > 0 ? errK[0] : 0;
     for (int i = 1; i < N; ++i) Kmin = errK[i] < Kmin ? errK[i] : Kmin;
-    double *Rarr = calloc(P, sizeof(double));
-    float *simu = calloc((size_t)D1 * D2 * P, sizeof(float));
+    double *Rarr = xcalloc(P, sizeof(double));
+    float *simu = xcalloc((size_t)D1 * D2 * P, sizeof(float));
     if (want_r)
         CHECK(genfire_rfactor_realspace(ctx, GENFIRE_PREC_FP64, recd, D1, D2, D1, pj.re, D1, D2, P, angles, Rarr, &Rtot,
                                         simu));
