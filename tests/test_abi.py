@@ -51,6 +51,71 @@ def test_params_layout_matches_header(lib):
         assert getattr(_lib.Params, f).offset == off, f
 
 
+def declared_prototypes():
+    """name -> (return type, [parameter types]) for every prototype of the header."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"//[^\n]*", "", txt)
+    out = {}
+    for ret, name, args in re.findall(r"([A-Za-z_][A-Za-z0-9_ \*]*?)\b(genfire_[a-z0-9_]+)\s*\(([^)]*)\)\s*;",
+                                      txt, flags=re.S):
+        params = [a.strip() for a in args.split(",") if a.strip() and a.strip() != "void"]
+        # drop the parameter name, keep array brackets as a pointer
+        types = []
+        for a in params:
+            is_array = "[" in a
+            a = re.sub(r"\[[^\]]*\]", "", a).strip()
+            t = re.sub(r"\b[A-Za-z_][A-Za-z0-9_]*$", "", a).strip()
+            types.append(t + (" *" if is_array else ""))
+        out[name] = (ret.strip(), types)
+    return out
+
+
+def _c_class(t):
+    """The calling-convention class of a C type of the header."""
+    t = t.replace("const", "").strip()
+    if "*" in t:
+        return "ptr"
+    return {"int32_t": "i32", "int": "i32", "genfire_status": "i32", "int64_t": "i64", "double": "f64"}[t]
+
+
+def _c_pointee(t):
+    """The pointee of a pointer type: a base type name, or 'ptr' for a pointer to a pointer."""
+    t = t.replace("const", "").strip()
+    assert t.endswith("*")
+    t = t[:-1].strip()
+    return "ptr" if "*" in t else t
+
+
+def test_ctypes_signatures_match_header(lib):
+    """The Python binding's ctypes table declares every entry point with the
+    header's parameter count and classes (pointer, 32-bit integer, 64-bit
+    integer, double), and a typed ctypes pointer points to the header's type."""
+    from genfire_gb300 import _lib
+    L = _lib.load()
+    protos = declared_prototypes()
+    assert sorted(protos) == declared_functions()
+    scalar = {C.c_int32: "i32", C.c_int: "i32", C.c_int64: "i64", C.c_double: "f64"}
+    pointee = {C.c_double: "double", C.c_float: "float", C.c_uint8: "uint8_t", C.c_int64: "int64_t",
+               C.c_int32: "int32_t", _lib.Params: "genfire_params", C.c_void_p: "ptr"}
+
+    def py_class(ct):
+        if ct in (C.c_void_p, C.c_char_p) or (isinstance(ct, type) and issubclass(ct, C._Pointer)):
+            return "ptr"
+        return scalar[ct]
+
+    for name, (ret, params) in protos.items():
+        f = getattr(L, name)
+        assert f.argtypes is not None, name
+        assert len(f.argtypes) == len(params), name
+        want_ret = "i32" if ret == "genfire_status" else _c_class(ret)
+        assert py_class(f.restype) == want_ret, name
+        for i, (ct, t) in enumerate(zip(f.argtypes, params)):
+            assert py_class(ct) == _c_class(t), (name, i, t)
+            if isinstance(ct, type) and issubclass(ct, C._Pointer):
+                assert pointee[ct._type_] == _c_pointee(t), (name, i, t)
+
+
 def test_abi_version_and_status_strings(lib):
     from genfire_gb300 import _lib
     L = _lib.load()
