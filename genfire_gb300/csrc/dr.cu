@@ -1111,7 +1111,7 @@ template <typename T> struct ReconT : ReconBase {
                 if (on_device) dinit = static_cast<const T *>(initial);
                 else {
                     init.alloc(nb, st);
-                    GF_CUDA(cudaMemcpyAsync(init.p, initial, nb, cudaMemcpyHostToDevice, st));
+                    copy_host(init.p, initial, nb, cudaMemcpyHostToDevice, st);
                     dinit = init.as<T>();
                 }
             }
@@ -1536,7 +1536,7 @@ template <typename T> struct ReconT : ReconBase {
                 xptrs.as<T *>(), ctl.as<Ctl>(), p.constraintSupport ? S.as<uint8_t>() : nullptr,
                 p.constraintPositivity, D1, D2, B1, B2, B3, dout);
             GF_CHECK_LAUNCH();
-            if (!on_device) GF_CUDA(cudaMemcpyAsync(rec, dout, sizeof(T) * nv, cudaMemcpyDeviceToHost, st));
+            if (!on_device) copy_host(rec, dout, sizeof(T) * nv, cudaMemcpyDeviceToHost, st);
         }
         if (errK) {
             if (on_device) GF_CUDA(cudaMemcpyAsync(errK, hist.p, sizeof(double) * it_done, cudaMemcpyDeviceToDevice, st));

@@ -132,10 +132,12 @@ void *genfire_stream(genfire_ctx *ctx);
  *   nk           NumProjs counts of gridded K-points per projection; NULL ok
  * Index sets are bit-exact with the FP32 selection of the reference
  * (:175-192) evaluated with a fixed operation order.  Host buffers of 64 MB
- * and more (measuredK, recIFFT here; measuredK and measuredK_mask in
- * genfire_reconstruct and a host genfire_recon_create) are page-locked with
- * cudaHostRegister for the duration of their copy and released before the
- * call returns; when registration fails the copy runs from pageable memory. */
+ * and more (measuredK, recIFFT here; measuredK, measuredK_mask and
+ * initialObject in genfire_reconstruct and a host genfire_recon_create; the
+ * reconstruction of genfire_reconstruct and a host genfire_recon_result) are
+ * page-locked with cudaHostRegister for the duration of their copy and
+ * released before the call returns; when registration fails the copy runs
+ * from pageable memory. */
 genfire_status genfire_grid_dft(genfire_ctx *ctx, const genfire_params *p,
                                 const double *projections, const double *angles,
                                 void *measuredK, void *recIFFT, int64_t *nk);
