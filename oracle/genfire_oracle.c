@@ -981,10 +981,22 @@ void orc_change_points(int N, int m, int *out)
  * rec_out: D1 x D2 x D1.  errK: numIterations.  errR/Rarr/Rarr2: per monitor
  * point (floor(N/loopLength), Rarr/Rarr2 NumProjs per point). */
 static double g_loop_seconds = 0.0;
+static double *g_iter_start = NULL;  /* wall time at the start of each iteration */
+static int g_iter_count = 0;
+static double g_loop_end = 0.0;
 
 /* Wall time of the iteration loop of the last orc_reconstruct call (the
  * setup before reconstruct.m:117 excluded). */
 double orc_last_loop_seconds(void) { return g_loop_seconds; }
+
+/* Wall time of iterations first+1 .. numIterations of the last
+ * orc_reconstruct call (the first `first` iterations as a warm-up); 0 when
+ * first is out of range. */
+double orc_last_loop_seconds_from(int first)
+{
+    if (first < 0 || first >= g_iter_count || !g_iter_start) return 0.0;
+    return g_loop_end - g_iter_start[first];
+}
 
 static double wall(void)
 {
@@ -1113,8 +1125,12 @@ int orc_reconstruct_rfree(const orc_params *prm, const double *measuredK, const 
     double *model = (double *)malloc(sizeof(double) * NV);
     double *bp = (double *)malloc(sizeof(double) * (size_t)D1 * D2);
 
+    free(g_iter_start);
+    g_iter_count = prm->numIterations > 0 ? prm->numIterations : 0;
+    g_iter_start = (double *)malloc(sizeof(double) * (g_iter_count ? g_iter_count : 1));
     double t_loop = wall();
     for (int it = 1; it <= prm->numIterations; ++it) {
+        if (g_iter_start) g_iter_start[it - 1] = wall();
         if (cur < m && it == changes[cur]) {
             int last = cur;
             for (int c = 0; c < m; ++c) if (changes[c] == it) last = c;
@@ -1186,7 +1202,8 @@ int orc_reconstruct_rfree(const orc_params *prm, const double *measuredK, const 
             ++nmon;
         }
     }
-    g_loop_seconds = wall() - t_loop;
+    g_loop_end = wall();
+    g_loop_seconds = g_loop_end - t_loop;
     /* reconstruction = My_stripzero(fftshift(best), [D1 D2 D1]) (:192) */
     for (int i3 = 0; i3 < D1; ++i3)
         for (int i2 = 0; i2 < D2; ++i2)

@@ -88,6 +88,8 @@ def lib():
         L.orc_rfree_candidates.argtypes = [C.c_int, C.c_int, dp, C.c_int, C.c_int, C.POINTER(C.c_int64)]
         L.orc_num_threads.restype = C.c_int
         L.orc_last_loop_seconds.restype = C.c_double
+        L.orc_last_loop_seconds_from.restype = C.c_double
+        L.orc_last_loop_seconds_from.argtypes = [C.c_int]
         _lib = L
     return _lib
 
@@ -425,6 +427,12 @@ def num_threads():
 def last_loop_seconds():
     """Wall time of the iteration loop of the last reconstruct() call."""
     return lib().orc_last_loop_seconds()
+
+
+def last_loop_seconds_from(first):
+    """Wall time of the iterations after the first `first` (a warm-up) of the
+    last reconstruct() call; 0 when `first` is not below its iteration count."""
+    return lib().orc_last_loop_seconds_from(int(first))
 
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -368,3 +368,19 @@ def test_symmetry_and_index_helpers_randomized(oracle):
         assert np.array_equal(oracle.stripzero(oracle.paddzero(v, big), ori), v)
 
     check()
+
+
+def test_loop_timer_after_warmup(oracle):
+    """The reference arm times the iterations after its warm-up ones: the time
+    from iteration `first` on is positive, shrinks as `first` grows, never
+    exceeds the whole loop's, and is 0 for an out-of-range start."""
+    prm = oracle.make_params(16, 16, 1, oversamplingRatio=2, numIterations=6)
+    M = np.zeros((32, 32, 32), complex, order="F")
+    M[16, 16, 16], M[17, 16, 16] = 1.0, 0.5
+    oracle.reconstruct(prm, M)
+    total = oracle.last_loop_seconds()
+    t = [oracle.last_loop_seconds_from(k) for k in range(6)]
+    assert all(x > 0 for x in t)
+    assert all(a >= b for a, b in zip(t, t[1:]))
+    assert t[0] <= total
+    assert oracle.last_loop_seconds_from(6) == 0 and oracle.last_loop_seconds_from(-1) == 0
