@@ -112,3 +112,28 @@ def test_gaussian_volume_is_analytic():
     v = synth.gaussian_volume(16, np.array([[0.0, 0.0, 0.0]]), [1.0], 1.5, dtype=np.float64)
     assert v[8, 8, 8] == pytest.approx(1.0)
     assert v[9, 8, 8] == pytest.approx(np.exp(-1 / (2 * 1.5 ** 2)))
+
+
+def test_product_path_fails_loudly_without_the_library(monkeypatch, tmp_path):
+    """Without libgenfire.so the package raises; it has no CPU fallback (the
+    oracle is never imported by the package)."""
+    from genfire_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "libgenfire.so"))
+    monkeypatch.setattr(GENFIRE_Reconstructor, "_ctx_cache", {})
+    with pytest.raises(RuntimeError, match="not built"):
+        _lib.Context(0)
+    G = _prepared(oversamplingRatio=2, DFT_doGPU=1).CheckPrepareData()
+    with pytest.raises(RuntimeError, match="not built"):
+        G.runGridding()
+
+
+def test_package_never_imports_the_oracle():
+    import re
+    root = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "genfire_gb300")
+    for dirpath, _, files in os.walk(root):
+        for f in files:
+            if f.endswith(".py"):
+                src = open(os.path.join(dirpath, f)).read()
+                assert not re.search(r"^\s*(from|import)\s+oracle\b", src, flags=re.M), f
+                assert "genfire_oracle" not in src and "oracle/" not in src, f
